@@ -1,0 +1,332 @@
+"""Benchmark: aligned cloud pairs/s on the full per-capture pipeline of one pair.
+
+Workload (one step = one pair): two synthetic Kinect-v1 captures, each a
+10-frame 640x480 uint16 burst -> zero-eliminated mean -> back-projection
+(~300k points, metres) -> VoxelGrid 1 mm -> StatisticalOutlierRemoval k=50,
+mul 1.0 -> NormalEstimation k=30 -> point-to-plane ICP (3 cm, <= 100
+iterations) of source onto target.  A pair counts as aligned when ICP
+converged and RMS |T_est p - T_gt p| over the source points is <= 1 mm.
+
+value: pairs/s with the depth bursts resident in HBM; e2e: the same through
+the host-pointer C-ABI entry (H2D copy of both bursts inside the timed region,
+D2H of the result).  L2 is flushed (256 MB write) between timed steps.
+--impl reference times the CPU restatement of the same pipeline (all host
+threads) on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "aligned cloud pairs/sec at ≤1 mm RMSE: proposal+ICP vs plain GPU ICP"
+WORKLOAD = ("burst(10x640x480 u16) ZE-mean -> back-projection -> VoxelGrid 1mm -> SOR k=50 mul=1 -> NE k=30 "
+            "-> point-to-plane ICP (20 deg + 3 cm, d_max 3 cm, <=100 it), 1 pair per step, plain GPU ICP "
+            "(identity initial guess, no learned proposal)")
+ICP = dict(max_correspondence_distance=0.03, max_iterations=100, transformation_epsilon=1e-8,
+           euclidean_fitness_epsilon=1e-6, point_to_plane=True)
+RMSE_LIMIT = 1e-3
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (median SM clock, throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.dev = device
+        self.rows: list[list[str]] = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def start(self):
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                           "--format=csv,noheader,nounits", "-lms", "200"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self._proc = None
+
+    def _read(self):
+        for line in self._proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self) -> dict:
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) > 8 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def make_inputs(seed: int = 1):
+    from lowcost3dreconstruction_gb300 import synthetic as S
+    pr = S.config1_pair(seed)
+    return pr
+
+
+def rmse_from_moments(T_est, T_gt, m1, m2, n) -> float:
+    """RMS |(T_est - T_gt) p| from the source's first/second moments."""
+    D = np.asarray(T_est, np.float64) - np.asarray(T_gt, np.float64)
+    A, b = D[:3, :3], D[:3, 3]
+    ms = np.trace(A @ m2 @ A.T) + 2.0 * b @ (A @ m1) + b @ b
+    return float(np.sqrt(max(ms, 0.0)))
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+# ---------------------------------------------------------------- GPU arm
+def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
+    import torch
+
+    from lowcost3dreconstruction_gb300 import _lib as L
+    from lowcost3dreconstruction_gb300.core import Context, xyz_of
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    pr = make_inputs(1 + rank)
+    ctx = Context(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    params = ctx.depth_params(L.KINECT_V1, 640, 480, frames=10, scale=0.001, depth_max=4000.0, normals=False)
+    icp_params = ctx.icp_params(**ICP)
+    frames = [np.ascontiguousarray(pr.src_frames), np.ascontiguousarray(pr.tgt_frames)]
+    d_frames = [torch.from_numpy(f.view(np.uint8).reshape(-1)).to(f"cuda:{dev}") for f in frames]
+    h_frames = [torch.from_numpy(f.view(np.uint8).reshape(-1)).pin_memory() for f in frames]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    stage_ms = {}
+
+    def capture(c, src_is_device: bool, k: int, timing: dict | None):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)] if timing is not None else None
+        with torch.cuda.stream(stream):
+            if ev: ev[0].record()
+            cl = (ctx.backproject_device(d_frames[k].data_ptr(), params) if src_is_device
+                  else ctx.backproject(h_frames[k].numpy().view(np.uint16), params))
+            if ev: ev[1].record()
+            v = ctx.voxel_grid(cl, 0.001)
+            if ev: ev[2].record()
+            inl, _, _ = ctx.sor(v, 50, 1.0)
+            if ev: ev[3].record()
+            nrm = ctx.normals(inl, 30)
+            if ev: ev[4].record()
+        if timing is not None:
+            stream.synchronize()
+            for name, a, b in (("backproject", 0, 1), ("voxel", 1, 2), ("sor", 2, 3), ("normals", 3, 4)):
+                timing[name] = timing.get(name, 0.0) + ev[a].elapsed_time(ev[b])
+        return nrm
+
+    def step(device_inputs: bool, timing: dict | None = None):
+        src = capture(ctx, device_inputs, 0, timing)
+        tgt = capture(ctx, device_inputs, 1, timing)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record()
+            res = ctx.icp(src, tgt, icp_params)
+            e1.record()
+        stream.synchronize()
+        if timing is not None:
+            timing["icp"] = timing.get("icp", 0.0) + e0.elapsed_time(e1)
+            timing["icp_iters"] = timing.get("icp_iters", 0) + res.iterations
+        return src, tgt, res
+
+    # moments of the source cloud for the RMSE check (outside the timed region)
+    src0, tgt0, res0 = step(True)
+    xs = xyz_of(src0.download()).astype(np.float64)
+    m1, m2, nsrc = xs.mean(0), (xs.T @ xs) / len(xs), len(xs)
+    ntgt = len(tgt0)
+    for _ in range(max(args.warmup, 3)):
+        step(True)
+        step(False)
+
+    def timed(device_inputs: bool, timing: dict | None):
+        aligned = 0
+        total_ms = 0.0
+        launches0 = ctx.launches
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ea.record(stream)
+            _, _, res = step(device_inputs, timing)
+            eb.record(stream)
+            eb.synchronize()
+            total_ms += ea.elapsed_time(eb)
+            r = rmse_from_moments(res.transform64, pr.T_gt, m1, m2, nsrc)
+            aligned += int(res.converged and r <= RMSE_LIMIT)
+        return aligned, total_ms, ctx.launches - launches0, r, res
+
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(dev)
+    clocks.start()
+    aligned, dev_ms, launches, last_rmse, last_res = timed(True, stage_ms)
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    e2e_aligned, e2e_ms, _, _, _ = timed(False, None)
+    if dist is not None:
+        dist.barrier()
+        t = torch.tensor([dev_ms, e2e_ms, float(aligned), float(e2e_aligned)], device=f"cuda:{dev}",
+                         dtype=torch.float64)
+        tmax = t.clone()
+        dist.all_reduce(tmax[:2], op=dist.ReduceOp.MAX)
+        dist.all_reduce(tmax[2:], op=dist.ReduceOp.SUM)
+        dev_ms, e2e_ms, aligned, e2e_aligned = [float(x) for x in tmax.tolist()]
+    if rank != 0:
+        ctx.close()
+        return None
+
+    steps_total = args.steps * world
+    value = aligned / (dev_ms / 1000.0)
+    e2e_value = e2e_aligned / (e2e_ms / 1000.0)
+    # Roofline of the dominant kernel: one ICP iteration (fused transform + exact
+    # 1-NN + correspondence terms + FP64 solve), time = ICP stage / iterations.
+    it = max(1, stage_ms.get("icp_iters", 1))
+    iter_ms = stage_ms["icp"] / it
+    nleaf = (ntgt + 31) // 32
+    bytes_per_iter = nsrc * 16 + ntgt * 16 + ntgt * 16 + nleaf * 32  # src xyz, tgt xyz, tgt normals, leaf boxes
+    pk = peaks()
+    achieved = bytes_per_iter / (iter_ms * 1e-3) / 1e9
+    ncu_traffic = None
+    tfile = ROOT / "profiles" / "icp_iteration_traffic.json"
+    if tfile.exists():
+        ncu_traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "points_src": nsrc, "points_tgt": ntgt, "l2": "flushed between steps "
+                   "(256 MB write)", "icp": ICP, "rmse_limit_m": RMSE_LIMIT, "pairs_aligned": int(aligned),
+                   "pairs_timed": steps_total, "last_rmse_m": last_rmse, "last_icp_iterations": last_res.iterations,
+                   "parallelism": f"replicas x{world}",
+                   "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stage_ms.items() if k != "icp_iters"},
+                   "icp_iterations_per_step": stage_ms.get("icp_iters", 0) / args.steps},
+        "roofline": {"kernel": "k_icp_iter (one fused ICP iteration)", "bound": "hbm",
+                     "achieved": round(achieved, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / pk["hbm_gbs"], 5), "peak_src": pk["src"],
+                     "algorithmic_bytes_per_launch": bytes_per_iter, "avg_launch_ms": round(iter_ms, 5),
+                     "traffic": ncu_traffic},
+        "e2e": {"value": round(e2e_value, 3), "unit": "pairs/s",
+                "h2d_bytes_per_step": int(sum(f.nbytes for f in frames)), "d2h_bytes_per_step": 4 * 16 + 8 * 16},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(pr, sample_pairs=1)
+    ctx.close()
+    return out
+
+
+# ------------------------------------------------------------ CPU (oracle)
+def cpu_pipeline(pr, threads: int):
+    from lowcost3dreconstruction_gb300 import synthetic as S
+    from oracle import oracle as O
+    O.set_threads(threads)
+    prm = O.bp_params(640, 480, scale=0.001, depth_max=4000.0, normals=False)
+    clouds = []
+    for fr in (pr.src_frames, pr.tgt_frames):
+        c = O.backproject_v1(O.ze_mean_u16(fr), prm)
+        v, _ = O.voxel_grid(c, 0.001)
+        _, keep, _ = O.sor(v, 50, 1.0)
+        clouds.append(O.normals(v[keep], 30))
+    r = O.icp(clouds[0], clouds[1], max_corr_dist=ICP["max_correspondence_distance"],
+              max_iterations=ICP["max_iterations"], transformation_epsilon=ICP["transformation_epsilon"],
+              euclidean_fitness_epsilon=ICP["euclidean_fitness_epsilon"], point_to_plane=True)
+    xs = np.c_[clouds[0]["x"], clouds[0]["y"], clouds[0]["z"]]
+    ok = r["converged"] and S.rmse(r["transform"], pr.T_gt, xs) <= RMSE_LIMIT
+    return ok, r
+
+
+def cpu_baseline(pr, sample_pairs: int = 1) -> dict:
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    aligned = 0
+    for _ in range(sample_pairs):
+        ok, _ = cpu_pipeline(pr, threads)
+        aligned += int(ok)
+    dt = time.perf_counter() - t0
+    return {"value": round(aligned / dt, 5), "unit": "pairs/s", "cores": threads, "kind": "port",
+            "sample": f"{sample_pairs} full pair(s) of the same workload through the CPU restatement "
+                      f"(own kd-tree, OpenMP over {threads} threads), {dt:.2f} s"}
+
+
+def reference_arm(args, rank: int) -> dict | None:
+    if rank != 0:
+        return None
+    pr = make_inputs(1)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup if args.warmup < 2 else 1):
+        cpu_pipeline(pr, threads)
+    t0 = time.perf_counter()
+    aligned = 0
+    for _ in range(args.steps):
+        ok, r = cpu_pipeline(pr, threads)
+        aligned += int(ok)
+    dt = time.perf_counter() - t0
+    v = aligned / dt
+    return {"impl": "reference", "metric": METRIC, "value": round(v, 5), "unit": "pairs/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * dt / args.steps, 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "icp": ICP, "last_iterations": r["iterations"]},
+            "cpu_baseline": {"value": round(v, 5), "unit": "pairs/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} pairs, each the full workload, CPU restatement of the "
+                                       f"reference path (PCL semantics), OpenMP over {threads} threads"},
+            "e2e": {"value": round(v, 5), "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    from lowcost3dreconstruction_gb300 import build
+    if args.impl == "reference":
+        build.build_oracle()
+        out = reference_arm(args, rank)
+    else:
+        build.build_lib()
+        build.build_oracle()
+        dist = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl")
+        out = gpu_arm(args, rank, world, dist)
+        if dist is not None:
+            dist.destroy_process_group()
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,244 @@
+/*
+ * liblcr -- C ABI of the GB300 (sm_103a) alignment path.
+ *
+ * The alignment path of LowCost3DReconstruction (scripts/alignment.sh and the
+ * pcl_tools it drives, plus the depth back-projection in capture/) runs here as
+ * hand-written CUDA kernels behind this plain C interface: POD arguments, host
+ * pointers and sizes, no C++ types and no exceptions across the boundary.  The
+ * PCL-shaped C++ facade (lcr_pcl.hpp) and the command-line tools are built on
+ * these entry points; other languages bind them with their FFI.
+ *
+ * Ownership: the caller owns every host array it passes; the library owns
+ * device clouds (lcr_cloud), which are immutable once created and are freed
+ * only by lcr_cloud_free.  A cloud caches its search index on first use.
+ * Threading: one lcr_ctx per host thread.  Each context owns one CUDA stream on
+ * its device; calls on one context are serialised on that stream; contexts are
+ * independent.  Every call returns after its results are complete unless the
+ * entry point says otherwise.
+ * Errors: every entry point returns an lcr_status; lcr_last_error() gives the
+ * message of the last failing call on that context.  There is no CPU fallback:
+ * without a usable CUDA device lcr_ctx_create fails with LCR_ERR_NO_DEVICE.
+ */
+#ifndef LCR_H
+#define LCR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define LCR_API __attribute__((visibility("default")))
+#else
+#define LCR_API
+#endif
+
+typedef enum lcr_status {
+  LCR_OK = 0,
+  LCR_ERR_INVALID_ARG = 1,      /* bad pointer, size or parameter */
+  LCR_ERR_EMPTY = 2,            /* input cloud has no (finite) points */
+  LCR_ERR_NO_CORRESPONDENCES = 3, /* ICP found fewer than 3 correspondences */
+  LCR_NOT_CONVERGED = 4,        /* non-fatal: result valid, criteria not met */
+  LCR_ERR_CUDA = 5,             /* a CUDA runtime call failed */
+  LCR_ERR_TIMEOUT = 6,          /* a bounded device wait expired */
+  LCR_ERR_OOM = 7,              /* device allocation failed */
+  LCR_ERR_IO = 8,               /* file could not be read or written */
+  LCR_ERR_TOO_FEW_POINTS = 9,   /* k neighbours requested from a cloud with <= k points */
+  LCR_ERR_NO_DEVICE = 10        /* no CUDA device */
+} lcr_status;
+
+/* Byte-compatible with pcl::PointXYZRGBNormal (48 bytes): x y z _ | nx ny nz _ |
+ * b g r a (PCL's packed rgba, little-endian) curvature _ _.  A PCL cloud's
+ * points.data() can be passed directly. */
+typedef struct lcr_point {
+  float x, y, z, pad0;
+  float normal_x, normal_y, normal_z, pad1;
+  uint8_t b, g, r, a;
+  float curvature;
+  float pad2[2];
+} lcr_point;
+
+typedef struct lcr_ctx lcr_ctx;
+typedef struct lcr_cloud lcr_cloud;
+
+/* ---------------------------------------------------------------- context */
+LCR_API lcr_status lcr_ctx_create(lcr_ctx** ctx, int device);
+LCR_API void lcr_ctx_destroy(lcr_ctx* ctx);
+LCR_API const char* lcr_last_error(const lcr_ctx* ctx);
+LCR_API const char* lcr_status_string(lcr_status s);
+LCR_API lcr_status lcr_ctx_synchronize(lcr_ctx* ctx);
+/* The context's cudaStream_t (as void*), for callers that order their own work
+ * after the library's. */
+LCR_API void* lcr_ctx_stream(lcr_ctx* ctx);
+/* Number of kernels this context has launched (graph launches count each
+ * kernel node executed per launch as reported by the graph's own counter). */
+LCR_API uint64_t lcr_ctx_launch_count(const lcr_ctx* ctx);
+
+/* ----------------------------------------------------------------- clouds */
+/* Replaces pcl::io::loadPLYFile + the PointCloud<PointXYZRGBNormal> a tool
+ * holds (e.g. pcl_tools/fine_registration.cpp:94-102). */
+LCR_API lcr_status lcr_cloud_upload(lcr_ctx* ctx, const lcr_point* pts, size_t n, lcr_cloud** out);
+/* Same from a plain xyz array (n*3 floats); normals, rgb and curvature are 0. */
+LCR_API lcr_status lcr_cloud_upload_xyz(lcr_ctx* ctx, const float* xyz, size_t n, lcr_cloud** out);
+/* Same from device memory: lcr_point records already on the context's device. */
+LCR_API lcr_status lcr_cloud_from_device(lcr_ctx* ctx, const void* d_pts, size_t n, lcr_cloud** out);
+LCR_API size_t lcr_cloud_size(const lcr_cloud* c);
+/* Copies min(n, capacity) points out; returns LCR_ERR_INVALID_ARG if capacity < n. */
+LCR_API lcr_status lcr_cloud_download(lcr_ctx* ctx, const lcr_cloud* c, lcr_point* out, size_t capacity);
+LCR_API void lcr_cloud_free(lcr_ctx* ctx, lcr_cloud* c);
+/* a followed by b (PointCloud operator+, e.g. accumulate_clouds.cpp:121-123). */
+LCR_API lcr_status lcr_cloud_concat(lcr_ctx* ctx, const lcr_cloud* a, const lcr_cloud* b, lcr_cloud** out);
+
+/* ------------------------------------------------------- back-projection */
+enum { LCR_DEPTH_KINECT_V1 = 0, LCR_DEPTH_KINECT_V2 = 1 };
+
+typedef struct lcr_depth_params {
+  int model;                 /* LCR_DEPTH_KINECT_V1 (uint16 mm) or LCR_DEPTH_KINECT_V2 (float32 mm) */
+  int width, height;
+  int frames;                /* burst length F >= 1; frames are fused by the zero-eliminated mean */
+  double fx, fy, cx, cy;     /* intrinsics */
+  double depth_min, depth_max; /* kept depth range in mm, inclusive */
+  int roi_left, roi_right, roi_top, roi_bottom; /* kept pixel window, inclusive */
+  double scale;              /* output units per mm (1: mm as the reference writes, 0.001: metres) */
+  int normals;               /* V1 only: 1 = image-gradient normals of depth_capture.cpp:231-265 */
+  uint8_t r, g, b, pad;      /* constant colour (super_resolution.cpp:114 writes 128,128,128) */
+} lcr_depth_params;
+
+/* Burst fusion + back-projection: F frames of width*height depth (frame-major,
+ * row-major) -> cloud of the kept pixels in row-major pixel order.
+ * Replaces capture/super_resolution/super_resolution.cpp:295-309 (ZE mean) and
+ * save_ply (:33-126), capture/depth_capture/depth_capture.cpp:216-317, and
+ * capture/depth_capture_kv2/kinect2.h:144-201 + depth_capture_kv2.cpp:224-256
+ * (V2: reprojection ROI + scale).  depth is a host pointer. */
+LCR_API lcr_status lcr_backproject(lcr_ctx* ctx, const void* depth, const lcr_depth_params* p, lcr_cloud** out);
+/* Same with the depth frames already on the context's device. */
+LCR_API lcr_status lcr_backproject_device(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p,
+                                          lcr_cloud** out);
+/* The fused (zero-eliminated mean) depth image alone, host in/out: uint16 for
+ * V1 (super_resolution.cpp:295-315), float for V2 (super_resolution_kv2.cpp:287-303). */
+LCR_API lcr_status lcr_burst_fuse(lcr_ctx* ctx, const void* frames, const lcr_depth_params* p, void* fused_out);
+
+/* --------------------------------------------------------------- filters */
+/* pcl::VoxelGrid<PointXYZRGBNormal> (pcl_tools/cloud_downsampling.cpp:73-76). */
+LCR_API lcr_status lcr_voxel_grid(lcr_ctx* ctx, const lcr_cloud* in, float leaf_x, float leaf_y, float leaf_z,
+                                  lcr_cloud** out);
+
+typedef struct lcr_sor_stats {
+  double mean, stddev, threshold;
+  size_t valid, kept, removed;
+} lcr_sor_stats;
+
+/* pcl::StatisticalOutlierRemoval (pcl_tools/outlier_removal.cpp:80-84 and the
+ * setNegative(true) pass :91-93).  inliers / outliers may each be NULL. */
+LCR_API lcr_status lcr_sor(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_cloud** inliers,
+                           lcr_cloud** outliers, lcr_sor_stats* stats);
+/* Per-point mean neighbour distance of the SOR first pass (host output, n floats). */
+LCR_API lcr_status lcr_sor_distances(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, float* distances,
+                                     lcr_sor_stats* stats);
+
+enum { LCR_NORMALS_FLIP_ALL = 1 };
+/* pcl::NormalEstimation with k neighbours and a viewpoint
+ * (pcl_tools/normal_estimation.cpp:84-118).  flags LCR_NORMALS_FLIP_ALL negates
+ * every normal afterwards (the tool's centroid XOR reverse rule :112-118).
+ * Output: the input cloud with normal_x/y/z and curvature replaced. */
+LCR_API lcr_status lcr_normals(lcr_ctx* ctx, const lcr_cloud* in, int k, const float viewpoint[3], int flags,
+                               lcr_cloud** out);
+
+/* ------------------------------------------------------------------- ICP */
+enum { LCR_ICP_POINT_TO_POINT = 0, LCR_ICP_POINT_TO_PLANE = 1 };
+
+typedef struct lcr_icp_params {
+  double max_correspondence_distance;   /* fine_registration.cpp:112 (default 0.1) */
+  int max_iterations;                   /* :114 (default 50) */
+  double transformation_epsilon;        /* :116 (default 1e-9) */
+  double euclidean_fitness_epsilon;     /* :118 (default 0.001) */
+  int method;                           /* LCR_ICP_POINT_TO_POINT (the tool's) or _TO_PLANE */
+  int compute_fitness;                  /* 1: run getFitnessScore() after align (default) */
+} lcr_icp_params;
+
+enum {
+  LCR_ICP_STATE_NOT_CONVERGED = 0,
+  LCR_ICP_STATE_ITERATIONS = 1,
+  LCR_ICP_STATE_TRANSFORM = 2,
+  LCR_ICP_STATE_ABS_MSE = 3,
+  LCR_ICP_STATE_REL_MSE = 4,
+  LCR_ICP_STATE_NO_CORRESPONDENCES = 5
+};
+
+typedef struct lcr_icp_result {
+  float transform[16];       /* row-major final transformation (getFinalTransformation) */
+  double transform64[16];    /* the same in FP64 */
+  int converged;             /* hasConverged() */
+  int iterations;
+  int state;                 /* LCR_ICP_STATE_* */
+  int n_correspondences;     /* of the last iteration */
+  double fitness;            /* getFitnessScore() */
+  double mse;                /* mean squared correspondence distance of the last iteration */
+} lcr_icp_result;
+
+LCR_API void lcr_icp_params_default(lcr_icp_params* p);
+/* pcl::IterativeClosestPoint::align + getFinalTransformation + hasConverged +
+ * getFitnessScore (pcl_tools/fine_registration.cpp:105-126).  guess may be
+ * NULL (identity).  registered (may be NULL) receives the source transformed
+ * by the final transformation, normals rotated (:121, :129). */
+LCR_API lcr_status lcr_icp(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr_icp_params* p,
+                           const float guess[16], lcr_icp_result* res, lcr_cloud** registered);
+
+/* One correspondence pass (for parity tests): source transformed by T
+ * (row-major FP64, applied in FP32), exact nearest target within the maximum
+ * distance; idx -1 when none.  Host outputs of length n_src. */
+LCR_API lcr_status lcr_correspondences(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const double T[16],
+                                       double max_correspondence_distance, int32_t* idx, float* dist);
+
+/* Exact k nearest neighbours of every query point in ref (squared FP32
+ * distance as FLANN computes it, ties to the lower index).  max_dist_sq < 0:
+ * uncapped.  Host outputs n_query*k, missing entries idx -1, dist +inf. */
+LCR_API lcr_status lcr_knn(lcr_ctx* ctx, const lcr_cloud* ref, const lcr_cloud* query, int k, float max_dist_sq,
+                           int32_t* idx, float* dist);
+
+/* ------------------------------------------------------------ accumulate */
+enum { LCR_ACCUM_ALL = 1 };
+/* accumulate_clouds (pcl_tools/accumulate_clouds.cpp:100-127): drop source
+ * points inside the cube [q-r, q+r] of any target point q, clean the rest by
+ * SOR(k, std_mul), output target followed by the remaining source.
+ * LCR_ACCUM_ALL skips the crop and the SOR (:100).  remaining (may be NULL)
+ * receives the remaining source (the --negative file, :130-134). */
+LCR_API lcr_status lcr_accumulate(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, double radius, int k,
+                                  double std_mul, int flags, lcr_cloud** out, lcr_cloud** remaining);
+/* The crop predicate alone: removed[i] = 1 for redundant source points (host, n_src bytes). */
+LCR_API lcr_status lcr_crop_redundant(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, double radius,
+                                      uint8_t* removed);
+
+/* ---------------------------------------------------- transforms, centroid */
+/* pcl::transformPointCloudWithNormals with a row-major 4x4 (pcl_tools/transform.cpp:90,
+ * scale.cpp:70 with diag(s,s,s,1), and inside every ICP iteration). */
+LCR_API lcr_status lcr_transform(lcr_ctx* ctx, const lcr_cloud* in, const float m[16], lcr_cloud** out);
+/* pcl::compute3DCentroid (pcl_tools/centroid_align.cpp:105-109), FP64 accumulation. */
+LCR_API lcr_status lcr_centroid(lcr_ctx* ctx, const lcr_cloud* in, float centroid[4]);
+/* centroid_align (centroid_align.cpp:102-130): move the source centroid to the
+ * origin, rotate by R_x(roll) R_y(pitch) R_z(yaw) (degrees), move to the target
+ * centroid and add `elevation` along y.  Returns the transformed source and the
+ * composed 4x4 (row-major). */
+LCR_API lcr_status lcr_centroid_align(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, double roll,
+                                      double pitch, double yaw, double elevation, lcr_cloud** out,
+                                      float transform[16]);
+
+/* ----------------------------------------------------------------- PLY I/O */
+/* pcl::io::loadPLYFile<PointXYZRGBNormal> (e.g. pcl_tools/fine_registration.cpp:94):
+ * ascii or binary PLY, any vertex layout; *pts is malloc'ed, release with
+ * lcr_free.  Host only, no context or GPU needed. */
+LCR_API lcr_status lcr_ply_read(const char* path, lcr_point** pts, size_t* n);
+/* pcl::io::savePLYFileBinary (e.g. fine_registration.cpp:129): binary=1 writes
+ * binary_little_endian, 0 ascii.  Fields x y z red green blue normal_x normal_y
+ * normal_z curvature. */
+LCR_API lcr_status lcr_ply_write(const char* path, const lcr_point* pts, size_t n, int binary);
+/* Message of the last failing PLY call on this thread. */
+LCR_API const char* lcr_ply_last_error(void);
+LCR_API void lcr_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LCR_H */

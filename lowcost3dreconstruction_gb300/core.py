@@ -1,0 +1,260 @@
+"""Python host API over liblcr: a context owning a CUDA stream and device
+clouds, and one method per C-ABI entry point.  Arrays cross as numpy arrays of
+POINT_DTYPE records (the 48-byte pcl::PointXYZRGBNormal layout)."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import POINT_DTYPE, LcrError
+
+
+def points_from_xyz(xyz: np.ndarray, normals: np.ndarray | None = None, rgb: np.ndarray | None = None,
+                    curvature: np.ndarray | None = None) -> np.ndarray:
+    xyz = np.asarray(xyz, dtype=np.float32).reshape(-1, 3)
+    out = np.zeros(len(xyz), dtype=POINT_DTYPE)
+    out["x"], out["y"], out["z"] = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+    if normals is not None:
+        n = np.asarray(normals, dtype=np.float32).reshape(-1, 3)
+        out["normal_x"], out["normal_y"], out["normal_z"] = n[:, 0], n[:, 1], n[:, 2]
+    if rgb is not None:
+        c = np.asarray(rgb, dtype=np.uint8).reshape(-1, 3)
+        out["r"], out["g"], out["b"] = c[:, 0], c[:, 1], c[:, 2]
+    if curvature is not None:
+        out["curvature"] = np.asarray(curvature, dtype=np.float32)
+    return out
+
+
+def xyz_of(pts: np.ndarray) -> np.ndarray:
+    return np.stack([pts["x"], pts["y"], pts["z"]], axis=1)
+
+
+def normals_of(pts: np.ndarray) -> np.ndarray:
+    return np.stack([pts["normal_x"], pts["normal_y"], pts["normal_z"]], axis=1)
+
+
+@dataclass
+class IcpOutcome:
+    transform: np.ndarray      # (4, 4) float32, row-major
+    transform64: np.ndarray    # (4, 4) float64
+    converged: bool
+    iterations: int
+    state: int
+    n_correspondences: int
+    fitness: float
+    mse: float
+    status: int
+
+
+class Cloud:
+    """A device-resident cloud (immutable; caches its search index)."""
+
+    def __init__(self, ctx: "Context", handle: C.c_void_p):
+        self._ctx = ctx
+        self.handle = handle
+
+    def __len__(self) -> int:
+        return int(self._ctx.lib.lcr_cloud_size(self.handle))
+
+    def download(self) -> np.ndarray:
+        n = len(self)
+        out = np.zeros(n, dtype=POINT_DTYPE)
+        self._ctx._check(self._ctx.lib.lcr_cloud_download(self._ctx.h, self.handle, L.ptr(out), n))
+        return out
+
+    def free(self) -> None:
+        if self.handle and self._ctx.h:
+            self._ctx.lib.lcr_cloud_free(self._ctx.h, self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    """One CUDA stream on one device (lcr_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = L.load()
+        h = C.c_void_p()
+        st = self.lib.lcr_ctx_create(C.byref(h), device)
+        if st != L.OK:
+            raise LcrError(st, self.lib.lcr_status_string(st).decode())
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.lcr_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------ plumbing
+    def _check(self, st: int, allow: tuple[int, ...] = ()) -> int:
+        if st != L.OK and st not in allow:
+            raise LcrError(st, self.lib.lcr_last_error(self.h).decode())
+        return st
+
+    def _cloud(self, fn, *args) -> Cloud:
+        out = C.c_void_p()
+        self._check(fn(self.h, *args, C.byref(out)))
+        return Cloud(self, out)
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.lcr_ctx_stream(self.h) or 0)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.lcr_ctx_launch_count(self.h))
+
+    def synchronize(self) -> None:
+        self._check(self.lib.lcr_ctx_synchronize(self.h))
+
+    # ------------------------------------------------------------- clouds
+    def upload(self, pts: np.ndarray) -> Cloud:
+        pts = np.ascontiguousarray(pts, dtype=POINT_DTYPE)
+        return self._cloud(self.lib.lcr_cloud_upload, L.ptr(pts), len(pts))
+
+    def upload_xyz(self, xyz: np.ndarray) -> Cloud:
+        xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+        return self._cloud(self.lib.lcr_cloud_upload_xyz, L.ptr(xyz), len(xyz))
+
+    def from_device(self, dev_ptr: int, n: int) -> Cloud:
+        return self._cloud(self.lib.lcr_cloud_from_device, C.c_void_p(dev_ptr), n)
+
+    def concat(self, a: Cloud, b: Cloud) -> Cloud:
+        return self._cloud(self.lib.lcr_cloud_concat, a.handle, b.handle)
+
+    # ------------------------------------------------------ back-projection
+    @staticmethod
+    def depth_params(model: int, width: int, height: int, frames: int = 1, fx: float = 525.0, fy: float = 525.0,
+                     cx: float = 319.5, cy: float = 239.5, depth_min: float = 0.0, depth_max: float = 65535.0,
+                     roi: tuple[int, int, int, int] | None = None, scale: float = 1.0, normals: bool = True,
+                     rgb: tuple[int, int, int] = (128, 128, 128)) -> L.DepthParams:
+        left, right, top, bottom = roi if roi is not None else (0, width - 1, 0, height - 1)
+        return L.DepthParams(model, width, height, frames, fx, fy, cx, cy, depth_min, depth_max, left, right, top,
+                             bottom, scale, 1 if normals else 0, rgb[0], rgb[1], rgb[2], 0)
+
+    def backproject(self, depth: np.ndarray, params: L.DepthParams) -> Cloud:
+        want = np.uint16 if params.model == L.KINECT_V1 else np.float32
+        depth = np.ascontiguousarray(depth, dtype=want)
+        assert depth.size == params.width * params.height * params.frames
+        return self._cloud(self.lib.lcr_backproject, L.ptr(depth), C.byref(params))
+
+    def backproject_device(self, dev_ptr: int, params: L.DepthParams) -> Cloud:
+        return self._cloud(self.lib.lcr_backproject_device, C.c_void_p(dev_ptr), C.byref(params))
+
+    def burst_fuse(self, frames: np.ndarray, params: L.DepthParams) -> np.ndarray:
+        want = np.uint16 if params.model == L.KINECT_V1 else np.float32
+        frames = np.ascontiguousarray(frames, dtype=want)
+        out = np.zeros((params.height, params.width), dtype=want)
+        self._check(self.lib.lcr_burst_fuse(self.h, L.ptr(frames), C.byref(params), L.ptr(out)))
+        return out
+
+    # -------------------------------------------------------------- filters
+    def voxel_grid(self, cloud: Cloud, leaf: float | tuple[float, float, float]) -> Cloud:
+        lx, ly, lz = (leaf, leaf, leaf) if np.isscalar(leaf) else leaf
+        return self._cloud(self.lib.lcr_voxel_grid, cloud.handle, lx, ly, lz)
+
+    def sor(self, cloud: Cloud, mean_k: int, std_mul: float, want_outliers: bool = False):
+        inl, outl = C.c_void_p(), C.c_void_p()
+        stats = L.SorStats()
+        self._check(self.lib.lcr_sor(self.h, cloud.handle, mean_k, std_mul, C.byref(inl),
+                                     C.byref(outl) if want_outliers else None, C.byref(stats)))
+        return Cloud(self, inl), (Cloud(self, outl) if want_outliers else None), stats
+
+    def sor_distances(self, cloud: Cloud, mean_k: int) -> tuple[np.ndarray, L.SorStats]:
+        out = np.zeros(len(cloud), dtype=np.float32)
+        stats = L.SorStats()
+        self._check(self.lib.lcr_sor_distances(self.h, cloud.handle, mean_k, L.ptr(out), C.byref(stats)))
+        return out, stats
+
+    def normals(self, cloud: Cloud, k: int, viewpoint=(0.0, 0.0, 0.0), flip_all: bool = False) -> Cloud:
+        vp = np.asarray(viewpoint, dtype=np.float32)
+        return self._cloud(self.lib.lcr_normals, cloud.handle, k, L.ptr(vp), L.NORMALS_FLIP_ALL if flip_all else 0)
+
+    # ------------------------------------------------------------------ ICP
+    @staticmethod
+    def icp_params(max_correspondence_distance: float = 0.1, max_iterations: int = 50,
+                   transformation_epsilon: float = 1e-9, euclidean_fitness_epsilon: float = 0.001,
+                   point_to_plane: bool = False, compute_fitness: bool = True) -> L.IcpParams:
+        return L.IcpParams(max_correspondence_distance, max_iterations, transformation_epsilon,
+                           euclidean_fitness_epsilon, L.ICP_POINT_TO_PLANE if point_to_plane else L.ICP_POINT_TO_POINT,
+                           1 if compute_fitness else 0)
+
+    def icp(self, src: Cloud, tgt: Cloud, params: L.IcpParams, guess: np.ndarray | None = None,
+            want_registered: bool = False):
+        res = L.IcpResult()
+        reg = C.c_void_p()
+        g = None if guess is None else np.ascontiguousarray(guess, dtype=np.float32).reshape(16)
+        st = self._check(self.lib.lcr_icp(self.h, src.handle, tgt.handle, C.byref(params),
+                                          L.ptr(g) if g is not None else None, C.byref(res),
+                                          C.byref(reg) if want_registered else None),
+                         allow=(L.NO_CORRESPONDENCES,))
+        out = IcpOutcome(np.array(res.transform, dtype=np.float32).reshape(4, 4),
+                         np.array(res.transform64, dtype=np.float64).reshape(4, 4), bool(res.converged),
+                         res.iterations, res.state, res.n_correspondences, res.fitness, res.mse, st)
+        return (out, Cloud(self, reg)) if want_registered else out
+
+    def correspondences(self, src: Cloud, tgt: Cloud, T: np.ndarray, max_dist: float):
+        n = len(src)
+        idx = np.zeros(n, dtype=np.int32)
+        dist = np.zeros(n, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float64).reshape(16)
+        self._check(self.lib.lcr_correspondences(self.h, src.handle, tgt.handle, L.ptr(T), max_dist, L.ptr(idx),
+                                                 L.ptr(dist)))
+        return idx, dist
+
+    def knn(self, ref: Cloud, query: Cloud, k: int, max_dist_sq: float = -1.0):
+        n = len(query)
+        idx = np.zeros((n, k), dtype=np.int32)
+        dist = np.zeros((n, k), dtype=np.float32)
+        self._check(self.lib.lcr_knn(self.h, ref.handle, query.handle, k, max_dist_sq, L.ptr(idx), L.ptr(dist)))
+        return idx, dist
+
+    # ----------------------------------------------------------- accumulate
+    def crop_redundant(self, src: Cloud, tgt: Cloud, radius: float) -> np.ndarray:
+        out = np.zeros(len(src), dtype=np.uint8)
+        self._check(self.lib.lcr_crop_redundant(self.h, src.handle, tgt.handle, radius, L.ptr(out)))
+        return out
+
+    def accumulate(self, src: Cloud, tgt: Cloud, radius: float = 0.05, k: int = 50, std_mul: float = 1.0,
+                   all_points: bool = False):
+        out, rem = C.c_void_p(), C.c_void_p()
+        self._check(self.lib.lcr_accumulate(self.h, src.handle, tgt.handle, radius, k, std_mul,
+                                            L.ACCUM_ALL if all_points else 0, C.byref(out), C.byref(rem)))
+        return Cloud(self, out), Cloud(self, rem)
+
+    # ------------------------------------------------- transforms, centroid
+    def transform(self, cloud: Cloud, m: np.ndarray) -> Cloud:
+        m = np.ascontiguousarray(m, dtype=np.float32).reshape(16)
+        return self._cloud(self.lib.lcr_transform, cloud.handle, L.ptr(m))
+
+    def centroid(self, cloud: Cloud) -> np.ndarray:
+        c = np.zeros(4, dtype=np.float32)
+        self._check(self.lib.lcr_centroid(self.h, cloud.handle, L.ptr(c)))
+        return c
+
+    def centroid_align(self, src: Cloud, tgt: Cloud, roll=0.0, pitch=0.0, yaw=0.0, elevation=0.0):
+        out = C.c_void_p()
+        m = np.zeros(16, dtype=np.float32)
+        self._check(self.lib.lcr_centroid_align(self.h, src.handle, tgt.handle, roll, pitch, yaw, elevation,
+                                                C.byref(out), L.ptr(m)))
+        return Cloud(self, out), m.reshape(4, 4)

@@ -1,0 +1,456 @@
+// The C ABI (include/lcr.h).  Every entry point validates its arguments,
+// selects the context's device, runs on the context stream and converts
+// internal errors into an lcr_status plus a message (lcr_last_error).
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "lcr_internal.cuh"
+
+namespace {
+
+#define API_BEGIN(ctx)                                \
+  if (!(ctx)) return LCR_ERR_INVALID_ARG;             \
+  try {                                               \
+    CUDA_TRY(cudaSetDevice((ctx)->device));
+
+#define API_END(ctx)                                                   \
+  }                                                                    \
+  catch (const LcrError& e) {                                          \
+    (ctx)->last_error = e.msg;                                         \
+    return e.st;                                                       \
+  }                                                                    \
+  catch (const std::bad_alloc&) {                                      \
+    (ctx)->last_error = "host allocation failed";                      \
+    return LCR_ERR_OOM;                                                \
+  }                                                                    \
+  catch (...) {                                                        \
+    (ctx)->last_error = "unknown error";                               \
+    return LCR_ERR_CUDA;                                               \
+  }
+
+#define REQUIRE(cond, ...)                                  \
+  do {                                                      \
+    if (!(cond)) LCR_THROW(LCR_ERR_INVALID_ARG, __VA_ARGS__); \
+  } while (0)
+
+__global__ void k_invert(const uint8_t* __restrict__ in, size_t n, uint8_t* __restrict__ out) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[i] ? 0 : 1;
+}
+
+void check_depth(const lcr_depth_params* p) {
+  REQUIRE(p, "null depth parameters");
+  REQUIRE(p->model == LCR_DEPTH_KINECT_V1 || p->model == LCR_DEPTH_KINECT_V2, "unknown depth model %d", p->model);
+  REQUIRE(p->width > 0 && p->height > 0 && static_cast<long long>(p->width) * p->height < (1LL << 31),
+          "bad image size %dx%d", p->width, p->height);
+  REQUIRE(p->frames >= 1 && p->frames <= 4096, "frames must be in [1, 4096]");
+  REQUIRE(p->fx != 0 && p->fy != 0, "zero focal length");
+}
+
+size_t depth_bytes(const lcr_depth_params* p) {
+  return static_cast<size_t>(p->width) * p->height * p->frames * (p->model == LCR_DEPTH_KINECT_V1 ? 2 : 4);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lcr_status_string(lcr_status s) {
+  switch (s) {
+    case LCR_OK: return "ok";
+    case LCR_ERR_INVALID_ARG: return "invalid argument";
+    case LCR_ERR_EMPTY: return "empty cloud";
+    case LCR_ERR_NO_CORRESPONDENCES: return "not enough correspondences";
+    case LCR_NOT_CONVERGED: return "not converged";
+    case LCR_ERR_CUDA: return "CUDA error";
+    case LCR_ERR_TIMEOUT: return "device wait timed out";
+    case LCR_ERR_OOM: return "out of memory";
+    case LCR_ERR_IO: return "I/O error";
+    case LCR_ERR_TOO_FEW_POINTS: return "too few points for k neighbours";
+    case LCR_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+lcr_status lcr_ctx_create(lcr_ctx** out, int device) {
+  if (!out) return LCR_ERR_INVALID_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return LCR_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= count) return LCR_ERR_INVALID_ARG;
+  lcr_ctx* ctx = new (std::nothrow) lcr_ctx();
+  if (!ctx) return LCR_ERR_OOM;
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return LCR_ERR_CUDA;
+  }
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  cudaGetLastError();
+  *out = ctx;
+  return LCR_OK;
+}
+
+void lcr_ctx_destroy(lcr_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (int m = 0; m < 2; ++m)
+    if (ctx->icp_exec[m]) cudaGraphExecDestroy(ctx->icp_exec[m]);
+  if (ctx->icp_block) cudaFree(ctx->icp_block);
+  if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  cudaStreamDestroy(ctx->stream);
+  cudaGetLastError();
+  delete ctx;
+}
+
+const char* lcr_last_error(const lcr_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+lcr_status lcr_ctx_synchronize(lcr_ctx* ctx) {
+  API_BEGIN(ctx)
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+void* lcr_ctx_stream(lcr_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
+
+uint64_t lcr_ctx_launch_count(const lcr_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+// ------------------------------------------------------------------ clouds
+lcr_status lcr_cloud_upload(lcr_ctx* ctx, const lcr_point* pts, size_t n, lcr_cloud** out) {
+  API_BEGIN(ctx)
+  REQUIRE(out && (pts || n == 0), "null argument");
+  REQUIRE(n < (1u << 31), "cloud too large");
+  *out = upload_records(ctx, pts, n, false);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_cloud_upload_xyz(lcr_ctx* ctx, const float* xyz, size_t n, lcr_cloud** out) {
+  API_BEGIN(ctx)
+  REQUIRE(out && (xyz || n == 0), "null argument");
+  REQUIRE(n < (1u << 31), "cloud too large");
+  *out = upload_xyz(ctx, xyz, n);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_cloud_from_device(lcr_ctx* ctx, const void* d_pts, size_t n, lcr_cloud** out) {
+  API_BEGIN(ctx)
+  REQUIRE(out && (d_pts || n == 0), "null argument");
+  REQUIRE(n < (1u << 31), "cloud too large");
+  *out = upload_records(ctx, d_pts, n, true);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+size_t lcr_cloud_size(const lcr_cloud* c) { return c ? c->n : 0; }
+
+lcr_status lcr_cloud_download(lcr_ctx* ctx, const lcr_cloud* c, lcr_point* out, size_t capacity) {
+  API_BEGIN(ctx)
+  REQUIRE(c && (out || c->n == 0), "null argument");
+  REQUIRE(capacity >= c->n, "capacity %zu < cloud size %zu", capacity, c->n);
+  download_records(ctx, c, out);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+void lcr_cloud_free(lcr_ctx* ctx, lcr_cloud* c) {
+  if (!ctx || !c) return;
+  try {
+    cudaSetDevice(ctx->device);
+    cloud_release(ctx, c);
+  } catch (...) {
+  }
+}
+
+lcr_status lcr_cloud_concat(lcr_ctx* ctx, const lcr_cloud* a, const lcr_cloud* b, lcr_cloud** out) {
+  API_BEGIN(ctx)
+  REQUIRE(a && b && out, "null argument");
+  *out = concat_clouds(ctx, a, b);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+// --------------------------------------------------------- back-projection
+lcr_status lcr_backproject_device(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p, lcr_cloud** out) {
+  API_BEGIN(ctx)
+  check_depth(p);
+  REQUIRE(d_depth && out, "null argument");
+  backproject_run(ctx, d_depth, p, out);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_backproject(lcr_ctx* ctx, const void* depth, const lcr_depth_params* p, lcr_cloud** out) {
+  API_BEGIN(ctx)
+  check_depth(p);
+  REQUIRE(depth && out, "null argument");
+  const size_t bytes = depth_bytes(p);
+  void* d = dev_alloc(ctx, bytes);
+  CUDA_TRY(cudaMemcpyAsync(d, depth, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  backproject_run(ctx, d, p, out);
+  dev_free(ctx, d);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_burst_fuse(lcr_ctx* ctx, const void* frames, const lcr_depth_params* p, void* fused_out) {
+  API_BEGIN(ctx)
+  check_depth(p);
+  REQUIRE(frames && fused_out, "null argument");
+  const size_t bytes = depth_bytes(p);
+  const size_t obytes = bytes / p->frames;
+  char* d = static_cast<char*>(dev_alloc(ctx, bytes + obytes));
+  CUDA_TRY(cudaMemcpyAsync(d, frames, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  burst_fuse_run(ctx, d, p, d + bytes);
+  CUDA_TRY(cudaMemcpyAsync(fused_out, d + bytes, obytes, cudaMemcpyDeviceToHost, ctx->stream));
+  dev_free(ctx, d);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+// ----------------------------------------------------------------- filters
+lcr_status lcr_voxel_grid(lcr_ctx* ctx, const lcr_cloud* in, float lx, float ly, float lz, lcr_cloud** out) {
+  API_BEGIN(ctx)
+  REQUIRE(in && out, "null argument");
+  *out = voxel_run(ctx, in, lx, ly, lz);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_sor(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_cloud** inliers,
+                   lcr_cloud** outliers, lcr_sor_stats* stats) {
+  API_BEGIN(ctx)
+  REQUIRE(in, "null argument");
+  if (inliers) *inliers = nullptr;
+  if (outliers) *outliers = nullptr;
+  sor_run(ctx, in, mean_k, std_mul, inliers, outliers, stats, nullptr);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_sor_distances(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, float* distances, lcr_sor_stats* stats) {
+  API_BEGIN(ctx)
+  REQUIRE(in && distances, "null argument");
+  lcr_sor_stats local;
+  sor_run(ctx, in, mean_k, 1.0, nullptr, nullptr, stats ? stats : &local, distances);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_normals(lcr_ctx* ctx, const lcr_cloud* in, int k, const float viewpoint[3], int flags,
+                       lcr_cloud** out) {
+  API_BEGIN(ctx)
+  REQUIRE(in && out, "null argument");
+  const float zero[3] = {0.f, 0.f, 0.f};
+  *out = normals_run(ctx, in, k, viewpoint ? viewpoint : zero, flags);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+// --------------------------------------------------------------------- ICP
+void lcr_icp_params_default(lcr_icp_params* p) {
+  if (!p) return;
+  p->max_correspondence_distance = 0.1;
+  p->max_iterations = 50;
+  p->transformation_epsilon = 1e-9;
+  p->euclidean_fitness_epsilon = 0.001;
+  p->method = LCR_ICP_POINT_TO_POINT;
+  p->compute_fitness = 1;
+}
+
+lcr_status lcr_icp(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr_icp_params* p,
+                   const float guess[16], lcr_icp_result* res, lcr_cloud** registered) {
+  lcr_status st = LCR_OK;
+  API_BEGIN(ctx)
+  REQUIRE(src && tgt && p && res, "null argument");
+  REQUIRE(p->method == LCR_ICP_POINT_TO_POINT || p->method == LCR_ICP_POINT_TO_PLANE, "unknown ICP method");
+  if (registered) *registered = nullptr;
+  icp_run(ctx, src, tgt, p, guess, res);
+  if (registered) *registered = transform_run(ctx, src, res->transform);
+  sync(ctx);
+  if (res->state == LCR_ICP_STATE_NO_CORRESPONDENCES) {
+    ctx->last_error = "not enough correspondences found";
+    st = LCR_ERR_NO_CORRESPONDENCES;
+  }
+  API_END(ctx)
+  return st;
+}
+
+lcr_status lcr_correspondences(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const double T[16],
+                               double max_correspondence_distance, int32_t* idx, float* dist) {
+  API_BEGIN(ctx)
+  REQUIRE(src && tgt && T && idx && dist, "null argument");
+  const size_t n = src->n;
+  if (n) {
+    char* d = static_cast<char*>(dev_alloc(ctx, n * 8));
+    corr_run(ctx, src, tgt, T, max_correspondence_distance, reinterpret_cast<int32_t*>(d),
+             reinterpret_cast<float*>(d + n * 4));
+    CUDA_TRY(cudaMemcpyAsync(idx, d, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(dist, d + n * 4, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    dev_free(ctx, d);
+  }
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_knn(lcr_ctx* ctx, const lcr_cloud* ref, const lcr_cloud* query, int k, float max_dist_sq,
+                   int32_t* idx, float* dist) {
+  API_BEGIN(ctx)
+  REQUIRE(ref && query && idx && dist, "null argument");
+  REQUIRE(k >= 1 && k <= 512, "k must be in [1, 512]");
+  const size_t m = query->n * static_cast<size_t>(k);
+  if (m) {
+    char* d = static_cast<char*>(dev_alloc(ctx, m * 8));
+    const float cap = max_dist_sq < 0 ? LCR_INF_HOST : max_dist_sq;
+    knn_run(ctx, ref, query, k, cap, reinterpret_cast<int32_t*>(d), reinterpret_cast<float*>(d + m * 4));
+    CUDA_TRY(cudaMemcpyAsync(idx, d, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(dist, d + m * 4, m * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    dev_free(ctx, d);
+  }
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+// -------------------------------------------------------------- accumulate
+lcr_status lcr_crop_redundant(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, double radius,
+                              uint8_t* removed) {
+  API_BEGIN(ctx)
+  REQUIRE(src && tgt && (removed || src->n == 0), "null argument");
+  REQUIRE(radius >= 0, "negative radius");
+  if (src->n) {
+    uint8_t* d = static_cast<uint8_t*>(dev_alloc(ctx, src->n));
+    crop_run(ctx, src, tgt, radius, d);
+    CUDA_TRY(cudaMemcpyAsync(removed, d, src->n, cudaMemcpyDeviceToHost, ctx->stream));
+    dev_free(ctx, d);
+  }
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_accumulate(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, double radius, int k,
+                          double std_mul, int flags, lcr_cloud** out, lcr_cloud** remaining) {
+  API_BEGIN(ctx)
+  REQUIRE(src && tgt && out, "null argument");
+  REQUIRE(radius >= 0 && k > 0, "bad radius or k");
+  lcr_cloud empty;
+  lcr_cloud* rem = nullptr;
+  if (flags & LCR_ACCUM_ALL) {
+    rem = concat_clouds(ctx, src, &empty);
+  } else {
+    const size_t n = src->n;
+    uint8_t* removed = static_cast<uint8_t*>(dev_alloc(ctx, 2 * n + 16));
+    uint8_t* keep = removed + n;
+    uint32_t* idx = static_cast<uint32_t*>(dev_alloc(ctx, 4 * n + 16));
+    crop_run(ctx, src, tgt, radius, removed);
+    int nk = 0;
+    if (n) {
+      LCR_LAUNCH(ctx, k_invert, static_cast<unsigned>((n + 255) / 256), 256, 0, removed, n, keep);
+      nk = compact_flags(ctx, keep, static_cast<int>(n), idx);
+    }
+    lcr_cloud* rem0 = cloud_alloc(ctx, nk);
+    gather_cloud(ctx, src, idx, nk, rem0);
+    dev_free(ctx, removed);
+    dev_free(ctx, idx);
+    // The reference's SOR reads past its results with <= k points; the cleaning
+    // pass is skipped for such small remainders.
+    if (nk > k) {
+      lcr_cloud* inl = nullptr;
+      sor_run(ctx, rem0, k, std_mul, &inl, nullptr, nullptr, nullptr);
+      cloud_release(ctx, rem0);
+      rem = inl;
+    } else {
+      rem = rem0;
+    }
+  }
+  *out = concat_clouds(ctx, tgt, rem);
+  if (remaining) *remaining = rem;
+  else cloud_release(ctx, rem);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+// --------------------------------------------------- transforms, centroid
+lcr_status lcr_transform(lcr_ctx* ctx, const lcr_cloud* in, const float m[16], lcr_cloud** out) {
+  API_BEGIN(ctx)
+  REQUIRE(in && m && out, "null argument");
+  *out = transform_run(ctx, in, m);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_centroid(lcr_ctx* ctx, const lcr_cloud* in, float centroid[4]) {
+  API_BEGIN(ctx)
+  REQUIRE(in && centroid, "null argument");
+  double c4[4];
+  centroid_run(ctx, in, c4);
+  if (c4[3] == 0) LCR_THROW(LCR_ERR_EMPTY, "centroid of a cloud without finite points");
+  for (int i = 0; i < 3; ++i) centroid[i] = static_cast<float>(c4[i]);
+  centroid[3] = 1.f;
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_centroid_align(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, double roll, double pitch,
+                              double yaw, double elevation, lcr_cloud** out, float transform[16]) {
+  API_BEGIN(ctx)
+  REQUIRE(src && tgt && out, "null argument");
+  double cs[4], ct[4];
+  centroid_run(ctx, src, cs);
+  centroid_run(ctx, tgt, ct);
+  if (cs[3] == 0 || ct[3] == 0) LCR_THROW(LCR_ERR_EMPTY, "centroid_align needs non-empty clouds");
+  const double d2r = 3.14159265358979323846 / 180.0;
+  const double a = roll * d2r, b = pitch * d2r, c = yaw * d2r;
+  const double Rx[9] = {1, 0, 0, 0, std::cos(a), -std::sin(a), 0, std::sin(a), std::cos(a)};
+  const double Ry[9] = {std::cos(b), 0, std::sin(b), 0, 1, 0, -std::sin(b), 0, std::cos(b)};
+  const double Rz[9] = {std::cos(c), -std::sin(c), 0, std::sin(c), std::cos(c), 0, 0, 0, 1};
+  double Rxy[9], R[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      Rxy[3 * i + j] = Rx[3 * i] * Ry[j] + Rx[3 * i + 1] * Ry[3 + j] + Rx[3 * i + 2] * Ry[6 + j];
+    }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[3 * i + j] = Rxy[3 * i] * Rz[j] + Rxy[3 * i + 1] * Rz[3 + j] + Rxy[3 * i + 2] * Rz[6 + j];
+  // p' = R (p - c_s) + c_t + (0, e, 0)
+  float m[16];
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) m[4 * i + j] = static_cast<float>(R[3 * i + j]);
+    const double t = ct[i] + (i == 1 ? elevation : 0.0) - (R[3 * i] * cs[0] + R[3 * i + 1] * cs[1] + R[3 * i + 2] * cs[2]);
+    m[4 * i + 3] = static_cast<float>(t);
+  }
+  m[12] = m[13] = m[14] = 0.f;
+  m[15] = 1.f;
+  *out = transform_run(ctx, src, m);
+  if (transform) std::memcpy(transform, m, sizeof(m));
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,223 @@
+// Context, device memory, cloud storage and the elementwise cloud kernels
+// (pack/unpack of PCL records, rigid transform with normals, centroid).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "lcr_internal.cuh"
+
+// ------------------------------------------------------------------ memory
+void* dev_alloc(lcr_ctx* ctx, size_t bytes) {
+  void* p = nullptr;
+  if (bytes == 0) bytes = 16;
+  CUDA_TRY(cudaMallocAsync(&p, bytes, ctx->stream));
+  return p;
+}
+
+void dev_free(lcr_ctx* ctx, void* p) {
+  if (p) CUDA_TRY(cudaFreeAsync(p, ctx->stream));
+}
+
+void* pinned(lcr_ctx* ctx, size_t bytes) {
+  if (bytes > ctx->pinned_bytes) {
+    sync(ctx);
+    if (ctx->pinned) CUDA_TRY(cudaFreeHost(ctx->pinned));
+    ctx->pinned = nullptr;
+    const size_t want = std::max<size_t>(bytes, 1 << 16);
+    CUDA_TRY(cudaMallocHost(&ctx->pinned, want));
+    ctx->pinned_bytes = want;
+  }
+  return ctx->pinned;
+}
+
+void sync(lcr_ctx* ctx) { CUDA_TRY(cudaStreamSynchronize(ctx->stream)); }
+
+lcr_cloud* cloud_alloc(lcr_ctx* ctx, size_t n) {
+  lcr_cloud* c = new lcr_cloud();
+  c->n = n;
+  const size_t m = std::max<size_t>(n, 1);
+  char* blk = static_cast<char*>(dev_alloc(ctx, m * (16 + 16 + 4) + 512));
+  c->xyz = reinterpret_cast<float4*>(blk);
+  c->nrm = reinterpret_cast<float4*>(blk + m * 16);
+  c->rgb = reinterpret_cast<uint32_t*>(blk + m * 32);
+  return c;
+}
+
+void cloud_release(lcr_ctx* ctx, lcr_cloud* c) {
+  if (!c) return;
+  free_index(ctx, c->index);
+  dev_free(ctx, c->xyz);
+  delete c;
+}
+
+const Index& cloud_index(lcr_ctx* ctx, const lcr_cloud* c) {
+  if (!c->index) const_cast<lcr_cloud*>(c)->index = build_index(ctx, c->xyz, static_cast<int>(c->n));
+  return *c->index;
+}
+
+// ----------------------------------------------------------------- kernels
+namespace {
+
+struct __align__(16) Sum4 {
+  double x, y, z, w;
+};
+
+// lcr_point (48 B) = float4 {x y z _} + float4 {nx ny nz _} + float4 {rgba curvature _ _}
+__global__ void k_unpack(const float4* __restrict__ rec, size_t n, float4* __restrict__ xyz, float4* __restrict__ nrm,
+                         uint32_t* __restrict__ rgb) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 a = rec[3 * i], b = rec[3 * i + 1], c = rec[3 * i + 2];
+  xyz[i] = make_float4(a.x, a.y, a.z, 0.f);
+  nrm[i] = make_float4(b.x, b.y, b.z, c.y);
+  rgb[i] = __float_as_uint(c.x);
+}
+
+__global__ void k_pack(const float4* __restrict__ xyz, const float4* __restrict__ nrm, const uint32_t* __restrict__ rgb,
+                       size_t n, float4* __restrict__ rec) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = xyz[i], q = nrm[i];
+  rec[3 * i] = make_float4(p.x, p.y, p.z, 1.f);
+  rec[3 * i + 1] = make_float4(q.x, q.y, q.z, 0.f);
+  rec[3 * i + 2] = make_float4(__uint_as_float(rgb[i]), q.w, 0.f, 0.f);
+}
+
+__global__ void k_from_xyz(const float* __restrict__ in, size_t n, float4* __restrict__ xyz, float4* __restrict__ nrm,
+                           uint32_t* __restrict__ rgb) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  xyz[i] = make_float4(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.f);
+  nrm[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  rgb[i] = 0u;
+}
+
+// transformPointCloudWithNormals: p' = M p (x,y,z,1), n' = M3x3 n; non-finite
+// points are copied unchanged.
+__global__ void k_transform(const float4* __restrict__ xyz, const float4* __restrict__ nrm,
+                            const uint32_t* __restrict__ rgb, size_t n, Xf T, float4* __restrict__ oxyz,
+                            float4* __restrict__ onrm, uint32_t* __restrict__ orgb) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = xyz[i], q = nrm[i];
+  float4 op = p, oq = q;
+  if (finite3(p.x, p.y, p.z)) {
+    const float3 a = xf_apply(T, p.x, p.y, p.z);
+    const float3 b = xf_rotate(T, q.x, q.y, q.z);
+    op = make_float4(a.x, a.y, a.z, 0.f);
+    oq = make_float4(b.x, b.y, b.z, q.w);
+  }
+  oxyz[i] = op;
+  onrm[i] = oq;
+  orgb[i] = rgb[i];
+}
+
+// FP64 centroid: per-block partial sums (x, y, z, count) then one block adds the
+// partials in block order (deterministic).
+__global__ void k_centroid_partial(const float4* __restrict__ xyz, size_t n, Sum4* __restrict__ part) {
+  __shared__ Sum4 ws[8];
+  double sx = 0, sy = 0, sz = 0, c = 0;
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const float4 p = xyz[i];
+    if (!finite3(p.x, p.y, p.z)) continue;
+    sx += p.x; sy += p.y; sz += p.z; c += 1.0;
+  }
+  sx = warp_sum(sx); sy = warp_sum(sy); sz = warp_sum(sz); c = warp_sum(c);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = Sum4{sx, sy, sz, c};
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Sum4 s = Sum4{0, 0, 0, 0};
+    for (int j = 0; j < static_cast<int>(blockDim.x >> 5); ++j) {
+      s.x += ws[j].x; s.y += ws[j].y; s.z += ws[j].z; s.w += ws[j].w;
+    }
+    part[blockIdx.x] = s;
+  }
+}
+
+__global__ void k_centroid_final(const Sum4* __restrict__ part, int nb, double* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  Sum4 s = Sum4{0, 0, 0, 0};
+  for (int j = 0; j < nb; ++j) {
+    s.x += part[j].x; s.y += part[j].y; s.z += part[j].z; s.w += part[j].w;
+  }
+  const double c = s.w > 0 ? s.w : 1.0;
+  out[0] = s.x / c;
+  out[1] = s.y / c;
+  out[2] = s.z / c;
+  out[3] = s.w;
+}
+
+}  // namespace
+
+lcr_cloud* upload_records(lcr_ctx* ctx, const void* recs, size_t n, bool device_src) {
+  lcr_cloud* c = cloud_alloc(ctx, n);
+  if (n == 0) return c;
+  float4* tmp = nullptr;
+  const float4* src = static_cast<const float4*>(recs);
+  if (!device_src) {
+    tmp = static_cast<float4*>(dev_alloc(ctx, n * sizeof(lcr_point)));
+    CUDA_TRY(cudaMemcpyAsync(tmp, recs, n * sizeof(lcr_point), cudaMemcpyHostToDevice, ctx->stream));
+    src = tmp;
+  }
+  LCR_LAUNCH(ctx, k_unpack, static_cast<unsigned>((n + 255) / 256), 256, 0, src, n, c->xyz, c->nrm, c->rgb);
+  dev_free(ctx, tmp);
+  return c;
+}
+
+lcr_cloud* upload_xyz(lcr_ctx* ctx, const float* xyz, size_t n) {
+  lcr_cloud* c = cloud_alloc(ctx, n);
+  if (n == 0) return c;
+  float* tmp = static_cast<float*>(dev_alloc(ctx, n * 3 * sizeof(float)));
+  CUDA_TRY(cudaMemcpyAsync(tmp, xyz, n * 3 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  LCR_LAUNCH(ctx, k_from_xyz, static_cast<unsigned>((n + 255) / 256), 256, 0, tmp, n, c->xyz, c->nrm, c->rgb);
+  dev_free(ctx, tmp);
+  return c;
+}
+
+void download_records(lcr_ctx* ctx, const lcr_cloud* c, void* out) {
+  if (c->n == 0) return;
+  float4* tmp = static_cast<float4*>(dev_alloc(ctx, c->n * sizeof(lcr_point)));
+  LCR_LAUNCH(ctx, k_pack, static_cast<unsigned>((c->n + 255) / 256), 256, 0, c->xyz, c->nrm, c->rgb, c->n, tmp);
+  CUDA_TRY(cudaMemcpyAsync(out, tmp, c->n * sizeof(lcr_point), cudaMemcpyDeviceToHost, ctx->stream));
+  dev_free(ctx, tmp);
+  sync(ctx);
+}
+
+lcr_cloud* concat_clouds(lcr_ctx* ctx, const lcr_cloud* a, const lcr_cloud* b) {
+  lcr_cloud* c = cloud_alloc(ctx, a->n + b->n);
+  if (a->n) {
+    CUDA_TRY(cudaMemcpyAsync(c->xyz, a->xyz, a->n * 16, cudaMemcpyDeviceToDevice, ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->nrm, a->nrm, a->n * 16, cudaMemcpyDeviceToDevice, ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->rgb, a->rgb, a->n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  if (b->n) {
+    CUDA_TRY(cudaMemcpyAsync(c->xyz + a->n, b->xyz, b->n * 16, cudaMemcpyDeviceToDevice, ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->nrm + a->n, b->nrm, b->n * 16, cudaMemcpyDeviceToDevice, ctx->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->rgb + a->n, b->rgb, b->n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  return c;
+}
+
+lcr_cloud* transform_run(lcr_ctx* ctx, const lcr_cloud* in, const float* m) {
+  lcr_cloud* c = cloud_alloc(ctx, in->n);
+  if (in->n == 0) return c;
+  Xf T;
+  for (int i = 0; i < 12; ++i) T.m[i] = m[i];
+  LCR_LAUNCH(ctx, k_transform, static_cast<unsigned>((in->n + 255) / 256), 256, 0, in->xyz, in->nrm, in->rgb, in->n,
+             T, c->xyz, c->nrm, c->rgb);
+  return c;
+}
+
+void centroid_run(lcr_ctx* ctx, const lcr_cloud* in, double* c4) {
+  const int nb = std::max(1, std::min(ctx->sms * 2, static_cast<int>((in->n + 255) / 256)));
+  Sum4* part = static_cast<Sum4*>(dev_alloc(ctx, nb * sizeof(Sum4) + 4 * sizeof(double)));
+  double* out = reinterpret_cast<double*>(part + nb);
+  LCR_LAUNCH(ctx, k_centroid_partial, nb, 256, 0, in->xyz, in->n, part);
+  LCR_LAUNCH(ctx, k_centroid_final, 1, 32, 0, part, nb, out);
+  double* h = static_cast<double*>(pinned(ctx, 4 * sizeof(double)));
+  CUDA_TRY(cudaMemcpyAsync(h, out, 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  dev_free(ctx, part);
+  sync(ctx);
+  for (int i = 0; i < 4; ++i) c4[i] = h[i];
+}

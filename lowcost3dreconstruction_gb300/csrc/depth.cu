@@ -1,0 +1,229 @@
+// Depth-image -> point-cloud path: burst fusion (zero-eliminated mean) and the
+// Kinect v1 / v2 back-projections, reproducing the reference's arithmetic with
+// explicit IEEE intrinsics (no FMA contraction) so results are bit-exact.
+#include <algorithm>
+
+#include "lcr_internal.cuh"
+
+namespace {
+
+struct BP {
+  int w, h;
+  double ifx, ify, cx, cy;  // V1: 1/fx, 1/fy in double as the reference computes them
+  float fxf, fyf, cxf, cyf; // V2: libfreenect2's float intrinsics
+  double dmin, dmax, scale;
+  float scalef;
+  int left, right, top, bottom;
+  int normals;
+  uint32_t rgb;
+};
+
+// super_resolution.cpp:295-315: mean of the non-zero samples in double, returned
+// as float, then converted to uint16 with round-half-even and saturation.  With
+// no sample the reference's 0/0 NaN saturates to 0.
+__global__ void k_fuse_u16(const uint16_t* __restrict__ frames, int F, size_t npix, uint16_t* __restrict__ out) {
+  const size_t p = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= npix) return;
+  uint32_t sum = 0, cnt = 0;
+  for (int f = 0; f < F; ++f) {
+    const uint32_t v = frames[static_cast<size_t>(f) * npix + p];
+    if (v) { sum += v; ++cnt; }
+  }
+  uint16_t r = 0;
+  if (cnt) {
+    const float m = __double2float_rn(__ddiv_rn(static_cast<double>(sum), static_cast<double>(cnt)));
+    const int ri = __float2int_rn(m);
+    r = static_cast<uint16_t>(ri <= 0 ? 0 : (ri >= 65535 ? 65535 : ri));
+  }
+  out[p] = r;
+}
+
+// super_resolution_kv2.cpp:287-303 (guarded: an empty pixel stays 0).
+__global__ void k_fuse_f32(const float* __restrict__ frames, int F, size_t npix, float* __restrict__ out) {
+  const size_t p = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= npix) return;
+  double sum = 0.0;
+  uint32_t cnt = 0;
+  for (int f = 0; f < F; ++f) {
+    const float v = frames[static_cast<size_t>(f) * npix + p];
+    if (v > 0.f) { sum = __dadd_rn(sum, static_cast<double>(v)); ++cnt; }
+  }
+  out[p] = cnt ? __double2float_rn(__ddiv_rn(sum, static_cast<double>(cnt))) : 0.f;
+}
+
+__device__ __forceinline__ bool keep_v1(const BP& b, int i, int j, uint16_t z) {
+  return z != 0 && z >= b.dmin && z <= b.dmax && i >= b.top && i <= b.bottom && j >= b.left && j <= b.right;
+}
+
+__global__ void k_flags_v1(const uint16_t* __restrict__ depth, BP b, uint8_t* __restrict__ flags) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= b.w * b.h) return;
+  const int i = p / b.w, j = p - i * b.w;
+  flags[p] = keep_v1(b, i, j, depth[p]) ? 1 : 0;
+}
+
+// depth_capture.cpp:231-265 (rows are the "x" direction of the gradient).
+__device__ __forceinline__ float3 image_normal(const uint16_t* __restrict__ d, int w, int h, int i, int j) {
+  const int c = d[static_cast<size_t>(i) * w + j];
+  int right = 0, left = 0, down = 0, up = 0;
+  if (i > 0 && j > 0 && i < h - 1 && j < w - 1) {
+    right = d[static_cast<size_t>(i + 1) * w + j];
+    left = d[static_cast<size_t>(i - 1) * w + j];
+    down = d[static_cast<size_t>(i) * w + j + 1];
+    up = d[static_cast<size_t>(i) * w + j - 1];
+  }
+  if (abs(c - right) > 20) right = 0;
+  if (abs(c - left) > 20) left = 0;
+  if (abs(c - down) > 20) down = 0;
+  if (abs(c - up) > 20) up = 0;
+  const double dzdx = __ddiv_rn(static_cast<double>(right - left), 2.0);
+  const double dzdy = __ddiv_rn(static_cast<double>(down - up), 2.0);
+  const double d0 = -dzdx, d1 = -dzdy, d2 = 1.0;
+  double s = __dmul_rn(d0, d0);
+  s = __dadd_rn(s, __dmul_rn(d1, d1));
+  s = __dadd_rn(s, __dmul_rn(d2, d2));
+  const double nv = __dsqrt_rn(s);
+  const double inv = nv != 0.0 ? __ddiv_rn(1.0, nv) : 0.0;
+  return make_float3(__double2float_rn(__dmul_rn(d0, inv)), __double2float_rn(__dmul_rn(d1, inv)),
+                     __double2float_rn(__dmul_rn(d2, inv)));
+}
+
+// depth_capture.cpp:294-308: x = z*(j-cx)*(1/fx), y = -z*(i-cy)*(1/fy), z' = -z in
+// double, times `scale`, rounded once to float.
+__global__ void k_emit_v1(const uint16_t* __restrict__ depth, BP b, const uint32_t* __restrict__ idx, int n,
+                          float4* __restrict__ xyz, float4* __restrict__ nrm, uint32_t* __restrict__ rgb) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int p = static_cast<int>(idx[k]);
+  const int i = p / b.w, j = p - i * b.w;
+  const int z = depth[p];
+  const double vx = __dmul_rn(__dmul_rn(static_cast<double>(z), __dsub_rn(static_cast<double>(j), b.cx)), b.ifx);
+  const double vy = __dmul_rn(__dmul_rn(static_cast<double>(-z), __dsub_rn(static_cast<double>(i), b.cy)), b.ify);
+  const double vz = static_cast<double>(-z);
+  xyz[k] = make_float4(__double2float_rn(__dmul_rn(vx, b.scale)), __double2float_rn(__dmul_rn(vy, b.scale)),
+                       __double2float_rn(__dmul_rn(vz, b.scale)), 0.f);
+  float3 nn = make_float3(0.f, 0.f, 0.f);
+  if (b.normals) nn = image_normal(depth, b.w, b.h, i, j);
+  nrm[k] = make_float4(nn.x, nn.y, nn.z, 0.f);
+  rgb[k] = b.rgb;
+}
+
+// kinect2.h:169-187 + depth_capture_kv2.cpp:233-245 for one pixel.  Returns
+// whether the point survives; p receives the (unscaled) point.
+__device__ __forceinline__ bool point_v2(const BP& b, const float* __restrict__ depth, int yy, int xx, float3& p) {
+  const float dv = __fdiv_rn(depth[static_cast<size_t>(yy) * b.w + xx], 1000.0f);
+  if (isnan(dv) || static_cast<double>(fabsf(dv)) < 0.0001) return false;
+  const float cm =
+      __double2float_rn(__ddiv_rn(__dadd_rn(static_cast<double>(__fsub_rn(static_cast<float>(xx), b.cxf)), 0.5),
+                                  static_cast<double>(b.fxf)));
+  const float rm =
+      __double2float_rn(__ddiv_rn(__dadd_rn(static_cast<double>(__fsub_rn(static_cast<float>(yy), b.cyf)), 0.5),
+                                  static_cast<double>(b.fyf)));
+  const float px = __fmul_rn(cm, dv);
+  const float py = -__fmul_rn(rm, dv);
+  const float pz = -dv;
+  const float X = __double2float_rn(__dadd_rn(
+      __dsub_rn(static_cast<double>(__fmul_rn(__fdiv_rn(px, -pz), b.fxf)), 0.5), static_cast<double>(b.cxf)));
+  const float Y = __double2float_rn(__dadd_rn(
+      __dsub_rn(static_cast<double>(__fmul_rn(__fdiv_rn(-py, -pz), b.fyf)), 0.5), static_cast<double>(b.cyf)));
+  const float D = __double2float_rn(__dmul_rn(static_cast<double>(-pz), 1000.0));
+  if (!(D != 0.f && D >= b.dmin && D <= b.dmax && Y >= static_cast<float>(b.top) && Y <= static_cast<float>(b.bottom) &&
+        X >= static_cast<float>(b.left) && X <= static_cast<float>(b.right)))
+    return false;
+  p = make_float3(px, py, pz);
+  return true;
+}
+
+__global__ void k_flags_v2(const float* __restrict__ depth, BP b, uint8_t* __restrict__ flags) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= b.w * b.h) return;
+  const int yy = p / b.w, xx = p - yy * b.w;
+  float3 q;
+  flags[p] = point_v2(b, depth, yy, xx, q) ? 1 : 0;
+}
+
+__global__ void k_emit_v2(const float* __restrict__ depth, BP b, const uint32_t* __restrict__ idx, int n,
+                          float4* __restrict__ xyz, float4* __restrict__ nrm, uint32_t* __restrict__ rgb) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int p = static_cast<int>(idx[k]);
+  const int yy = p / b.w, xx = p - yy * b.w;
+  float3 q = make_float3(0.f, 0.f, 0.f);
+  point_v2(b, depth, yy, xx, q);
+  xyz[k] = make_float4(__fmul_rn(b.scalef, q.x), __fmul_rn(b.scalef, q.y), __fmul_rn(b.scalef, q.z), 0.f);
+  nrm[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+  rgb[k] = b.rgb;
+}
+
+BP make_bp(const lcr_depth_params* p) {
+  BP b;
+  b.w = p->width;
+  b.h = p->height;
+  b.ifx = 1 / p->fx;
+  b.ify = 1 / p->fy;
+  b.cx = p->cx;
+  b.cy = p->cy;
+  b.fxf = static_cast<float>(p->fx);
+  b.fyf = static_cast<float>(p->fy);
+  b.cxf = static_cast<float>(p->cx);
+  b.cyf = static_cast<float>(p->cy);
+  b.dmin = p->depth_min;
+  b.dmax = p->depth_max;
+  b.scale = p->scale;
+  b.scalef = static_cast<float>(p->scale);
+  b.left = p->roi_left;
+  b.right = p->roi_right;
+  b.top = p->roi_top;
+  b.bottom = p->roi_bottom;
+  b.normals = p->normals;
+  b.rgb = static_cast<uint32_t>(p->b) | (static_cast<uint32_t>(p->g) << 8) | (static_cast<uint32_t>(p->r) << 16);
+  return b;
+}
+
+}  // namespace
+
+void burst_fuse_run(lcr_ctx* ctx, const void* d_frames, const lcr_depth_params* p, void* d_out) {
+  const size_t npix = static_cast<size_t>(p->width) * p->height;
+  const unsigned grid = static_cast<unsigned>((npix + 255) / 256);
+  if (p->model == LCR_DEPTH_KINECT_V1)
+    LCR_LAUNCH(ctx, k_fuse_u16, grid, 256, 0, static_cast<const uint16_t*>(d_frames), p->frames, npix,
+               static_cast<uint16_t*>(d_out));
+  else
+    LCR_LAUNCH(ctx, k_fuse_f32, grid, 256, 0, static_cast<const float*>(d_frames), p->frames, npix,
+               static_cast<float*>(d_out));
+}
+
+int backproject_run(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p, lcr_cloud** out) {
+  const int npix = p->width * p->height;
+  const BP b = make_bp(p);
+  const size_t esz = p->model == LCR_DEPTH_KINECT_V1 ? 2 : 4;
+  void* fused = nullptr;
+  const void* depth = d_depth;
+  if (p->frames > 1) {
+    fused = dev_alloc(ctx, npix * esz);
+    burst_fuse_run(ctx, d_depth, p, fused);
+    depth = fused;
+  }
+  uint8_t* flags = static_cast<uint8_t*>(dev_alloc(ctx, npix));
+  uint32_t* idx = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * npix));
+  const unsigned grid = (npix + 255) / 256;
+  if (p->model == LCR_DEPTH_KINECT_V1)
+    LCR_LAUNCH(ctx, k_flags_v1, grid, 256, 0, static_cast<const uint16_t*>(depth), b, flags);
+  else
+    LCR_LAUNCH(ctx, k_flags_v2, grid, 256, 0, static_cast<const float*>(depth), b, flags);
+  const int n = compact_flags(ctx, flags, npix, idx);
+  lcr_cloud* c = cloud_alloc(ctx, n);
+  if (n > 0) {
+    if (p->model == LCR_DEPTH_KINECT_V1)
+      LCR_LAUNCH(ctx, k_emit_v1, (n + 255) / 256, 256, 0, static_cast<const uint16_t*>(depth), b, idx, n, c->xyz,
+                 c->nrm, c->rgb);
+    else
+      LCR_LAUNCH(ctx, k_emit_v2, (n + 255) / 256, 256, 0, static_cast<const float*>(depth), b, idx, n, c->xyz,
+                 c->nrm, c->rgb);
+  }
+  dev_free(ctx, flags);
+  dev_free(ctx, idx);
+  dev_free(ctx, fused);
+  *out = c;
+  return n;
+}

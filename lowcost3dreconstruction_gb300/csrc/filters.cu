@@ -1,0 +1,389 @@
+// StatisticalOutlierRemoval, NormalEstimation and the accumulate_clouds crop
+// predicate, each fused into the epilogue of the warp-tile neighbour search.
+#include <algorithm>
+#include <cmath>
+
+#include "search.cuh"
+
+namespace {
+
+// ------------------------------------------------------------------ SOR
+// outlier_removal.cpp:80-84.  kNN with k+1 results (the query itself first),
+// mean of sqrt(d) over results 1..k summed in double in ascending order
+// (float sqrt, as std::sqrt on a float), stored as float.
+__global__ void k_sor_dist(IndexView ix, int mean_k, float* __restrict__ dist, uint8_t* __restrict__ valid,
+                           unsigned int* __restrict__ nvalid) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int K = mean_k + 1;
+  WarpScratch& ws = reinterpret_cast<WarpScratch*>(smem)[wib];
+  unsigned long long* list =
+      reinterpret_cast<unsigned long long*>(smem + nw * sizeof(WarpScratch)) + static_cast<size_t>(wib) * K * 32;
+  const int tile = blockIdx.x * nw + wib;
+  if (tile >= ix.nleaf) return;
+  const float4 q = ix.pts[static_cast<size_t>(tile) * 32 + lane];
+  const bool qv = finite3(q.x, q.y, q.z);
+  float4 tlo, thi;
+  if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
+  NNK v;
+  v.init(q.x, q.y, q.z, qv, LCR_INF, K, list, tlo, thi);
+  tile_traverse(ix, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), ws);
+  if (!qv) return;
+  double s = 0.0;
+  for (int j = 1; j < K; ++j) s = __dadd_rn(s, static_cast<double>(__fsqrt_rn(key_dist(list[j * 32 + lane]))));
+  const uint32_t o = __float_as_uint(q.w);
+  dist[o] = __double2float_rn(__ddiv_rn(s, static_cast<double>(mean_k)));
+  valid[o] = 1;
+  atomicAdd(nvalid, 1u);
+}
+
+// Fixed blocked order: chunks of 256 consecutive terms summed sequentially
+// from 0.0 (level 0 sums d and float(d*d)), repeated until one value remains.
+__global__ void k_bsum_level0(const float* __restrict__ d, int n, double* __restrict__ oa, double* __restrict__ ob) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = c * 256;
+  if (b >= n) return;
+  const int e = min(n, b + 256);
+  double sa = 0.0, sb = 0.0;
+  for (int i = b; i < e; ++i) {
+    const float v = d[i];
+    sa = __dadd_rn(sa, static_cast<double>(v));
+    sb = __dadd_rn(sb, static_cast<double>(__fmul_rn(v, v)));
+  }
+  oa[c] = sa;
+  ob[c] = sb;
+}
+
+__global__ void k_bsum_level(const double* __restrict__ a, const double* __restrict__ b, int n,
+                             double* __restrict__ oa, double* __restrict__ ob) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = c * 256;
+  if (s >= n) return;
+  const int e = min(n, s + 256);
+  double sa = 0.0, sb = 0.0;
+  for (int i = s; i < e; ++i) {
+    sa = __dadd_rn(sa, a[i]);
+    sb = __dadd_rn(sb, b[i]);
+  }
+  oa[c] = sa;
+  ob[c] = sb;
+}
+
+// mean = sum/nv; variance = (sq - sum*sum/nv)/(nv-1); threshold = mean + mul*stddev.
+__global__ void k_sor_threshold(const double* __restrict__ sum, const double* __restrict__ sq,
+                                const unsigned int* __restrict__ nvalid, double mul, double* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  const double nv = static_cast<double>(*nvalid);
+  const double mean = __ddiv_rn(*sum, nv);
+  const double var = __ddiv_rn(__dsub_rn(*sq, __ddiv_rn(__dmul_rn(*sum, *sum), nv)), __dsub_rn(nv, 1.0));
+  const double sd = __dsqrt_rn(var);
+  out[0] = mean;
+  out[1] = sd;
+  out[2] = __dadd_rn(mean, __dmul_rn(mul, sd));
+}
+
+__global__ void k_sor_flags(const float* __restrict__ dist, int n, const double* __restrict__ stats,
+                            uint8_t* __restrict__ keep, uint8_t* __restrict__ drop) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bool out = static_cast<double>(dist[i]) > stats[2];
+  keep[i] = out ? 0 : 1;
+  drop[i] = out ? 1 : 0;
+}
+
+// -------------------------------------------------------------- normals
+// Smallest eigenpair of a symmetric 3x3 (FP64): FP32 trigonometric estimate of
+// the smallest root of the characteristic cubic, Newton refinement in FP64, and
+// the eigenvector as the best-conditioned cross product of two rows of A - l*I.
+__device__ void smallest_eig(const double C[6], double& lam, double n[3]) {
+  // C = {a00, a01, a02, a11, a12, a22}
+  double s = 0.0;
+  for (int i = 0; i < 6; ++i) s = fmax(s, fabs(C[i]));
+  if (!(s > 0.0)) {
+    lam = 0.0;
+    n[0] = 0.0; n[1] = 0.0; n[2] = 1.0;
+    return;
+  }
+  const double a00 = C[0] / s, a01 = C[1] / s, a02 = C[2] / s, a11 = C[3] / s, a12 = C[4] / s, a22 = C[5] / s;
+  const double c2 = a00 + a11 + a22;
+  const double c1 = a00 * a11 + a00 * a22 + a11 * a22 - a01 * a01 - a02 * a02 - a12 * a12;
+  const double c0 = a00 * (a11 * a22 - a12 * a12) - a01 * (a01 * a22 - a12 * a02) + a02 * (a01 * a12 - a11 * a02);
+  // FP32 estimate (trigonometric solution of the depressed cubic)
+  float l0;
+  {
+    const float q = static_cast<float>(c2) / 3.f;
+    const float b00 = static_cast<float>(a00) - q, b11 = static_cast<float>(a11) - q, b22 = static_cast<float>(a22) - q;
+    const float f01 = static_cast<float>(a01), f02 = static_cast<float>(a02), f12 = static_cast<float>(a12);
+    const float p1 = f01 * f01 + f02 * f02 + f12 * f12;
+    const float p2 = b00 * b00 + b11 * b11 + b22 * b22 + 2.f * p1;
+    const float p = sqrtf(p2 / 6.f);
+    if (p > 0.f) {
+      const float ip = 1.f / p;
+      const float B00 = b00 * ip, B11 = b11 * ip, B22 = b22 * ip, B01 = f01 * ip, B02 = f02 * ip, B12 = f12 * ip;
+      float r = 0.5f * (B00 * (B11 * B22 - B12 * B12) - B01 * (B01 * B22 - B12 * B02) + B02 * (B01 * B12 - B11 * B02));
+      r = fminf(1.f, fmaxf(-1.f, r));
+      const float phi = acosf(r) / 3.f;
+      l0 = q + 2.f * p * cosf(phi + 2.0943951f);
+    } else {
+      l0 = q;
+    }
+  }
+  double l = l0;
+  for (int it = 0; it < 4; ++it) {
+    const double f = ((-l + c2) * l - c1) * l + c0;       // det(A - l I)
+    const double fp = (-3.0 * l + 2.0 * c2) * l - c1;     // derivative
+    if (!(fabs(fp) > 0.0)) break;
+    const double step = f / fp;
+    l -= step;
+    if (fabs(step) <= 1e-17 * fmax(1.0, fabs(l))) break;
+  }
+  const double r0[3] = {a00 - l, a01, a02}, r1[3] = {a01, a11 - l, a12}, r2[3] = {a02, a12, a22 - l};
+  double x[3][3];
+  x[0][0] = r0[1] * r1[2] - r0[2] * r1[1]; x[0][1] = r0[2] * r1[0] - r0[0] * r1[2]; x[0][2] = r0[0] * r1[1] - r0[1] * r1[0];
+  x[1][0] = r0[1] * r2[2] - r0[2] * r2[1]; x[1][1] = r0[2] * r2[0] - r0[0] * r2[2]; x[1][2] = r0[0] * r2[1] - r0[1] * r2[0];
+  x[2][0] = r1[1] * r2[2] - r1[2] * r2[1]; x[2][1] = r1[2] * r2[0] - r1[0] * r2[2]; x[2][2] = r1[0] * r2[1] - r1[1] * r2[0];
+  int best = 0;
+  double bn = -1.0;
+  for (int k = 0; k < 3; ++k) {
+    const double m = x[k][0] * x[k][0] + x[k][1] * x[k][1] + x[k][2] * x[k][2];
+    if (m > bn) { bn = m; best = k; }
+  }
+  if (bn > 1e-28) {
+    const double inv = 1.0 / sqrt(bn);
+    n[0] = x[best][0] * inv; n[1] = x[best][1] * inv; n[2] = x[best][2] * inv;
+  } else {
+    // A - l I has rank <= 1: any unit vector orthogonal to its largest row.
+    const double* rr[3] = {r0, r1, r2};
+    int br = 0;
+    double brn = -1.0;
+    for (int k = 0; k < 3; ++k) {
+      const double m = rr[k][0] * rr[k][0] + rr[k][1] * rr[k][1] + rr[k][2] * rr[k][2];
+      if (m > brn) { brn = m; br = k; }
+    }
+    const double* a = rr[br];
+    double e[3] = {0, 0, 0};
+    const int ax = (fabs(a[0]) <= fabs(a[1]) && fabs(a[0]) <= fabs(a[2])) ? 0 : (fabs(a[1]) <= fabs(a[2]) ? 1 : 2);
+    e[ax] = 1.0;
+    double c[3] = {a[1] * e[2] - a[2] * e[1], a[2] * e[0] - a[0] * e[2], a[0] * e[1] - a[1] * e[0]};
+    double cn = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    if (!(cn > 0.0)) {
+      c[0] = 0.0; c[1] = 0.0; c[2] = 1.0;
+      cn = 1.0;
+    }
+    n[0] = c[0] / cn; n[1] = c[1] / cn; n[2] = c[2] / cn;
+  }
+  lam = l * s;
+}
+
+// normal_estimation.cpp:84-118: kNN(k) including the point itself, covariance,
+// eigenvector of the smallest eigenvalue, curvature = |l0 / trace|, flipped so
+// that (vp - p).n >= 0, optionally negated afterwards.
+__global__ void k_normals(IndexView ix, int K, const float4* __restrict__ xyz, float vx, float vy, float vz,
+                          int flip_all, float4* __restrict__ onrm) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  WarpScratch& ws = reinterpret_cast<WarpScratch*>(smem)[wib];
+  unsigned long long* list =
+      reinterpret_cast<unsigned long long*>(smem + nw * sizeof(WarpScratch)) + static_cast<size_t>(wib) * K * 32;
+  const int tile = blockIdx.x * nw + wib;
+  if (tile >= ix.nleaf) return;
+  const float4 q = ix.pts[static_cast<size_t>(tile) * 32 + lane];
+  const bool qv = finite3(q.x, q.y, q.z);
+  float4 tlo, thi;
+  if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
+  NNK v;
+  v.init(q.x, q.y, q.z, qv, LCR_INF, K, list, tlo, thi);
+  tile_traverse(ix, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), ws);
+  if (!qv) return;
+  const uint32_t o = __float_as_uint(q.w);
+  float sx = 0.f, sy = 0.f, sz = 0.f, sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
+  int m = 0;
+  for (int j = 0; j < K; ++j) {
+    const uint32_t id = key_idx(list[j * 32 + lane]);
+    if (id == 0xffffffffu) break;
+    const float4 p = xyz[id];
+    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+    sx += dx; sy += dy; sz += dz;
+    sxx += dx * dx; sxy += dx * dy; sxz += dx * dz;
+    syy += dy * dy; syz += dy * dz; szz += dz * dz;
+    ++m;
+  }
+  const float nan = __int_as_float(0x7fc00000);
+  if (m < 3) {
+    onrm[o] = make_float4(nan, nan, nan, nan);
+    return;
+  }
+  const double im = 1.0 / m;
+  const double mx = sx * im, my = sy * im, mz = sz * im;
+  const double C[6] = {sxx * im - mx * mx, sxy * im - mx * my, sxz * im - mx * mz,
+                       syy * im - my * my, syz * im - my * mz, szz * im - mz * mz};
+  double lam, nn[3];
+  smallest_eig(C, lam, nn);
+  const double tr = C[0] + C[3] + C[5];
+  const double curv = tr != 0.0 ? fabs(lam / tr) : 0.0;
+  const double cs = static_cast<double>(__fsub_rn(vx, q.x)) * nn[0] + static_cast<double>(__fsub_rn(vy, q.y)) * nn[1] +
+                    static_cast<double>(__fsub_rn(vz, q.z)) * nn[2];
+  double sgn = cs < 0 ? -1.0 : 1.0;
+  if (flip_all) sgn = -sgn;
+  onrm[o] = make_float4(static_cast<float>(sgn * nn[0]), static_cast<float>(sgn * nn[1]),
+                        static_cast<float>(sgn * nn[2]), static_cast<float>(curv));
+}
+
+// ----------------------------------------------------------------- crop
+// accumulate_clouds.cpp:100-111: a source point p is redundant when some target
+// q has float(q - r) <= p <= float(q + r) on every axis (the CropBox bounds are
+// Vector4f(q.x - radius, ...) with a double radius).  Node test: for any member
+// q of a box, float(q - r) >= float(lo - r) and float(q + r) <= float(hi + r).
+struct Crop {
+  float qx, qy, qz;
+  bool qv, found, all;
+  float4 tlo, thi;
+  double r;
+  __device__ __forceinline__ float lo_r(float v) const { return __double2float_rn(__dsub_rn(static_cast<double>(v), r)); }
+  __device__ __forceinline__ float hi_r(float v) const { return __double2float_rn(__dadd_rn(static_cast<double>(v), r)); }
+  __device__ __forceinline__ float metric(const float4& lo, const float4& hi) const {
+    const bool hit = lo_r(lo.x) <= thi.x && hi_r(hi.x) >= tlo.x && lo_r(lo.y) <= thi.y && hi_r(hi.y) >= tlo.y &&
+                     lo_r(lo.z) <= thi.z && hi_r(hi.z) >= tlo.z;
+    return hit ? 0.f : LCR_INF;
+  }
+  __device__ __forceinline__ bool still(float m) const { return m <= 0.f && !all; }
+  __device__ __forceinline__ bool need(const float4& lo, const float4& hi) const {
+    return qv && !found && lo_r(lo.x) <= qx && qx <= hi_r(hi.x) && lo_r(lo.y) <= qy && qy <= hi_r(hi.y) &&
+           lo_r(lo.z) <= qz && qz <= hi_r(hi.z);
+  }
+  __device__ __forceinline__ void scan(const float4* st) {
+    for (int j = 0; j < 32 && !found; ++j) {
+      const float4 t = st[j];
+      if (qx >= lo_r(t.x) && qx <= hi_r(t.x) && qy >= lo_r(t.y) && qy <= hi_r(t.y) && qz >= lo_r(t.z) &&
+          qz <= hi_r(t.z))
+        found = true;
+    }
+  }
+  __device__ __forceinline__ void refresh() { all = __all_sync(LCR_FULL, !qv || found); }
+};
+
+__global__ void k_crop(IndexView tgt, IndexView src, double r, uint8_t* __restrict__ removed) {
+  __shared__ WarpScratch wss[8];
+  const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (tile >= src.nleaf) return;
+  const float4 p = src.pts[static_cast<size_t>(tile) * 32 + lane];
+  const bool qv = finite3(p.x, p.y, p.z);
+  float4 tlo, thi;
+  if (!tile_box(p.x, p.y, p.z, qv, tlo, thi)) return;
+  Crop v;
+  v.qx = p.x; v.qy = p.y; v.qz = p.z;
+  v.qv = qv;
+  v.found = false;
+  v.tlo = tlo;
+  v.thi = thi;
+  v.r = r;
+  v.refresh();
+  tile_traverse(tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), wss[wib]);
+  if (qv && v.found) removed[__float_as_uint(p.w)] = 1;
+}
+
+size_t list_smem(int nw, int K) { return nw * (sizeof(WarpScratch) + static_cast<size_t>(K) * 32 * 8); }
+
+int finite_count(lcr_ctx* ctx, const lcr_cloud* in) {
+  double c4[4];
+  centroid_run(ctx, in, c4);
+  return static_cast<int>(c4[3] + 0.5);
+}
+
+}  // namespace
+
+void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_cloud** inliers,
+             lcr_cloud** outliers, lcr_sor_stats* stats, float* host_dist) {
+  if (mean_k <= 0) LCR_THROW(LCR_ERR_INVALID_ARG, "mean_k must be positive");
+  const int n = static_cast<int>(in->n);
+  if (n == 0) LCR_THROW(LCR_ERR_EMPTY, "statistical outlier removal on an empty cloud");
+  if (mean_k + 1 > finite_count(ctx, in))
+    LCR_THROW(LCR_ERR_TOO_FEW_POINTS, "SOR needs more than %d finite points (k+1 neighbours)", mean_k);
+  const IndexView ix = cloud_index(ctx, in).v;
+  const int K = mean_k + 1;
+  const int nw = K <= 64 ? 4 : 2;
+  const size_t smem = list_smem(nw, K);
+  if (smem > 227 * 1024) LCR_THROW(LCR_ERR_INVALID_ARG, "mean_k=%d too large", mean_k);
+  float* dist = static_cast<float*>(dev_alloc(ctx, sizeof(float) * n));
+  uint8_t* flags = static_cast<uint8_t*>(dev_alloc(ctx, 3 * static_cast<size_t>(n)));
+  uint8_t* valid = flags, *keep = flags + n, *drop = flags + 2 * static_cast<size_t>(n);
+  const int nc0 = (n + 255) / 256;
+  double* sums = static_cast<double*>(dev_alloc(ctx, sizeof(double) * (4 * static_cast<size_t>(nc0) + 8)));
+  unsigned int* nvalid = reinterpret_cast<unsigned int*>(sums + 4 * nc0 + 4);
+  double* st = sums + 4 * nc0;
+  CUDA_TRY(cudaMemsetAsync(dist, 0, sizeof(float) * n, ctx->stream));
+  CUDA_TRY(cudaMemsetAsync(valid, 0, n, ctx->stream));
+  CUDA_TRY(cudaMemsetAsync(nvalid, 0, sizeof(unsigned int), ctx->stream));
+  CUDA_TRY(cudaFuncSetAttribute(k_sor_dist, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  LCR_LAUNCH(ctx, k_sor_dist, (ix.nleaf + nw - 1) / nw, nw * 32, smem, ix, mean_k, dist, valid, nvalid);
+  // blocked sums (ping-pong between two halves of `sums`)
+  double *a = sums, *b = sums + nc0, *a2 = sums + 2 * nc0, *b2 = sums + 3 * nc0;
+  int m = nc0;
+  LCR_LAUNCH(ctx, k_bsum_level0, (m + 127) / 128, 128, 0, dist, n, a, b);
+  while (m > 1) {
+    const int m2 = (m + 255) / 256;
+    LCR_LAUNCH(ctx, k_bsum_level, (m2 + 127) / 128, 128, 0, a, b, m, a2, b2);
+    std::swap(a, a2);
+    std::swap(b, b2);
+    m = m2;
+  }
+  LCR_LAUNCH(ctx, k_sor_threshold, 1, 32, 0, a, b, nvalid, std_mul, st);
+  LCR_LAUNCH(ctx, k_sor_flags, (n + 255) / 256, 256, 0, dist, n, st, keep, drop);
+  uint32_t* idx = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * n));
+  const int nkeep = compact_flags(ctx, keep, n, idx);
+  if (inliers) {
+    *inliers = cloud_alloc(ctx, nkeep);
+    gather_cloud(ctx, in, idx, nkeep, *inliers);
+  }
+  if (outliers) {
+    const int ndrop = compact_flags(ctx, drop, n, idx);
+    *outliers = cloud_alloc(ctx, ndrop);
+    gather_cloud(ctx, in, idx, ndrop, *outliers);
+  }
+  double* hs = static_cast<double*>(pinned(ctx, 64));
+  CUDA_TRY(cudaMemcpyAsync(hs, st, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaMemcpyAsync(hs + 4, nvalid, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
+  if (host_dist) CUDA_TRY(cudaMemcpyAsync(host_dist, dist, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  sync(ctx);
+  if (stats) {
+    stats->mean = hs[0];
+    stats->stddev = hs[1];
+    stats->threshold = hs[2];
+    stats->valid = *reinterpret_cast<unsigned int*>(hs + 4);
+    stats->kept = static_cast<size_t>(nkeep);
+    stats->removed = static_cast<size_t>(n - nkeep);
+  }
+  dev_free(ctx, dist);
+  dev_free(ctx, flags);
+  dev_free(ctx, sums);
+  dev_free(ctx, idx);
+}
+
+lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[3], int flags) {
+  if (k <= 0) LCR_THROW(LCR_ERR_INVALID_ARG, "k must be positive");
+  const int n = static_cast<int>(in->n);
+  lcr_cloud* out = cloud_alloc(ctx, n);
+  if (n == 0) return out;
+  const IndexView ix = cloud_index(ctx, in).v;
+  const int nw = k <= 64 ? 4 : 2;
+  const size_t smem = list_smem(nw, k);
+  if (smem > 227 * 1024) LCR_THROW(LCR_ERR_INVALID_ARG, "k=%d too large", k);
+  CUDA_TRY(cudaMemcpyAsync(out->xyz, in->xyz, sizeof(float4) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  CUDA_TRY(cudaMemcpyAsync(out->rgb, in->rgb, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  // non-finite points keep NaN normals (they are not searched)
+  CUDA_TRY(cudaMemsetAsync(out->nrm, 0xff, sizeof(float4) * n, ctx->stream));
+  CUDA_TRY(cudaFuncSetAttribute(k_normals, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  LCR_LAUNCH(ctx, k_normals, (ix.nleaf + nw - 1) / nw, nw * 32, smem, ix, k, in->xyz, vp[0], vp[1], vp[2],
+             (flags & LCR_NORMALS_FLIP_ALL) ? 1 : 0, out->nrm);
+  return out;
+}
+
+void crop_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, double radius, uint8_t* d_removed) {
+  if (src->n == 0) return;
+  CUDA_TRY(cudaMemsetAsync(d_removed, 0, src->n, ctx->stream));
+  if (tgt->n == 0) return;
+  const IndexView tv = cloud_index(ctx, tgt).v;
+  const IndexView sv = cloud_index(ctx, src).v;
+  LCR_LAUNCH(ctx, k_crop, (sv.nleaf + 7) / 8, 256, 0, tv, sv, radius, d_removed);
+}

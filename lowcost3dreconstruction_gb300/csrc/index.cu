@@ -1,0 +1,160 @@
+// Search-index build: bounding box -> 30-bit Morton keys of a uniform 1024^3
+// grid over the cloud's cube -> stable radix sort (the sorted grid, i.e. the
+// voxel hash in key order) -> points gathered in key order as float4 with the
+// original index in w -> leaf boxes (32 points) -> 32-ary box levels.
+#include <algorithm>
+
+#include "lcr_internal.cuh"
+
+namespace {
+
+__device__ __forceinline__ uint32_t expand10(uint32_t v) {
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000ffu;
+  v = (v | (v << 8)) & 0x0300f00fu;
+  v = (v | (v << 4)) & 0x030c30c3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__global__ void k_morton(const float4* __restrict__ xyz, int n, const float4* __restrict__ box,
+                         uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = xyz[i];
+  uint32_t key = 0xffffffffu;
+  if (finite3(p.x, p.y, p.z)) {
+    const float4 lo = box[0], hi = box[1];
+    const float ext = fmaxf(fmaxf(hi.x - lo.x, hi.y - lo.y), hi.z - lo.z);
+    const float s = ext > 0.f ? 1023.0f / ext : 0.f;
+    const uint32_t ix = min(1023u, static_cast<uint32_t>(fmaxf((p.x - lo.x) * s, 0.f)));
+    const uint32_t iy = min(1023u, static_cast<uint32_t>(fmaxf((p.y - lo.y) * s, 0.f)));
+    const uint32_t iz = min(1023u, static_cast<uint32_t>(fmaxf((p.z - lo.z) * s, 0.f)));
+    key = expand10(ix) | (expand10(iy) << 1) | (expand10(iz) << 2);
+  }
+  keys[i] = key;
+  vals[i] = static_cast<uint32_t>(i);
+}
+
+__global__ void k_gather_sorted(const float4* __restrict__ xyz, const uint32_t* __restrict__ keys,
+                                const uint32_t* __restrict__ vals, int n, int npad, float4* __restrict__ pts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npad) return;
+  float4 o;
+  if (i < n && keys[i] != 0xffffffffu) {
+    const uint32_t s = vals[i];
+    const float4 p = xyz[s];
+    o = make_float4(p.x, p.y, p.z, __uint_as_float(s));
+  } else {
+    const float nan = __int_as_float(0x7fc00000);
+    o = make_float4(nan, nan, nan, __uint_as_float(0xffffffffu));
+  }
+  pts[i] = o;
+}
+
+// One warp per leaf; sentinel (non-finite) slots do not extend the box.  A leaf
+// with no finite point gets the empty box [+inf, -inf].
+__global__ void k_leaf_boxes(const float4* __restrict__ pts, int nleaf, float4* __restrict__ lo,
+                             float4* __restrict__ hi) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= nleaf) return;
+  const float4 p = pts[static_cast<size_t>(warp) * 32 + lane];
+  const bool f = finite3(p.x, p.y, p.z);
+  const float inf = __int_as_float(0x7f800000);
+  const float lx = warp_min(f ? p.x : inf), ly = warp_min(f ? p.y : inf), lz = warp_min(f ? p.z : inf);
+  const float hx = warp_max(f ? p.x : -inf), hy = warp_max(f ? p.y : -inf), hz = warp_max(f ? p.z : -inf);
+  if (lane == 0) {
+    lo[warp] = make_float4(lx, ly, lz, 0.f);
+    hi[warp] = make_float4(hx, hy, hz, 0.f);
+  }
+}
+
+__global__ void k_level_boxes(const float4* __restrict__ clo, const float4* __restrict__ chi, int nchild, int nnode,
+                              float4* __restrict__ lo, float4* __restrict__ hi) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= nnode) return;
+  const int c = warp * 32 + lane;
+  const float inf = __int_as_float(0x7f800000);
+  float4 a = make_float4(inf, inf, inf, 0.f), b = make_float4(-inf, -inf, -inf, 0.f);
+  if (c < nchild) {
+    a = clo[c];
+    b = chi[c];
+  }
+  const float lx = warp_min(a.x), ly = warp_min(a.y), lz = warp_min(a.z);
+  const float hx = warp_max(b.x), hy = warp_max(b.y), hz = warp_max(b.z);
+  if (lane == 0) {
+    lo[warp] = make_float4(lx, ly, lz, 0.f);
+    hi[warp] = make_float4(hx, hy, hz, 0.f);
+  }
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+}  // namespace
+
+Index* build_index(lcr_ctx* ctx, const float4* xyz, int n) {
+  if (n <= 0) LCR_THROW(LCR_ERR_EMPTY, "cannot index an empty cloud");
+  Index* ix = new Index();
+  IndexView& v = ix->v;
+  v.n = n;
+  v.nleaf = (n + 31) / 32;
+  int counts[kMaxLevels + 1];
+  int levels = 0;
+  counts[0] = v.nleaf;
+  while (counts[levels] > 1) {
+    if (levels + 1 >= kMaxLevels) {
+      delete ix;
+      LCR_THROW(LCR_ERR_INVALID_ARG, "cloud too large for the index (%d points)", n);
+    }
+    counts[levels + 1] = (counts[levels] + 31) / 32;
+    ++levels;
+  }
+  v.top = levels;
+  const size_t npad = static_cast<size_t>(v.nleaf) * 32;
+  size_t bytes = align256(npad * sizeof(float4));
+  for (int l = 0; l <= levels; ++l) bytes += 2 * align256(static_cast<size_t>(counts[l]) * sizeof(float4));
+  char* blk = static_cast<char*>(dev_alloc(ctx, bytes));
+  ix->block = blk;
+  ix->bytes = bytes;
+  size_t off = 0;
+  v.pts = reinterpret_cast<float4*>(blk);
+  off += align256(npad * sizeof(float4));
+  for (int l = 0; l < kMaxLevels; ++l) {
+    v.lo[l] = v.hi[l] = nullptr;
+    v.count[l] = 0;
+  }
+  for (int l = 0; l <= levels; ++l) {
+    v.count[l] = counts[l];
+    v.lo[l] = reinterpret_cast<float4*>(blk + off);
+    off += align256(static_cast<size_t>(counts[l]) * sizeof(float4));
+    v.hi[l] = reinterpret_cast<float4*>(blk + off);
+    off += align256(static_cast<size_t>(counts[l]) * sizeof(float4));
+  }
+
+  uint32_t* keys = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * static_cast<size_t>(n)));
+  uint32_t* vals = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * static_cast<size_t>(n)));
+  float4* box = static_cast<float4*>(dev_alloc(ctx, 2 * sizeof(float4)));
+  bbox(ctx, xyz, n, box);
+  LCR_LAUNCH(ctx, k_morton, (n + 255) / 256, 256, 0, xyz, n, box, keys, vals);
+  radix_sort_pairs(ctx, keys, vals, n, 32);
+  LCR_LAUNCH(ctx, k_gather_sorted, static_cast<int>((npad + 255) / 256), 256, 0, xyz, keys, vals, n,
+             static_cast<int>(npad), const_cast<float4*>(v.pts));
+  LCR_LAUNCH(ctx, k_leaf_boxes, (v.nleaf * 32 + 255) / 256, 256, 0, v.pts, v.nleaf, const_cast<float4*>(v.lo[0]),
+             const_cast<float4*>(v.hi[0]));
+  for (int l = 1; l <= levels; ++l) {
+    LCR_LAUNCH(ctx, k_level_boxes, (counts[l] * 32 + 255) / 256, 256, 0, v.lo[l - 1], v.hi[l - 1], counts[l - 1],
+               counts[l], const_cast<float4*>(v.lo[l]), const_cast<float4*>(v.hi[l]));
+  }
+  dev_free(ctx, keys);
+  dev_free(ctx, vals);
+  dev_free(ctx, box);
+  return ix;
+}
+
+void free_index(lcr_ctx* ctx, Index* ix) {
+  if (!ix) return;
+  dev_free(ctx, ix->block);
+  delete ix;
+}

@@ -1,0 +1,220 @@
+// Internal declarations shared by the liblcr CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+
+#include "../../include/lcr.h"
+
+#define LCR_FULL 0xffffffffu
+
+// ---------------------------------------------------------------- errors
+struct LcrError {
+  lcr_status st;
+  std::string msg;
+};
+
+// Throwing inside the library, caught at the C ABI boundary (api.cu).
+#define LCR_THROW(status, ...)                                  \
+  do {                                                          \
+    char _b[512];                                               \
+    snprintf(_b, sizeof _b, __VA_ARGS__);                       \
+    throw LcrError{status, std::string(_b)};                    \
+  } while (0)
+
+#define CUDA_TRY(expr)                                                                      \
+  do {                                                                                      \
+    cudaError_t _e = (expr);                                                                \
+    if (_e != cudaSuccess) {                                                                \
+      lcr_status _s = _e == cudaErrorMemoryAllocation ? LCR_ERR_OOM : LCR_ERR_CUDA;         \
+      LCR_THROW(_s, "%s:%d %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(_e));     \
+    }                                                                                       \
+  } while (0)
+
+// Every kernel launch goes through LCR_LAUNCH so that the context counts it and
+// launch errors surface immediately.
+#define LCR_LAUNCH(ctx, kernel, grid, block, smem, ...)                        \
+  do {                                                                         \
+    kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);           \
+    (ctx)->launches++;                                                         \
+    CUDA_TRY(cudaGetLastError());                                              \
+  } while (0)
+
+// ---------------------------------------------------------- search index
+// Morton-sorted points grouped into leaves of 32 (one warp-wide float4 load per
+// leaf) with a 32-ary hierarchy of axis-aligned boxes above them.
+constexpr int kMaxLevels = 8;
+
+struct IndexView {
+  const float4* pts;            // npad = nleaf*32 sorted points, w = original index (int bits), sentinel NaN / -1
+  const float4* lo[kMaxLevels]; // boxes per level; level 0 = leaves
+  const float4* hi[kMaxLevels];
+  int count[kMaxLevels];        // boxes per level
+  int top;                      // level of the root (count[top] == 1)
+  int n;                        // points (including non-finite ones, which become sentinels)
+  int nleaf;
+};
+
+struct Index {
+  IndexView v;
+  void* block = nullptr;        // one allocation holding everything
+  size_t bytes = 0;
+};
+
+// ------------------------------------------------------------------ cloud
+struct lcr_cloud {
+  size_t n = 0;
+  float4* xyz = nullptr;        // x y z 0
+  float4* nrm = nullptr;        // nx ny nz curvature
+  uint32_t* rgb = nullptr;      // packed b g r a (little-endian PCL rgba)
+  Index* index = nullptr;       // built on first search, freed with the cloud
+};
+
+struct lcr_ctx {
+  int device = 0;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t launches = 0;
+  std::string last_error;
+  // pinned host staging for small results
+  void* pinned = nullptr;
+  size_t pinned_bytes = 0;
+  // persistent ICP device buffers (state + partial sums)
+  void* icp_block = nullptr;
+  size_t icp_bytes = 0;
+  // captured ICP loops (one per method), reused across calls
+  cudaGraphExec_t icp_exec[2] = {nullptr, nullptr};
+  int icp_graph_ok = -1;        // -1 unknown, 0 unavailable, 1 usable
+};
+
+// --------------------------------------------------------- memory helpers
+void* dev_alloc(lcr_ctx* ctx, size_t bytes);
+void dev_free(lcr_ctx* ctx, void* p);
+void* pinned(lcr_ctx* ctx, size_t bytes);
+lcr_cloud* cloud_alloc(lcr_ctx* ctx, size_t n);
+void cloud_release(lcr_ctx* ctx, lcr_cloud* c);
+const Index& cloud_index(lcr_ctx* ctx, const lcr_cloud* c);
+void sync(lcr_ctx* ctx);
+
+// --------------------------------------------------------- exact FP32 ops
+// Squared distance exactly as FLANN's L2_Simple<float> evaluates it on three
+// components: d = q - p, r = d0*d0; r += d1*d1; r += d2*d2 -- separate IEEE
+// multiplies and adds (never contracted to FMA), so the GPU reproduces the CPU
+// bit for bit.
+__device__ __forceinline__ float exact_dist2(float qx, float qy, float qz, float px, float py, float pz) {
+  const float d0 = __fsub_rn(qx, px), d1 = __fsub_rn(qy, py), d2 = __fsub_rn(qz, pz);
+  return __fadd_rn(__fadd_rn(__fmul_rn(d0, d0), __fmul_rn(d1, d1)), __fmul_rn(d2, d2));
+}
+
+// Lower bound of exact_dist2 over every point inside [lo, hi]: each per-axis gap
+// is a rounded difference no larger than the corresponding point difference and
+// rounding is monotone, so the bound never exceeds a member's distance.
+__device__ __forceinline__ float box_dist2(const float4 lo, const float4 hi, float x, float y, float z) {
+  const float gx = fmaxf(fmaxf(__fsub_rn(lo.x, x), __fsub_rn(x, hi.x)), 0.f);
+  const float gy = fmaxf(fmaxf(__fsub_rn(lo.y, y), __fsub_rn(y, hi.y)), 0.f);
+  const float gz = fmaxf(fmaxf(__fsub_rn(lo.z, z), __fsub_rn(z, hi.z)), 0.f);
+  return __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
+}
+
+// Lower bound between any point of box a and any point of box b.
+__device__ __forceinline__ float box_box_dist2(const float4 alo, const float4 ahi, const float4 blo, const float4 bhi) {
+  const float gx = fmaxf(fmaxf(__fsub_rn(alo.x, bhi.x), __fsub_rn(blo.x, ahi.x)), 0.f);
+  const float gy = fmaxf(fmaxf(__fsub_rn(alo.y, bhi.y), __fsub_rn(blo.y, ahi.y)), 0.f);
+  const float gz = fmaxf(fmaxf(__fsub_rn(alo.z, bhi.z), __fsub_rn(blo.z, ahi.z)), 0.f);
+  return __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
+}
+
+// (distance, index) packed so that integer order is (distance, then index) order.
+__device__ __forceinline__ unsigned long long make_key(float d, uint32_t idx) {
+  return (static_cast<unsigned long long>(__float_as_uint(d)) << 32) | idx;
+}
+__device__ __forceinline__ float key_dist(unsigned long long k) { return __uint_as_float(static_cast<uint32_t>(k >> 32)); }
+__device__ __forceinline__ uint32_t key_idx(unsigned long long k) { return static_cast<uint32_t>(k); }
+
+// 3x4 FP32 rigid transform applied as Eigen evaluates Matrix4f * Vector4f:
+// ((r0*x + r1*y) + r2*z) + t with separate roundings.
+struct Xf {
+  float m[12];
+};
+__device__ __forceinline__ float3 xf_apply(const Xf& T, float x, float y, float z) {
+  float3 o;
+  o.x = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(T.m[0], x), __fmul_rn(T.m[1], y)), __fmul_rn(T.m[2], z)), T.m[3]);
+  o.y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(T.m[4], x), __fmul_rn(T.m[5], y)), __fmul_rn(T.m[6], z)), T.m[7]);
+  o.z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(T.m[8], x), __fmul_rn(T.m[9], y)), __fmul_rn(T.m[10], z)), T.m[11]);
+  return o;
+}
+__device__ __forceinline__ float3 xf_rotate(const Xf& T, float x, float y, float z) {
+  float3 o;
+  o.x = __fadd_rn(__fadd_rn(__fmul_rn(T.m[0], x), __fmul_rn(T.m[1], y)), __fmul_rn(T.m[2], z));
+  o.y = __fadd_rn(__fadd_rn(__fmul_rn(T.m[4], x), __fmul_rn(T.m[5], y)), __fmul_rn(T.m[6], z));
+  o.z = __fadd_rn(__fadd_rn(__fmul_rn(T.m[8], x), __fmul_rn(T.m[9], y)), __fmul_rn(T.m[10], z));
+  return o;
+}
+
+__device__ __forceinline__ bool finite3(float x, float y, float z) {
+  return isfinite(x) && isfinite(y) && isfinite(z);
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(LCR_FULL, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(LCR_FULL, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(LCR_FULL, v, o));
+  return v;
+}
+
+// ---------------------------------------------------- shared primitives
+// Stable LSD radix sort of (key, value) pairs on the context stream.  keys/vals
+// are sorted in place (tmp buffers allocated internally).  `bits` = significant
+// key bits (rounded up to 8-bit digits).
+void radix_sort_pairs(lcr_ctx* ctx, uint32_t* keys, uint32_t* vals, int n, int bits);
+// Order-preserving compaction: indices of flags[i] != 0 written to out_idx in
+// ascending order.  Returns the count (synchronises).
+int compact_flags(lcr_ctx* ctx, const uint8_t* flags, int n, uint32_t* out_idx);
+// Gathers cloud rows: out[j] = in[idx[j]].
+void gather_cloud(lcr_ctx* ctx, const lcr_cloud* in, const uint32_t* idx, int n, lcr_cloud* out);
+// Device-side bounding box of the finite points of an xyz array: out[0] = lo, out[1] = hi.
+void bbox(lcr_ctx* ctx, const float4* xyz, int n, float4* out2);
+
+// ------------------------------------------------------------ index build
+Index* build_index(lcr_ctx* ctx, const float4* xyz, int n);
+void free_index(lcr_ctx* ctx, Index* ix);
+
+// ----------------------------------------------------- algorithm entry points
+void knn_run(lcr_ctx* ctx, const lcr_cloud* ref, const lcr_cloud* query, int k, float cap, int32_t* d_idx,
+             float* d_dist);
+int backproject_run(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p, lcr_cloud** out);
+void burst_fuse_run(lcr_ctx* ctx, const void* d_frames, const lcr_depth_params* p, void* d_out);
+lcr_cloud* voxel_run(lcr_ctx* ctx, const lcr_cloud* in, float lx, float ly, float lz);
+void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_cloud** inliers,
+             lcr_cloud** outliers, lcr_sor_stats* stats, float* host_dist);
+lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[3], int flags);
+void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr_icp_params* p, const float* guess,
+             lcr_icp_result* res);
+void corr_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const double* T, double dmax, int32_t* d_idx,
+              float* d_dist);
+void crop_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, double radius, uint8_t* d_removed);
+lcr_cloud* transform_run(lcr_ctx* ctx, const lcr_cloud* in, const float* m);
+// c4 = {x, y, z, finite count}, FP64 accumulation (synchronises).
+void centroid_run(lcr_ctx* ctx, const lcr_cloud* in, double* c4);
+lcr_cloud* upload_records(lcr_ctx* ctx, const void* recs, size_t n, bool device_src);
+lcr_cloud* upload_xyz(lcr_ctx* ctx, const float* xyz, size_t n);
+void download_records(lcr_ctx* ctx, const lcr_cloud* c, void* out);
+lcr_cloud* concat_clouds(lcr_ctx* ctx, const lcr_cloud* a, const lcr_cloud* b);
+// Largest float whose double value is <= v (PCL compares a float distance with a
+// double squared threshold).
+float float_cap(double v);
+
+#define LCR_INF_HOST __builtin_huge_valf()

@@ -16,18 +16,16 @@ __global__ void k_sor_dist(IndexView ix, int mean_k, float* __restrict__ dist, u
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int K = mean_k + 1;
-  WarpScratch& ws = reinterpret_cast<WarpScratch*>(smem)[wib];
-  unsigned long long* list =
-      reinterpret_cast<unsigned long long*>(smem + nw * sizeof(WarpScratch)) + static_cast<size_t>(wib) * K * 32;
+  unsigned char* wbase = smem + wib * knn_warp_bytes(K);
+  unsigned char* region = wbase + sizeof(KnnWarp);
+  const unsigned long long* list = reinterpret_cast<const unsigned long long*>(region);
   const int tile = blockIdx.x * nw + wib;
   if (tile >= ix.nleaf) return;
   const float4 q = ix.pts[static_cast<size_t>(tile) * 32 + lane];
   const bool qv = finite3(q.x, q.y, q.z);
   float4 tlo, thi;
   if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
-  NNK v;
-  v.init(q.x, q.y, q.z, qv, LCR_INF, K, list, tlo, thi);
-  tile_traverse(ix, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), ws);
+  tile_knn(ix, q.x, q.y, q.z, qv, K, LCR_INF, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), region, tile);
   if (!qv) return;
   double s = 0.0;
   for (int j = 1; j < K; ++j) s = __dadd_rn(s, static_cast<double>(__fsqrt_rn(key_dist(list[j * 32 + lane]))));
@@ -182,18 +180,16 @@ __global__ void k_normals(IndexView ix, int K, const float4* __restrict__ xyz, f
                           int flip_all, float4* __restrict__ onrm) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  WarpScratch& ws = reinterpret_cast<WarpScratch*>(smem)[wib];
-  unsigned long long* list =
-      reinterpret_cast<unsigned long long*>(smem + nw * sizeof(WarpScratch)) + static_cast<size_t>(wib) * K * 32;
+  unsigned char* wbase = smem + wib * knn_warp_bytes(K);
+  unsigned char* region = wbase + sizeof(KnnWarp);
+  const unsigned long long* list = reinterpret_cast<const unsigned long long*>(region);
   const int tile = blockIdx.x * nw + wib;
   if (tile >= ix.nleaf) return;
   const float4 q = ix.pts[static_cast<size_t>(tile) * 32 + lane];
   const bool qv = finite3(q.x, q.y, q.z);
   float4 tlo, thi;
   if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
-  NNK v;
-  v.init(q.x, q.y, q.z, qv, LCR_INF, K, list, tlo, thi);
-  tile_traverse(ix, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), ws);
+  tile_knn(ix, q.x, q.y, q.z, qv, K, LCR_INF, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), region, tile);
   if (!qv) return;
   const uint32_t o = __float_as_uint(q.w);
   float sx = 0.f, sy = 0.f, sz = 0.f, sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
@@ -259,6 +255,8 @@ struct Crop {
         found = true;
     }
   }
+  __device__ __forceinline__ bool skip(int) const { return false; }
+  __device__ __forceinline__ void visited(int) {}
   __device__ __forceinline__ void refresh() { all = __all_sync(LCR_FULL, !qv || found); }
 };
 
@@ -283,7 +281,7 @@ __global__ void k_crop(IndexView tgt, IndexView src, double r, uint8_t* __restri
   if (qv && v.found) removed[__float_as_uint(p.w)] = 1;
 }
 
-size_t list_smem(int nw, int K) { return nw * (sizeof(WarpScratch) + static_cast<size_t>(K) * 32 * 8); }
+size_t list_smem(int nw, int K) { return nw * knn_warp_bytes(K); }
 
 int finite_count(lcr_ctx* ctx, const lcr_cloud* in) {
   double c4[4];

@@ -1,15 +1,22 @@
 // pcl::IterativeClosestPoint on the GPU (pcl_tools/fine_registration.cpp:105-126).
 //
-// One launch = one ICP iteration, fused: every warp grabs tiles of 32
-// Morton-sorted source points, transforms them by the current FP32 transform,
-// finds each point's exact nearest target within the correspondence distance
-// (warp-tile traversal), forms the per-correspondence terms in FP32, reduces
-// them across the warp with a transposing reduce-scatter (lane l ends with term
-// l), and accumulates term l with Kahan compensation in FP32.  Blocks write FP64
-// partials; the last block to finish adds them in a fixed order, solves in FP64
-// (3x3 SVD for point-to-point, 6x6 LDL^T for point-to-plane), composes and
-// re-orthonormalises the transform, applies PCL's DefaultConvergenceCriteria and
-// tells the enclosing CUDA-graph WHILE node whether to run another iteration.
+// One ICP iteration is five launches, captured once per context as the body of
+// a CUDA-graph WHILE node (LCR_ICP_GRAPH=0 runs them from a host loop):
+//  1. k_icp_search  warps take tiles of 32 Hilbert-sorted source points,
+//                   transform them by the current FP32 transform, find each
+//                   point's exact nearest target within the correspondence
+//                   distance (one shared warp-tile traversal), form the
+//                   per-correspondence terms in FP32 and reduce them across the
+//                   warp with a transposing reduce-scatter (lane l ends with
+//                   term l) into a per-tile row.  Tiles wider than four search
+//                   radii are deferred.
+//  2. k_icp_hard    one warp per point of a deferred tile (per-query pruning).
+//  3. k_icp_wide    the term rows of the deferred tiles.
+//  4. k_icp_reduce  fixed-order FP64 sums of the tile rows.
+//  5. k_icp_solve   one block: FP64 solve (3x3 SVD for point-to-point, 6x6
+//                   LDL^T for point-to-plane), compose, re-orthonormalise, PCL's
+//                   DefaultConvergenceCriteria, and the WHILE condition.
+// Every sum runs in a fixed order, so the result does not depend on scheduling.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -21,6 +28,7 @@ namespace {
 
 constexpr int kIcpThreads = 256;
 constexpr int kIcpWarps = kIcpThreads / 32;
+constexpr int kIcpReduceBlocks = 128;
 
 struct IcpParams {
   IndexView tgt;
@@ -33,6 +41,13 @@ struct IcpParams {
   int max_iter;
   double teps, feps;
   int use_graph;
+  float* fd;              // fitness: squared NN distance per sorted source slot
+  float4* far;            // fitness: queries with no target point inside the cap
+  float* tile_part;       // per-tile FP32 term sums [ntiles][32]
+  uint32_t* hard_q;       // deferred query slots (points of wide tiles)
+  float4* hard_tp;        // per-slot result of a deferred query: target xyz, distance
+  uint32_t* hard_ti;      // per-slot target index (0xffffffff: none within the cap)
+  uint32_t* wide_tiles;   // tiles whose terms wait for the deferred queries
 };
 
 struct IcpState {
@@ -41,7 +56,8 @@ struct IcpState {
   double prev_mse, mse, fitness;
   int iter, done, converged, state, ncorr, launches;
   unsigned int tile_ctr, blocks_done;
-  unsigned int fit_tile_ctr, fit_blocks_done;
+  unsigned int fit_tile_ctr, fit_blocks_done, nfar, far_ctr;
+  unsigned int nhard, hard_ctr, nwide, wide_ctr;
 };
 
 // Transposing warp reduction: on entry every lane holds 32 terms; on exit lane l
@@ -58,13 +74,6 @@ __device__ __forceinline__ float reduce_scatter32(float (&v)[32], int lane) {
     }
   }
   return v[0];
-}
-
-__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
-  const float y = __fsub_rn(x, c);
-  const float t = __fadd_rn(s, y);
-  c = __fsub_rn(__fsub_rn(t, s), y);
-  s = t;
 }
 
 // ---------------------------------------------------------- FP64 solvers
@@ -312,128 +321,241 @@ __device__ void icp_update(const double* S, const IcpParams* prm, IcpState* st) 
   st->prev_mse = mse;
 }
 
+// Terms of one correspondence (all zero when the source point has none):
+// point-to-point S[0..2] s', S[3..5] t', S[6+3a+b] t'_a s'_b, S[15] count,
+// S[16] distance; point-to-plane S[0..20] upper A^T A, S[21..26] A^T b,
+// S[27] count, S[28] distance; s' = s - c, t' = t - c.
 template <int P2PL>
-__global__ void __launch_bounds__(kIcpThreads) k_icp_iter(const IcpParams* __restrict__ prm, IcpState* st,
-                                                          double* __restrict__ part, cudaGraphConditionalHandle h) {
+__device__ __forceinline__ void corr_terms(float (&t)[32], bool found, const float3& q, const float4& tp, float d,
+                                           uint32_t tidx, const IcpParams* __restrict__ prm) {
+#pragma unroll
+  for (int i = 0; i < 32; ++i) t[i] = 0.f;
+  if (!found) return;
+  const float c0 = prm->c[0], c1 = prm->c[1], c2 = prm->c[2];
+  const float sx = q.x - c0, sy = q.y - c1, sz = q.z - c2;
+  const float tx = tp.x - c0, ty = tp.y - c1, tz = tp.z - c2;
+  if (!P2PL) {
+    t[0] = sx; t[1] = sy; t[2] = sz;
+    t[3] = tx; t[4] = ty; t[5] = tz;
+    t[6] = tx * sx; t[7] = tx * sy; t[8] = tx * sz;
+    t[9] = ty * sx; t[10] = ty * sy; t[11] = ty * sz;
+    t[12] = tz * sx; t[13] = tz * sy; t[14] = tz * sz;
+    t[15] = 1.f;
+    t[16] = d;
+  } else {
+    const float4 n = prm->tgt_nrm[tidx];
+    t[27] = 1.f;
+    t[28] = d;
+    if (finite3(n.x, n.y, n.z)) {
+      float A[6];
+      A[0] = sy * n.z - sz * n.y;
+      A[1] = sz * n.x - sx * n.z;
+      A[2] = sx * n.y - sy * n.x;
+      A[3] = n.x; A[4] = n.y; A[5] = n.z;
+      const float r = n.x * (tx - sx) + n.y * (ty - sy) + n.z * (tz - sz);
+      int k = 0;
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = i; j < 6; ++j) t[k++] = A[i] * A[j];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) t[21 + i] = A[i] * r;
+    }
+  }
+}
+
+__device__ __forceinline__ bool icp_done(const IcpState* st) {
+  return *reinterpret_cast<const volatile int*>(&st->done) != 0;
+}
+
+// Pass 1 of an iteration.  Warps take tiles of 32 Morton-sorted source points
+// dynamically; a compact tile shares one capped 1-NN traversal and stores its
+// 32 FP32 term sums (lane l = term l) in tile_part[tile].  A tile wider than
+// four search radii (its queries straddle distant surfaces) is deferred: its
+// points go to the hard-query list and the tile to the wide list.
+template <int P2PL>
+__global__ void __launch_bounds__(kIcpThreads) k_icp_search(const IcpParams* __restrict__ prm, IcpState* st) {
   __shared__ IndexView s_tgt;
   __shared__ Xf s_T;
   __shared__ WarpScratch wss[kIcpWarps];
-  __shared__ double s_acc[kIcpWarps][32];
-  __shared__ int s_flag;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  if (icp_done(st)) return;
   if (threadIdx.x == 0) {
-    s_flag = *reinterpret_cast<volatile int*>(&st->done);
-    if (s_flag && blockIdx.x == 0 && prm->use_graph) cudaGraphSetConditional(h, 0);
     s_tgt = prm->tgt;
     s_T = st->Tf;
   }
   __syncthreads();
-  if (s_flag) return;
   const float4* __restrict__ src = prm->src_pts;
   const int ntiles = prm->src_ntiles;
   const float cap = prm->cap;
-  const float c0 = prm->c[0], c1 = prm->c[1], c2 = prm->c[2];
-  float acc = 0.f, cmp = 0.f;
   for (;;) {
     int tile = 0;
     if (lane == 0) tile = static_cast<int>(atomicAdd(&st->tile_ctr, 1u));
     tile = __shfl_sync(LCR_FULL, tile, 0);
     if (tile >= ntiles) break;
-    const float4 p = src[static_cast<size_t>(tile) * 32 + lane];
+    const int slot = tile * 32 + lane;
+    const float4 p = src[slot];
     const bool pv = finite3(p.x, p.y, p.z);
     float3 q = make_float3(0.f, 0.f, 0.f);
     if (pv) q = xf_apply(s_T, p.x, p.y, p.z);
     float4 tlo, thi;
-    if (!tile_box(q.x, q.y, q.z, pv, tlo, thi)) continue;
+    if (!tile_box(q.x, q.y, q.z, pv, tlo, thi)) {
+      prm->tile_part[slot] = 0.f;
+      continue;
+    }
+    const float dx = thi.x - tlo.x, dy = thi.y - tlo.y, dz = thi.z - tlo.z;
+    if (dx * dx + dy * dy + dz * dz > 16.f * cap) {
+      const unsigned valid = __ballot_sync(LCR_FULL, pv);
+      unsigned base = 0;
+      if (lane == 0) {
+        base = atomicAdd(&st->nhard, static_cast<unsigned>(__popc(valid)));
+        prm->wide_tiles[atomicAdd(&st->nwide, 1u)] = static_cast<uint32_t>(tile);
+      }
+      base = __shfl_sync(LCR_FULL, base, 0);
+      if (pv) prm->hard_q[base + __popc(valid & ((1u << lane) - 1u))] = static_cast<uint32_t>(slot);
+      continue;
+    }
     NN1 v;
-    v.init(q.x, q.y, q.z, pv, cap, tlo, thi);
+    v.init(q.x, q.y, q.z, pv, cap, wss[wib]);
     tile_traverse(s_tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), wss[wib]);
     float t[32];
-#pragma unroll
-    for (int i = 0; i < 32; ++i) t[i] = 0.f;
-    if (pv && v.found()) {
-      const float sx = q.x - c0, sy = q.y - c1, sz = q.z - c2;
-      const float tx = v.bp.x - c0, ty = v.bp.y - c1, tz = v.bp.z - c2;
-      const float d = key_dist(v.best);
-      if (!P2PL) {
-        t[0] = sx; t[1] = sy; t[2] = sz;
-        t[3] = tx; t[4] = ty; t[5] = tz;
-        t[6] = tx * sx; t[7] = tx * sy; t[8] = tx * sz;
-        t[9] = ty * sx; t[10] = ty * sy; t[11] = ty * sz;
-        t[12] = tz * sx; t[13] = tz * sy; t[14] = tz * sz;
-        t[15] = 1.f;
-        t[16] = d;
-      } else {
-        const float4 n = prm->tgt_nrm[key_idx(v.best)];
-        t[27] = 1.f;
-        t[28] = d;
-        if (finite3(n.x, n.y, n.z)) {
-          float A[6];
-          A[0] = sy * n.z - sz * n.y;
-          A[1] = sz * n.x - sx * n.z;
-          A[2] = sx * n.y - sy * n.x;
-          A[3] = n.x; A[4] = n.y; A[5] = n.z;
-          const float r = n.x * (tx - sx) + n.y * (ty - sy) + n.z * (tz - sz);
-          int k = 0;
-#pragma unroll
-          for (int i = 0; i < 6; ++i)
-#pragma unroll
-            for (int j = i; j < 6; ++j) t[k++] = A[i] * A[j];
-#pragma unroll
-          for (int i = 0; i < 6; ++i) t[21 + i] = A[i] * r;
-        }
-      }
-    }
-    const float mine = reduce_scatter32(t, lane);
-    kahan_add(acc, cmp, mine);
+    corr_terms<P2PL>(t, pv && v.found(), q, v.bp, key_dist(v.best), key_idx(v.best), prm);
+    prm->tile_part[slot] = reduce_scatter32(t, lane);
   }
-  s_acc[wib][lane] = static_cast<double>(acc) - static_cast<double>(cmp);
+}
+
+// Pass 2: the deferred queries, one per warp (exact per-query pruning), spread
+// over the whole grid; results land in per-point slots.
+__global__ void __launch_bounds__(kIcpThreads) k_icp_hard(const IcpParams* __restrict__ prm, IcpState* st) {
+  __shared__ IndexView s_tgt;
+  __shared__ Xf s_T;
+  __shared__ WarpScratch wss[kIcpWarps];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  if (icp_done(st)) return;
+  if (threadIdx.x == 0) {
+    s_tgt = prm->tgt;
+    s_T = st->Tf;
+  }
+  __syncthreads();
+  const unsigned nhard = *reinterpret_cast<volatile unsigned*>(&st->nhard);
+  for (;;) {
+    unsigned i = 0;
+    if (lane == 0) i = atomicAdd(&st->hard_ctr, 1u);
+    i = __shfl_sync(LCR_FULL, i, 0);
+    if (i >= nhard) break;
+    const uint32_t slot = prm->hard_q[i];
+    const float4 p = prm->src_pts[slot];
+    const float3 q = xf_apply(s_T, p.x, p.y, p.z);
+    unsigned long long best;
+    float4 bp;
+    warp_query_nn(s_tgt, q.x, q.y, q.z, prm->cap, wss[wib], best, bp);
+    if (lane == 0) {
+      prm->hard_tp[slot] = make_float4(bp.x, bp.y, bp.z, key_dist(best));
+      prm->hard_ti[slot] = key_idx(best);
+    }
+  }
+}
+
+// Pass 3: term sums of the wide tiles from the per-point results.
+template <int P2PL>
+__global__ void __launch_bounds__(kIcpThreads) k_icp_wide(const IcpParams* __restrict__ prm, IcpState* st) {
+  __shared__ Xf s_T;
+  const int lane = threadIdx.x & 31;
+  if (icp_done(st)) return;
+  if (threadIdx.x == 0) s_T = st->Tf;
+  __syncthreads();
+  const unsigned nwide = *reinterpret_cast<volatile unsigned*>(&st->nwide);
+  for (;;) {
+    unsigned i = 0;
+    if (lane == 0) i = atomicAdd(&st->wide_ctr, 1u);
+    i = __shfl_sync(LCR_FULL, i, 0);
+    if (i >= nwide) break;
+    const int slot = static_cast<int>(prm->wide_tiles[i]) * 32 + lane;
+    const float4 p = prm->src_pts[slot];
+    const bool pv = finite3(p.x, p.y, p.z);
+    float3 q = make_float3(0.f, 0.f, 0.f);
+    float4 tp = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t ti = 0xffffffffu;
+    if (pv) {
+      q = xf_apply(s_T, p.x, p.y, p.z);
+      tp = prm->hard_tp[slot];
+      ti = prm->hard_ti[slot];
+    }
+    float t[32];
+    corr_terms<P2PL>(t, pv && ti != 0xffffffffu, q, tp, tp.w, ti, prm);
+    prm->tile_part[slot] = reduce_scatter32(t, lane);
+  }
+}
+
+// Pass 4: fixed-order FP64 reduction of the per-tile sums: block b owns a
+// contiguous range of tiles, 8 sub-slices x 32 terms per block.
+__global__ void __launch_bounds__(256) k_icp_reduce(const IcpParams* __restrict__ prm, const IcpState* st,
+                                                   double* __restrict__ red) {
+  __shared__ double s[8][32];
+  if (icp_done(st)) return;
+  const int ntiles = prm->src_ntiles;
+  const int chunk = (ntiles + gridDim.x - 1) / gridDim.x;
+  const int t0 = blockIdx.x * chunk, t1 = min(ntiles, t0 + chunk);
+  const int term = threadIdx.x & 31, sub = threadIdx.x >> 5;
+  double acc = 0.0;
+  for (int t = t0 + sub; t < t1; t += 8) acc += static_cast<double>(prm->tile_part[t * 32 + term]);
+  s[sub][term] = acc;
   __syncthreads();
   if (threadIdx.x < 32) {
-    double s = 0.0;
+    double v = 0.0;
 #pragma unroll
-    for (int w = 0; w < kIcpWarps; ++w) s += s_acc[w][threadIdx.x];
-    part[static_cast<size_t>(blockIdx.x) * 32 + threadIdx.x] = s;
+    for (int k = 0; k < 8; ++k) v += s[k][threadIdx.x];
+    red[blockIdx.x * 32 + threadIdx.x] = v;
   }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_flag = (atomicAdd(&st->blocks_done, 1u) == gridDim.x - 1) ? 1 : 0;
-  __syncthreads();
-  if (!s_flag) return;
-  __threadfence();
-  {  // fixed-order FP64 reduction of the block partials: 8 slices x 32 terms
-    const int term = threadIdx.x & 31, slice = threadIdx.x >> 5;
-    double s = 0.0;
-    for (int b = slice; b < static_cast<int>(gridDim.x); b += kIcpWarps) s += __ldcg(&part[static_cast<size_t>(b) * 32 + term]);
-    s_acc[slice][term] = s;
+}
+
+// Pass 5, one block: sum of the block partials in order, FP64 solve, compose,
+// convergence test, counters reset, and the loop condition for the graph.
+template <int P2PL>
+__global__ void __launch_bounds__(kIcpThreads) k_icp_solve(const IcpParams* __restrict__ prm, IcpState* st,
+                                                           const double* __restrict__ red, int nred,
+                                                           cudaGraphConditionalHandle h) {
+  __shared__ double s_acc[kIcpWarps][32];
+  if (icp_done(st)) {
+    if (threadIdx.x == 0 && prm->use_graph) cudaGraphSetConditional(h, 0u);
+    return;
   }
+  const int term = threadIdx.x & 31, slice = threadIdx.x >> 5;
+  double s = 0.0;
+  for (int b = slice; b < nred; b += kIcpWarps) s += red[static_cast<size_t>(b) * 32 + term];
+  s_acc[slice][term] = s;
   __syncthreads();
   if (threadIdx.x == 0) {
     double S[32];
     for (int t = 0; t < 32; ++t) {
-      double s = 0.0;
-      for (int w = 0; w < kIcpWarps; ++w) s += s_acc[w][t];
-      S[t] = s;
+      double v = 0.0;
+      for (int w = 0; w < kIcpWarps; ++w) v += s_acc[w][t];
+      S[t] = v;
     }
     icp_update<P2PL>(S, prm, st);
     st->launches += 1;
     if (st->launches > prm->max_iter + 1) st->done = 1;  // hard bound on the device loop
     st->tile_ctr = 0;
-    st->blocks_done = 0;
-    __threadfence();
+    st->nhard = 0;
+    st->hard_ctr = 0;
+    st->nwide = 0;
+    st->wide_ctr = 0;
     if (prm->use_graph) cudaGraphSetConditional(h, st->done ? 0u : 1u);
   }
 }
 
 // getFitnessScore(): mean squared distance from every transformed source point
-// to its exact (uncapped) nearest target point.
-__global__ void __launch_bounds__(kIcpThreads) k_fitness(const IcpParams* __restrict__ prm, IcpState* st,
-                                                         double* __restrict__ part) {
+// to its exact (uncapped) nearest target point.  Phase 1 searches the tiles with
+// the correspondence cap (a far lane would otherwise widen its whole tile's
+// search); lanes with no target point inside the cap are queued and phase 2
+// finds their nearest point with one warp per query (per-query pruning, the 32
+// lanes scan a leaf together).  Distances land in fd[] by sorted source
+// position and are summed in a fixed order.  The points of a tile wider than
+// four search radii go straight to phase 2.
+__global__ void __launch_bounds__(kIcpThreads) k_fitness(const IcpParams* __restrict__ prm, IcpState* st) {
   __shared__ IndexView s_tgt;
   __shared__ Xf s_T;
   __shared__ WarpScratch wss[kIcpWarps];
-  __shared__ double s_acc[kIcpWarps][2];
-  __shared__ int s_flag;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   if (threadIdx.x == 0) {
     s_tgt = prm->tgt;
@@ -442,55 +564,112 @@ __global__ void __launch_bounds__(kIcpThreads) k_fitness(const IcpParams* __rest
   __syncthreads();
   const float4* __restrict__ src = prm->src_pts;
   const int ntiles = prm->src_ntiles;
-  float acc = 0.f, cmp = 0.f;
-  int cnt = 0;
+  float* __restrict__ fd = prm->fd;
   for (;;) {
     int tile = 0;
     if (lane == 0) tile = static_cast<int>(atomicAdd(&st->fit_tile_ctr, 1u));
     tile = __shfl_sync(LCR_FULL, tile, 0);
     if (tile >= ntiles) break;
-    const float4 p = src[static_cast<size_t>(tile) * 32 + lane];
+    const int pos = tile * 32 + lane;
+    const float4 p = src[pos];
     const bool pv = finite3(p.x, p.y, p.z);
     float3 q = make_float3(0.f, 0.f, 0.f);
     if (pv) q = xf_apply(s_T, p.x, p.y, p.z);
     float4 tlo, thi;
-    if (!tile_box(q.x, q.y, q.z, pv, tlo, thi)) continue;
+    if (!tile_box(q.x, q.y, q.z, pv, tlo, thi)) {
+      fd[pos] = -1.f;
+      continue;
+    }
+    const float dx = thi.x - tlo.x, dy = thi.y - tlo.y, dz = thi.z - tlo.z;
+    if (dx * dx + dy * dy + dz * dz > 16.f * prm->cap) {
+      // wide tile: every point goes to the per-query phase (same exact result)
+      if (pv) prm->far[atomicAdd(&st->nfar, 1u)] = make_float4(q.x, q.y, q.z, __int_as_float(pos));
+      else fd[pos] = -1.f;
+      continue;
+    }
     NN1 v;
-    v.init(q.x, q.y, q.z, pv, LCR_INF, tlo, thi);
+    v.init(q.x, q.y, q.z, pv, prm->cap, wss[wib]);
     tile_traverse(s_tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), wss[wib]);
-    if (pv && v.found()) {
-      kahan_add(acc, cmp, key_dist(v.best));
-      ++cnt;
+    if (!pv) {
+      fd[pos] = -1.f;  // not a point
+    } else if (v.found()) {
+      fd[pos] = key_dist(v.best);
+    } else {
+      const unsigned slot = atomicAdd(&st->nfar, 1u);
+      prm->far[slot] = make_float4(q.x, q.y, q.z, __int_as_float(pos));
     }
   }
-  double s = static_cast<double>(acc) - static_cast<double>(cmp);
-  double c = static_cast<double>(cnt);
+}
+
+__global__ void __launch_bounds__(kIcpThreads) k_fitness_far(const IcpParams* __restrict__ prm, IcpState* st) {
+  __shared__ IndexView s_tgt;
+  __shared__ WarpScratch wss[kIcpWarps];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_tgt = prm->tgt;
+  __syncthreads();
+  const unsigned nfar = *reinterpret_cast<volatile unsigned*>(&st->nfar);
+  for (;;) {
+    unsigned i = 0;
+    if (lane == 0) i = atomicAdd(&st->far_ctr, 1u);
+    i = __shfl_sync(LCR_FULL, i, 0);
+    if (i >= nfar) break;
+    const float4 q = prm->far[i];
+    unsigned long long best;
+    float4 bp;
+    warp_query_nn(s_tgt, q.x, q.y, q.z, LCR_INF, wss[wib], best, bp);
+    if (lane == 0) prm->fd[__float_as_int(q.w)] = key_dist(best);
+  }
+}
+
+// Fixed-order FP64 sum of fd[] (negative entries are not points): contiguous
+// chunks per block, fixed tree inside the block, blocks added in order by the
+// last block.
+__global__ void __launch_bounds__(256) k_fitness_reduce(const IcpParams* __restrict__ prm, IcpState* st,
+                                                        double* __restrict__ part) {
+  __shared__ double s_s[8], s_c[8];
+  __shared__ int s_flag;
+  const int n = prm->src_ntiles * 32;
+  const int chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
+  double s = 0.0, c = 0.0;
+  for (int i = b0 + static_cast<int>(threadIdx.x); i < b1; i += blockDim.x) {
+    const float d = prm->fd[i];
+    if (d >= 0.f) {
+      s += d;
+      c += 1.0;
+    }
+  }
   s = warp_sum(s);
   c = warp_sum(c);
-  if (lane == 0) {
-    s_acc[wib][0] = s;
-    s_acc[wib][1] = c;
+  if ((threadIdx.x & 31) == 0) {
+    s_s[threadIdx.x >> 5] = s;
+    s_c[threadIdx.x >> 5] = c;
   }
   __syncthreads();
-  if (threadIdx.x < 2) {
-    double t = 0.0;
-    for (int w = 0; w < kIcpWarps; ++w) t += s_acc[w][threadIdx.x];
-    part[static_cast<size_t>(blockIdx.x) * 2 + threadIdx.x] = t;
+  if (threadIdx.x == 0) {
+    double ts = 0.0, tc = 0.0;
+    for (int w = 0; w < 8; ++w) {
+      ts += s_s[w];
+      tc += s_c[w];
+    }
+    part[2 * blockIdx.x] = ts;
+    part[2 * blockIdx.x + 1] = tc;
+    __threadfence();
+    s_flag = (atomicAdd(&st->fit_blocks_done, 1u) == gridDim.x - 1) ? 1 : 0;
   }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_flag = (atomicAdd(&st->fit_blocks_done, 1u) == gridDim.x - 1) ? 1 : 0;
   __syncthreads();
   if (!s_flag || threadIdx.x != 0) return;
   __threadfence();
   double ts = 0.0, tc = 0.0;
   for (int b = 0; b < static_cast<int>(gridDim.x); ++b) {
-    ts += __ldcg(&part[static_cast<size_t>(b) * 2]);
-    tc += __ldcg(&part[static_cast<size_t>(b) * 2 + 1]);
+    ts += __ldcg(&part[2 * b]);
+    tc += __ldcg(&part[2 * b + 1]);
   }
   st->fitness = tc > 0 ? ts / tc : DBL_MAX;
   st->fit_tile_ctr = 0;
   st->fit_blocks_done = 0;
+  st->nfar = 0;
+  st->far_ctr = 0;
 }
 
 struct IcpBuffers {
@@ -521,11 +700,15 @@ IcpBuffers icp_buffers(lcr_ctx* ctx, int grid) {
                     reinterpret_cast<double*>(b + 2048)};
 }
 
-int icp_grid(lcr_ctx* ctx) { return ctx->sms * 2; }
+int icp_grid(lcr_ctx* ctx) { return ctx->sms * 4; }
 
-// Builds (once per context and method) the graph WHILE(cond) { k_icp_iter }.
+// Builds (once per context and method) the graph WHILE(cond) { iteration }.
 // Returns nullptr if conditional nodes are unavailable.
 cudaGraphExec_t icp_graph(lcr_ctx* ctx, int p2pl, const IcpBuffers& B) {
+  // LCR_ICP_GRAPH=0 runs the same iteration kernels from a host loop instead
+  // (profilers do not see kernels inside conditional graph bodies).
+  const char* env = std::getenv("LCR_ICP_GRAPH");
+  if (env && env[0] == '0') return nullptr;
   if (ctx->icp_graph_ok == 0) return nullptr;
   if (ctx->icp_exec[p2pl]) return ctx->icp_exec[p2pl];
   cudaGraph_t g = nullptr;
@@ -546,20 +729,35 @@ cudaGraphExec_t icp_graph(lcr_ctx* ctx, int p2pl, const IcpBuffers& B) {
     ok = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
   }
   if (ok) {
+    // body: search, deferred queries, wide-tile terms, fixed-order reduction,
+    // then the one-block FP64 solve that sets the loop condition.
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    cudaKernelNodeParams kp;
-    std::memset(&kp, 0, sizeof(kp));
-    kp.func = p2pl ? reinterpret_cast<void*>(k_icp_iter<1>) : reinterpret_cast<void*>(k_icp_iter<0>);
-    kp.gridDim = dim3(icp_grid(ctx));
-    kp.blockDim = dim3(kIcpThreads);
-    kp.sharedMemBytes = 0;
     const IcpParams* a0 = B.prm;
     IcpState* a1 = B.st;
     double* a2 = B.part;
-    void* args[] = {&a0, &a1, &a2, &h};
-    kp.kernelParams = args;
-    cudaGraphNode_t kn = nullptr;
-    ok = cudaGraphAddKernelNode(&kn, body, nullptr, 0, &kp) == cudaSuccess;
+    int a3 = kIcpReduceBlocks;
+    void* args2[] = {&a0, &a1};
+    void* args_red[] = {&a0, &a1, &a2};
+    void* args_solve[] = {&a0, &a1, &a2, &a3, &h};
+    struct NodeSpec { void* fn; int grid; void** args; };
+    const NodeSpec specs[5] = {
+        {p2pl ? reinterpret_cast<void*>(k_icp_search<1>) : reinterpret_cast<void*>(k_icp_search<0>), icp_grid(ctx), args2},
+        {reinterpret_cast<void*>(k_icp_hard), icp_grid(ctx), args2},
+        {p2pl ? reinterpret_cast<void*>(k_icp_wide<1>) : reinterpret_cast<void*>(k_icp_wide<0>), icp_grid(ctx), args2},
+        {reinterpret_cast<void*>(k_icp_reduce), kIcpReduceBlocks, args_red},
+        {p2pl ? reinterpret_cast<void*>(k_icp_solve<1>) : reinterpret_cast<void*>(k_icp_solve<0>), 1, args_solve}};
+    cudaGraphNode_t prev = nullptr;
+    for (int k = 0; k < 5 && ok; ++k) {
+      cudaKernelNodeParams kp;
+      std::memset(&kp, 0, sizeof(kp));
+      kp.func = specs[k].fn;
+      kp.gridDim = dim3(specs[k].grid);
+      kp.blockDim = dim3(kIcpThreads);
+      kp.kernelParams = specs[k].args;
+      cudaGraphNode_t node = nullptr;
+      ok = cudaGraphAddKernelNode(&node, body, prev ? &prev : nullptr, prev ? 1 : 0, &kp) == cudaSuccess;
+      prev = node;
+    }
   }
   if (ok) ok = cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
   if (g) cudaGraphDestroy(g);
@@ -607,6 +805,19 @@ void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr
   hp->teps = p->transformation_epsilon;
   hp->feps = p->euclidean_fitness_epsilon;
   hp->use_graph = exec ? 1 : 0;
+  const size_t nslots = static_cast<size_t>(si.v.nleaf) * 32;
+  // per-call scratch: fitness slots + far list, tile sums, deferred queries
+  const size_t b_fd = nslots * 4, b_far = nslots * 16, b_part = nslots * 4, b_hq = nslots * 4, b_htp = nslots * 16,
+               b_hti = nslots * 4, b_wide = static_cast<size_t>(si.v.nleaf) * 4;
+  char* callbuf = static_cast<char*>(dev_alloc(ctx, b_fd + b_far + b_part + b_hq + b_htp + b_hti + b_wide + 256));
+  char* cur = callbuf;
+  hp->far = reinterpret_cast<float4*>(cur); cur += b_far;
+  hp->hard_tp = reinterpret_cast<float4*>(cur); cur += b_htp;
+  hp->fd = reinterpret_cast<float*>(cur); cur += b_fd;
+  hp->tile_part = reinterpret_cast<float*>(cur); cur += b_part;
+  hp->hard_q = reinterpret_cast<uint32_t*>(cur); cur += b_hq;
+  hp->hard_ti = reinterpret_cast<uint32_t*>(cur); cur += b_hti;
+  hp->wide_tiles = reinterpret_cast<uint32_t*>(cur);
   const double I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
   for (int i = 0; i < 16; ++i) hs->T[i] = guess ? static_cast<double>(guess[i]) : I[i];
   for (int i = 0; i < 12; ++i) hs->Tf.m[i] = static_cast<float>(hs->T[i]);
@@ -618,8 +829,14 @@ void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr
   } else {
     cudaGraphConditionalHandle none = 0;
     for (int it = 0; it < p->max_iterations; ++it) {
-      if (p2pl) LCR_LAUNCH(ctx, k_icp_iter<1>, grid, kIcpThreads, 0, B.prm, B.st, B.part, none);
-      else LCR_LAUNCH(ctx, k_icp_iter<0>, grid, kIcpThreads, 0, B.prm, B.st, B.part, none);
+      if (p2pl) LCR_LAUNCH(ctx, k_icp_search<1>, grid, kIcpThreads, 0, B.prm, B.st);
+      else LCR_LAUNCH(ctx, k_icp_search<0>, grid, kIcpThreads, 0, B.prm, B.st);
+      LCR_LAUNCH(ctx, k_icp_hard, grid, kIcpThreads, 0, B.prm, B.st);
+      if (p2pl) LCR_LAUNCH(ctx, k_icp_wide<1>, grid, kIcpThreads, 0, B.prm, B.st);
+      else LCR_LAUNCH(ctx, k_icp_wide<0>, grid, kIcpThreads, 0, B.prm, B.st);
+      LCR_LAUNCH(ctx, k_icp_reduce, kIcpReduceBlocks, 256, 0, B.prm, B.st, B.part);
+      if (p2pl) LCR_LAUNCH(ctx, k_icp_solve<1>, 1, kIcpThreads, 0, B.prm, B.st, B.part, kIcpReduceBlocks, none);
+      else LCR_LAUNCH(ctx, k_icp_solve<0>, 1, kIcpThreads, 0, B.prm, B.st, B.part, kIcpReduceBlocks, none);
       if ((it & 7) == 7) {
         int* hd = static_cast<int*>(pinned(ctx, 2048)) + 384;
         CUDA_TRY(cudaMemcpyAsync(hd, &B.st->done, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -628,10 +845,15 @@ void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr
       }
     }
   }
-  if (p->compute_fitness) LCR_LAUNCH(ctx, k_fitness, grid, kIcpThreads, 0, B.prm, B.st, B.part);
+  if (p->compute_fitness) {
+    LCR_LAUNCH(ctx, k_fitness, grid, kIcpThreads, 0, B.prm, B.st);
+    LCR_LAUNCH(ctx, k_fitness_far, grid, kIcpThreads, 0, B.prm, B.st);
+    LCR_LAUNCH(ctx, k_fitness_reduce, std::min(grid, 256), 256, 0, B.prm, B.st, B.part);
+  }
   CUDA_TRY(cudaMemcpyAsync(hs, B.st, sizeof(IcpState), cudaMemcpyDeviceToHost, ctx->stream));
+  dev_free(ctx, callbuf);
   sync(ctx);
-  if (exec) ctx->launches += static_cast<uint64_t>(hs->launches);
+  if (exec) ctx->launches += 5 * static_cast<uint64_t>(hs->launches);  // five kernels per body run
   std::memset(res, 0, sizeof(*res));
   for (int i = 0; i < 16; ++i) {
     res->transform64[i] = hs->T[i];

@@ -17,33 +17,32 @@ __global__ void k_fill_knn(int32_t* __restrict__ idx, float* __restrict__ dist, 
 
 // Queries are the Morton-sorted points of the query cloud's own index; results
 // are scattered back to the query's original position.
-__global__ void k_knn(IndexView ref, IndexView qry, int K, float cap, int32_t* __restrict__ oidx,
+__global__ void k_knn(IndexView ref, IndexView qry, int K, float cap, int self, int32_t* __restrict__ oidx,
                       float* __restrict__ odist) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  WarpScratch& ws = reinterpret_cast<WarpScratch*>(smem)[wib];
+  const size_t wbytes = K == 1 ? sizeof(WarpScratch) : knn_warp_bytes(K);
+  unsigned char* wbase = smem + wib * wbytes;
+  WarpScratch& ws = *reinterpret_cast<WarpScratch*>(wbase);
   const int tile = blockIdx.x * nw + wib;
   if (tile >= qry.nleaf) return;
   const float4 q = qry.pts[static_cast<size_t>(tile) * 32 + lane];
   const bool qv = finite3(q.x, q.y, q.z);
   float4 tlo, thi;
   if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
-  const float cx = 0.5f * (tlo.x + thi.x), cy = 0.5f * (tlo.y + thi.y), cz = 0.5f * (tlo.z + thi.z);
   const uint32_t orig = __float_as_uint(q.w);
   if (K == 1) {
     NN1 v;
-    v.init(q.x, q.y, q.z, qv, cap, tlo, thi);
-    tile_traverse(ref, v, cx, cy, cz, ws);
+    tile_nn1(ref, q.x, q.y, q.z, qv, cap, tlo, thi, ws, v);
     if (qv && v.found()) {
       oidx[orig] = static_cast<int32_t>(key_idx(v.best));
       odist[orig] = key_dist(v.best);
     }
   } else {
-    unsigned long long* list =
-        reinterpret_cast<unsigned long long*>(smem + nw * sizeof(WarpScratch)) + static_cast<size_t>(wib) * K * 32;
-    NNK v;
-    v.init(q.x, q.y, q.z, qv, cap, K, list, tlo, thi);
-    tile_traverse(ref, v, cx, cy, cz, ws);
+    unsigned char* region = wbase + sizeof(KnnWarp);
+    const unsigned long long* list = reinterpret_cast<const unsigned long long*>(region);
+    tile_knn(ref, q.x, q.y, q.z, qv, K, cap, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), region,
+             self ? tile : -1);
     if (qv) {
       for (int j = 0; j < K; ++j) {
         const unsigned long long k = list[j * 32 + lane];
@@ -69,8 +68,7 @@ __global__ void k_corr(IndexView tgt, IndexView src, Xf T, float cap, int32_t* _
   float4 tlo, thi;
   if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
   NN1 v;
-  v.init(q.x, q.y, q.z, qv, cap, tlo, thi);
-  tile_traverse(tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), wss[wib]);
+  tile_nn1(tgt, q.x, q.y, q.z, qv, cap, tlo, thi, wss[wib], v);
   if (qv && v.found()) {
     const uint32_t orig = __float_as_uint(p.w);
     oidx[orig] = static_cast<int32_t>(key_idx(v.best));
@@ -97,12 +95,12 @@ void knn_run(lcr_ctx* ctx, const lcr_cloud* ref, const lcr_cloud* query, int k, 
   if (ref->n == 0) return;
   const IndexView rv = cloud_index(ctx, ref).v;
   const IndexView qv = cloud_index(ctx, query).v;
-  const int nw = k == 1 ? 8 : 4;
-  const size_t smem = nw * (sizeof(WarpScratch) + (k > 1 ? static_cast<size_t>(k) * 32 * 8 : 0));
+  const int nw = k == 1 ? 8 : (k <= 64 ? 4 : 2);
+  const size_t smem = nw * (k == 1 ? sizeof(WarpScratch) : knn_warp_bytes(k));
   if (smem > 227 * 1024) LCR_THROW(LCR_ERR_INVALID_ARG, "k=%d too large", k);
   CUDA_TRY(cudaFuncSetAttribute(k_knn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   const int grid = (qv.nleaf + nw - 1) / nw;
-  LCR_LAUNCH(ctx, k_knn, grid, nw * 32, smem, rv, qv, k, cap, d_idx, d_dist);
+  LCR_LAUNCH(ctx, k_knn, grid, nw * 32, smem, rv, qv, k, cap, ref == query ? 1 : 0, d_idx, d_dist);
 }
 
 void corr_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const double* T, double dmax, int32_t* d_idx,

@@ -11,28 +11,97 @@ namespace {
 // outlier_removal.cpp:80-84.  kNN with k+1 results (the query itself first),
 // mean of sqrt(d) over results 1..k summed in double in ascending order
 // (float sqrt, as std::sqrt on a float), stored as float.
+//
+// Fast form: the k+1 nearest as an unordered set (tile_kset).  The ascending
+// double sum equals the exact sum, in any order, whenever no partial sum can
+// round: all terms are non-negative multiples of u = the smallest ulp among the
+// nonzero float terms, so every partial sum is a multiple of u no larger than
+// the total T, and T < 2^53 u makes all of them representable.  Then
+// sum(results 1..k) = T - sqrt(d_min) exactly.  A tile with a lane that fails
+// the test (a dynamic range above ~2^23 between neighbour distances) is
+// queued and redone by k_sor_dist_sorted.
+struct SorAcc {
+  double sum;
+  float dmin;
+  int emin;  // smallest biased exponent (>= 1) of a nonzero term
+  __device__ __forceinline__ void add_d(float d) {
+    const float v = __fsqrt_rn(d);
+    sum = __dadd_rn(sum, static_cast<double>(v));
+    dmin = fminf(dmin, d);
+    if (v > 0.f) emin = min(emin, max(1, static_cast<int>(__float_as_uint(v) >> 23)));
+  }
+  __device__ __forceinline__ void add(const float4&, float d) { add_d(d); }
+  __device__ __forceinline__ void add_key(unsigned long long k) { add_d(key_dist(k)); }
+  // true if the sum is exact; s = sum of all terms but the smallest
+  __device__ __forceinline__ bool result(double& s) const {
+    // ulp of a float with biased exponent e is 2^(max(e,1) - 150); bound 2^(emin - 97)
+    const double bound = emin >= 255 ? LCR_INF : __longlong_as_double(static_cast<long long>(emin - 97 + 1023) << 52);
+    if (!(sum < bound)) return false;
+    s = __dsub_rn(sum, static_cast<double>(__fsqrt_rn(dmin)));
+    return true;
+  }
+};
+
+__device__ __forceinline__ void sor_store(const float4& q, double s, int mean_k, float* __restrict__ dist,
+                                          uint8_t* __restrict__ valid, unsigned int* __restrict__ nvalid) {
+  const uint32_t o = __float_as_uint(q.w);
+  dist[o] = __double2float_rn(__ddiv_rn(s, static_cast<double>(mean_k)));
+  valid[o] = 1;
+  atomicAdd(nvalid, 1u);
+}
+
 __global__ void k_sor_dist(IndexView ix, int mean_k, float* __restrict__ dist, uint8_t* __restrict__ valid,
-                           unsigned int* __restrict__ nvalid) {
+                           unsigned int* __restrict__ nvalid, uint32_t* __restrict__ redo, unsigned int* nredo) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int K = mean_k + 1;
-  unsigned char* wbase = smem + wib * knn_warp_bytes(K);
-  unsigned char* region = wbase + sizeof(KnnWarp);
-  const unsigned long long* list = reinterpret_cast<const unsigned long long*>(region);
+  unsigned char* wbase = smem + wib * kset_warp_bytes();
   const int tile = blockIdx.x * nw + wib;
   if (tile >= ix.nleaf) return;
   const float4 q = ix.pts[static_cast<size_t>(tile) * 32 + lane];
   const bool qv = finite3(q.x, q.y, q.z);
   float4 tlo, thi;
   if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
-  tile_knn(ix, q.x, q.y, q.z, qv, K, LCR_INF, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), region, tile);
-  if (!qv) return;
+  SorAcc acc;
+  acc.sum = 0.0;
+  acc.dmin = LCR_INF;
+  acc.emin = 255;
+  tile_kset(ix, q.x, q.y, q.z, qv, K, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), wbase + sizeof(KnnWarp), tile,
+            acc);
   double s = 0.0;
-  for (int j = 1; j < K; ++j) s = __dadd_rn(s, static_cast<double>(__fsqrt_rn(key_dist(list[j * 32 + lane]))));
-  const uint32_t o = __float_as_uint(q.w);
-  dist[o] = __double2float_rn(__ddiv_rn(s, static_cast<double>(mean_k)));
-  valid[o] = 1;
-  atomicAdd(nvalid, 1u);
+  if (!__all_sync(LCR_FULL, !qv || acc.result(s))) {
+    if (lane == 0) redo[atomicAdd(nredo, 1u)] = static_cast<uint32_t>(tile);
+    return;
+  }
+  if (qv) sor_store(q, s, mean_k, dist, valid, nvalid);
+}
+
+// Sorted form for the queued tiles: the ascending double sum over the sorted
+// k+1 nearest, one warp per tile, warps striding over the queue.
+__global__ void k_sor_dist_sorted(IndexView ix, int mean_k, float* __restrict__ dist, uint8_t* __restrict__ valid,
+                                  unsigned int* __restrict__ nvalid, const uint32_t* __restrict__ redo,
+                                  const unsigned int* nredo) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int K = mean_k + 1;
+  unsigned char* wbase = smem + wib * knn_warp_bytes(K);
+  unsigned char* region = wbase + sizeof(KnnWarp);
+  const unsigned long long* list = reinterpret_cast<const unsigned long long*>(region);
+  const unsigned int count = *nredo;
+  for (unsigned int i = blockIdx.x * nw + wib; i < count; i += gridDim.x * nw) {
+    const int tile = static_cast<int>(redo[i]);
+    const float4 q = ix.pts[static_cast<size_t>(tile) * 32 + lane];
+    const bool qv = finite3(q.x, q.y, q.z);
+    float4 tlo, thi;
+    if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) continue;
+    tile_knn(ix, q.x, q.y, q.z, qv, K, LCR_INF, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), region, tile);
+    if (qv) {
+      double s = 0.0;
+      for (int j = 1; j < K; ++j) s = __dadd_rn(s, static_cast<double>(__fsqrt_rn(key_dist(list[j * 32 + lane]))));
+      sor_store(q, s, mean_k, dist, valid, nvalid);
+    }
+    __syncwarp();
+  }
 }
 
 // Fixed blocked order: chunks of 256 consecutive terms summed sequentially
@@ -98,8 +167,9 @@ __device__ void smallest_eig(const double C[6], double& lam, double n[3]) {
   double s = 0.0;
   for (int i = 0; i < 6; ++i) s = fmax(s, fabs(C[i]));
   if (!(s > 0.0)) {
+    // all neighbours coincide: no plane (PCL's eigen33 divides 0 by 0 here)
     lam = 0.0;
-    n[0] = 0.0; n[1] = 0.0; n[2] = 1.0;
+    n[0] = n[1] = n[2] = __longlong_as_double(0x7ff8000000000000ll);
     return;
   }
   const double a00 = C[0] / s, a01 = C[1] / s, a02 = C[2] / s, a11 = C[3] / s, a12 = C[4] / s, a22 = C[5] / s;
@@ -175,54 +245,69 @@ __device__ void smallest_eig(const double C[6], double& lam, double n[3]) {
 
 // normal_estimation.cpp:84-118: kNN(k) including the point itself, covariance,
 // eigenvector of the smallest eigenvalue, curvature = |l0 / trace|, flipped so
-// that (vp - p).n >= 0, optionally negated afterwards.
+// that (vp - p).n >= 0, optionally negated afterwards.  The covariance sums run
+// in FP32 over offsets from the query point, in the order the unordered k-NN
+// set reduction meets the neighbours; the eigen-solve is FP64.
+struct NeAcc {
+  float qx, qy, qz;
+  const float4* __restrict__ xyz;
+  float sx, sy, sz, sxx, sxy, sxz, syy, syz, szz;
+  int m;
+  __device__ __forceinline__ void init(float x, float y, float z, const float4* p) {
+    qx = x; qy = y; qz = z;
+    xyz = p;
+    sx = sy = sz = sxx = sxy = sxz = syy = syz = szz = 0.f;
+    m = 0;
+  }
+  __device__ __forceinline__ void add(const float4& p, float) {
+    const float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+    sx += dx; sy += dy; sz += dz;
+    sxx += dx * dx; sxy += dx * dy; sxz += dx * dz;
+    syy += dy * dy; syz += dy * dz; szz += dz * dz;
+    ++m;
+  }
+  __device__ __forceinline__ void add_key(unsigned long long k) { add(xyz[key_idx(k)], 0.f); }
+};
+
+__device__ __forceinline__ void normal_store(const NeAcc& a, float vx, float vy, float vz, int flip_all, uint32_t o,
+                                             float4* __restrict__ onrm) {
+  const float nan = __int_as_float(0x7fc00000);
+  if (a.m < 3) {
+    onrm[o] = make_float4(nan, nan, nan, nan);
+    return;
+  }
+  const double im = 1.0 / a.m;
+  const double mx = a.sx * im, my = a.sy * im, mz = a.sz * im;
+  const double C[6] = {a.sxx * im - mx * mx, a.sxy * im - mx * my, a.sxz * im - mx * mz,
+                       a.syy * im - my * my, a.syz * im - my * mz, a.szz * im - mz * mz};
+  double lam, nn[3];
+  smallest_eig(C, lam, nn);
+  const double tr = C[0] + C[3] + C[5];
+  const double curv = tr != 0.0 ? fabs(lam / tr) : 0.0;
+  const double cs = static_cast<double>(__fsub_rn(vx, a.qx)) * nn[0] + static_cast<double>(__fsub_rn(vy, a.qy)) * nn[1] +
+                    static_cast<double>(__fsub_rn(vz, a.qz)) * nn[2];
+  double sgn = cs < 0 ? -1.0 : 1.0;
+  if (flip_all) sgn = -sgn;
+  onrm[o] = make_float4(static_cast<float>(sgn * nn[0]), static_cast<float>(sgn * nn[1]),
+                        static_cast<float>(sgn * nn[2]), static_cast<float>(curv));
+}
+
 __global__ void k_normals(IndexView ix, int K, const float4* __restrict__ xyz, float vx, float vy, float vz,
                           int flip_all, float4* __restrict__ onrm) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  unsigned char* wbase = smem + wib * knn_warp_bytes(K);
-  unsigned char* region = wbase + sizeof(KnnWarp);
-  const unsigned long long* list = reinterpret_cast<const unsigned long long*>(region);
+  unsigned char* wbase = smem + wib * kset_warp_bytes();
   const int tile = blockIdx.x * nw + wib;
   if (tile >= ix.nleaf) return;
   const float4 q = ix.pts[static_cast<size_t>(tile) * 32 + lane];
   const bool qv = finite3(q.x, q.y, q.z);
   float4 tlo, thi;
   if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
-  tile_knn(ix, q.x, q.y, q.z, qv, K, LCR_INF, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), region, tile);
-  if (!qv) return;
-  const uint32_t o = __float_as_uint(q.w);
-  float sx = 0.f, sy = 0.f, sz = 0.f, sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
-  int m = 0;
-  for (int j = 0; j < K; ++j) {
-    const uint32_t id = key_idx(list[j * 32 + lane]);
-    if (id == 0xffffffffu) break;
-    const float4 p = xyz[id];
-    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-    sx += dx; sy += dy; sz += dz;
-    sxx += dx * dx; sxy += dx * dy; sxz += dx * dz;
-    syy += dy * dy; syz += dy * dz; szz += dz * dz;
-    ++m;
-  }
-  const float nan = __int_as_float(0x7fc00000);
-  if (m < 3) {
-    onrm[o] = make_float4(nan, nan, nan, nan);
-    return;
-  }
-  const double im = 1.0 / m;
-  const double mx = sx * im, my = sy * im, mz = sz * im;
-  const double C[6] = {sxx * im - mx * mx, sxy * im - mx * my, sxz * im - mx * mz,
-                       syy * im - my * my, syz * im - my * mz, szz * im - mz * mz};
-  double lam, nn[3];
-  smallest_eig(C, lam, nn);
-  const double tr = C[0] + C[3] + C[5];
-  const double curv = tr != 0.0 ? fabs(lam / tr) : 0.0;
-  const double cs = static_cast<double>(__fsub_rn(vx, q.x)) * nn[0] + static_cast<double>(__fsub_rn(vy, q.y)) * nn[1] +
-                    static_cast<double>(__fsub_rn(vz, q.z)) * nn[2];
-  double sgn = cs < 0 ? -1.0 : 1.0;
-  if (flip_all) sgn = -sgn;
-  onrm[o] = make_float4(static_cast<float>(sgn * nn[0]), static_cast<float>(sgn * nn[1]),
-                        static_cast<float>(sgn * nn[2]), static_cast<float>(curv));
+  NeAcc acc;
+  acc.init(q.x, q.y, q.z, xyz);
+  tile_kset(ix, q.x, q.y, q.z, qv, K, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), wbase + sizeof(KnnWarp), tile,
+            acc);
+  if (qv) normal_store(acc, vx, vy, vz, flip_all, __float_as_uint(q.w), onrm);
 }
 
 // ----------------------------------------------------------------- crop
@@ -283,6 +368,25 @@ __global__ void k_crop(IndexView tgt, IndexView src, double r, uint8_t* __restri
 
 size_t list_smem(int nw, int K) { return nw * knn_warp_bytes(K); }
 
+// Warps per block of the unordered k-NN kernels (12 KB of shared memory per
+// warp: 6 warps x 3 blocks = 18 resident warps per SM).
+constexpr int kSetWarps = 6;
+
+// Queue of tiles the unordered form hands to the sorted form: [0] = count,
+// [1..] = tile ids.  Its grid: one block per SM, warps striding the queue.
+struct RedoQueue {
+  uint32_t* block;
+  unsigned int* count() const { return reinterpret_cast<unsigned int*>(block); }
+  uint32_t* tiles() const { return block + 1; }
+};
+
+RedoQueue redo_queue(lcr_ctx* ctx, int nleaf) {
+  RedoQueue q;
+  q.block = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * (static_cast<size_t>(nleaf) + 1)));
+  CUDA_TRY(cudaMemsetAsync(q.block, 0, sizeof(uint32_t), ctx->stream));
+  return q;
+}
+
 int finite_count(lcr_ctx* ctx, const lcr_cloud* in) {
   double c4[4];
   centroid_run(ctx, in, c4);
@@ -303,6 +407,7 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
   const int nw = K <= 64 ? 4 : 2;
   const size_t smem = list_smem(nw, K);
   if (smem > 227 * 1024) LCR_THROW(LCR_ERR_INVALID_ARG, "mean_k=%d too large", mean_k);
+  const size_t smem_set = kSetWarps * kset_warp_bytes();
   float* dist = static_cast<float*>(dev_alloc(ctx, sizeof(float) * n));
   uint8_t* flags = static_cast<uint8_t*>(dev_alloc(ctx, 3 * static_cast<size_t>(n)));
   uint8_t* valid = flags, *keep = flags + n, *drop = flags + 2 * static_cast<size_t>(n);
@@ -313,8 +418,14 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
   CUDA_TRY(cudaMemsetAsync(dist, 0, sizeof(float) * n, ctx->stream));
   CUDA_TRY(cudaMemsetAsync(valid, 0, n, ctx->stream));
   CUDA_TRY(cudaMemsetAsync(nvalid, 0, sizeof(unsigned int), ctx->stream));
-  CUDA_TRY(cudaFuncSetAttribute(k_sor_dist, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  LCR_LAUNCH(ctx, k_sor_dist, (ix.nleaf + nw - 1) / nw, nw * 32, smem, ix, mean_k, dist, valid, nvalid);
+  const RedoQueue rq = redo_queue(ctx, ix.nleaf);
+  CUDA_TRY(cudaFuncSetAttribute(k_sor_dist, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_set)));
+  CUDA_TRY(cudaFuncSetAttribute(k_sor_dist_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(smem)));
+  LCR_LAUNCH(ctx, k_sor_dist, (ix.nleaf + kSetWarps - 1) / kSetWarps, kSetWarps * 32, smem_set, ix, mean_k, dist,
+             valid, nvalid, rq.tiles(), rq.count());
+  LCR_LAUNCH(ctx, k_sor_dist_sorted, ctx->sms, nw * 32, smem, ix, mean_k, dist, valid, nvalid, rq.tiles(), rq.count());
+  dev_free(ctx, rq.block);
   // blocked sums (ping-pong between two halves of `sums`)
   double *a = sums, *b = sums + nc0, *a2 = sums + 2 * nc0, *b2 = sums + 3 * nc0;
   int m = nc0;
@@ -364,16 +475,15 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
   lcr_cloud* out = cloud_alloc(ctx, n);
   if (n == 0) return out;
   const IndexView ix = cloud_index(ctx, in).v;
-  const int nw = k <= 64 ? 4 : 2;
-  const size_t smem = list_smem(nw, k);
-  if (smem > 227 * 1024) LCR_THROW(LCR_ERR_INVALID_ARG, "k=%d too large", k);
   CUDA_TRY(cudaMemcpyAsync(out->xyz, in->xyz, sizeof(float4) * n, cudaMemcpyDeviceToDevice, ctx->stream));
   CUDA_TRY(cudaMemcpyAsync(out->rgb, in->rgb, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
   // non-finite points keep NaN normals (they are not searched)
   CUDA_TRY(cudaMemsetAsync(out->nrm, 0xff, sizeof(float4) * n, ctx->stream));
-  CUDA_TRY(cudaFuncSetAttribute(k_normals, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  LCR_LAUNCH(ctx, k_normals, (ix.nleaf + nw - 1) / nw, nw * 32, smem, ix, k, in->xyz, vp[0], vp[1], vp[2],
-             (flags & LCR_NORMALS_FLIP_ALL) ? 1 : 0, out->nrm);
+  const size_t smem_set = kSetWarps * kset_warp_bytes();
+  const int flip = (flags & LCR_NORMALS_FLIP_ALL) ? 1 : 0;
+  CUDA_TRY(cudaFuncSetAttribute(k_normals, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_set)));
+  LCR_LAUNCH(ctx, k_normals, (ix.nleaf + kSetWarps - 1) / kSetWarps, kSetWarps * 32, smem_set, ix, k, in->xyz, vp[0],
+             vp[1], vp[2], flip, out->nrm);
   return out;
 }
 

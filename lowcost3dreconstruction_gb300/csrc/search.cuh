@@ -461,22 +461,36 @@ struct KCollect {
   __device__ __forceinline__ void refresh() {}
 };
 
-// Runs both passes for the warp's tile.  Afterwards list = region as
-// unsigned long long [.][32] holds each lane's sorted k nearest keys in its
-// first K rows (missing entries: key (inf, 0xffffffff)).  When the queries are
-// the points of leaf `self_leaf` of ix itself, that leaf and its two neighbours
-// on each side along the Hilbert order are scanned first: they settle the
-// per-lane bounds before the traversal starts (16x fewer leaf visits on
-// depth-camera clouds than traversal order alone).  self_leaf < 0: no seeding.
-__device__ __forceinline__ void tile_knn(const IndexView& ix, float qx, float qy, float qz, bool qv, int K, float cap,
-                                         const float4& tlo, const float4& thi, KnnWarp& kw, unsigned char* region,
-                                         int self_leaf = -1) {
+// Pass 1 for the warp's tile (traversal + histogram, see KHist).  When the
+// queries are the points of leaf `self_leaf` of ix itself, that leaf and its
+// two neighbours on each side along the Hilbert order are scanned first: they
+// settle the per-lane bounds before the traversal starts (16x fewer leaf visits
+// on depth-camera clouds than traversal order alone).  self_leaf < 0: no
+// seeding.  Afterwards kw.leaves holds the scanned leaves (h.nleaves of them).
+__device__ __forceinline__ void knn_pass1(const IndexView& ix, float qx, float qy, float qz, bool qv, int K, float cap,
+                                          const float4& tlo, const float4& thi, KnnWarp& kw, unsigned char* region,
+                                          int self_leaf, KHist& h) {
   const int lane = threadIdx.x & 31;
-  const float cx = 0.5f * (tlo.x + thi.x), cy = 0.5f * (tlo.y + thi.y), cz = 0.5f * (tlo.z + thi.z);
-  // bins span 16 octaves of d^2 below (16 x tile diagonal)^2
+  // Each lane's bins span 16 octaves of d^2 below min(16 x the tile diagonal,
+  // 64 x the distance to the nearer of its two neighbours along the Hilbert
+  // order)^2: the second term keeps the range local in a tile whose queries
+  // straddle distant surfaces (there the tile diagonal would push every
+  // neighbour into the lowest, clamped bin).
   const float dx = thi.x - tlo.x, dy = thi.y - tlo.y, dz = thi.z - tlo.z;
-  const float top2 = fmaxf(256.f * (dx * dx + dy * dy + dz * dz), 1e-30f);
-  KHist h;
+  float top2 = 256.f * (dx * dx + dy * dy + dz * dz);
+  {
+    const float ux = __shfl_up_sync(LCR_FULL, qx, 1), uy = __shfl_up_sync(LCR_FULL, qy, 1),
+                uz = __shfl_up_sync(LCR_FULL, qz, 1);
+    const float wx = __shfl_down_sync(LCR_FULL, qx, 1), wy = __shfl_down_sync(LCR_FULL, qy, 1),
+                wz = __shfl_down_sync(LCR_FULL, qz, 1);
+    const bool uv = __shfl_up_sync(LCR_FULL, qv, 1) && lane > 0;
+    const bool wv = __shfl_down_sync(LCR_FULL, qv, 1) && lane < 31;
+    float sp = LCR_INF;
+    if (qv && uv) sp = exact_dist2(qx, qy, qz, ux, uy, uz);
+    if (qv && wv) sp = fminf(sp, exact_dist2(qx, qy, qz, wx, wy, wz));
+    if (sp > 0.f && sp < LCR_INF) top2 = fminf(top2, 4096.f * sp);
+  }
+  top2 = fmaxf(top2, 1e-30f);
   h.qx = qx; h.qy = qy; h.qz = qz; h.qv = qv;
   h.K = K; h.lane = lane;
   h.e0 = static_cast<int>(__float_as_uint(top2) >> 21) - (kBins - 1);
@@ -499,8 +513,42 @@ __device__ __forceinline__ void tile_knn(const IndexView& ix, float qx, float qy
       if (self_leaf + d < ix.nleaf) h.scan_leaf(ix, self_leaf + d, kw.ws);
     }
   }
-  tile_traverse(ix, h, cx, cy, cz, kw.ws);
+  tile_traverse(ix, h, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), kw.ws);
   __syncwarp();
+}
+
+// Pass 2 over the leaves pass 1 scanned (or a re-traversal when they did not
+// fit the leaf list).  vis.need() is re-evaluated per leaf with the final bound.
+template <class V>
+__device__ __forceinline__ void knn_pass2(const IndexView& ix, const KHist& h, V& vis, const float4& tlo,
+                                          const float4& thi, KnnWarp& kw) {
+  const int lane = threadIdx.x & 31;
+  if (h.nleaves <= kLeafList) {
+    for (int l = 0; l < h.nleaves; ++l) {
+      const int id = static_cast<int>(kw.leaves[l]);
+      const float4 lo = ix.lo[0][id], hi = ix.hi[0][id];
+      const bool nd = vis.need(lo, hi);
+      if (!__any_sync(LCR_FULL, nd)) continue;
+      kw.ws.stage[lane] = ix.pts[static_cast<size_t>(id) * 32 + lane];
+      __syncwarp();
+      if (nd) vis.scan(kw.ws.stage);
+      __syncwarp();
+    }
+  } else {
+    tile_traverse(ix, vis, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), kw.ws);
+  }
+  __syncwarp();
+}
+
+// Runs both passes for the warp's tile.  Afterwards list = region as
+// unsigned long long [.][32] holds each lane's sorted k nearest keys in its
+// first K rows (missing entries: key (inf, 0xffffffff)).
+__device__ __forceinline__ void tile_knn(const IndexView& ix, float qx, float qy, float qz, bool qv, int K, float cap,
+                                         const float4& tlo, const float4& thi, KnnWarp& kw, unsigned char* region,
+                                         int self_leaf = -1) {
+  const int lane = threadIdx.x & 31;
+  KHist h;
+  knn_pass1(ix, qx, qy, qz, qv, K, cap, tlo, thi, kw, region, self_leaf, h);
   const float tau = h.bound();
   const int cnt = h.cl;
   KCollect c;
@@ -514,21 +562,7 @@ __device__ __forceinline__ void tile_knn(const IndexView& ix, float qx, float qy
   if (c.insert)
     for (int j = 0; j < K; ++j) c.buf[j * 32 + lane] = none;
   __syncwarp();
-  if (h.nleaves <= kLeafList) {
-    for (int l = 0; l < h.nleaves; ++l) {
-      const int id = static_cast<int>(kw.leaves[l]);
-      const float4 lo = ix.lo[0][id], hi = ix.hi[0][id];
-      const bool nd = c.need(lo, hi);
-      if (!__any_sync(LCR_FULL, nd)) continue;
-      kw.ws.stage[lane] = ix.pts[static_cast<size_t>(id) * 32 + lane];
-      __syncwarp();
-      if (nd) c.scan(kw.ws.stage);
-      __syncwarp();
-    }
-  } else {
-    tile_traverse(ix, c, cx, cy, cz, kw.ws);
-  }
-  __syncwarp();
+  knn_pass2(ix, h, c, tlo, thi, kw);
   if (!c.insert) {
     unsigned long long* b = c.buf;
     const int n = c.cnt;
@@ -544,6 +578,191 @@ __device__ __forceinline__ void tile_knn(const IndexView& ix, float qx, float qy
       b[j * 32 + lane] = k;
     }
     for (int j = n; j < K; ++j) b[j * 32 + lane] = none;
+  }
+  __syncwarp();
+}
+
+// ------------------------------------------------ unordered k-NN reductions
+// Statistics over the set of k nearest neighbours (a sum, a covariance) need
+// the set, not its order.  After pass 1 every lane knows the bin holding its
+// k-th key and the count of candidates in lower bins; those are all among the
+// k nearest.  The boundary is kept as a key range [klo, khi] with the number m
+// of keys still needed from it.  While some lane's range holds more than
+// kBoundCap candidates (equal or nearly equal distances, a clamped bin), a
+// refinement pass splits the range into 64 sub-ranges of the (distance, index)
+// key and keeps the one holding the m-th key (radix selection: keys are unique,
+// so this ends).  The collect pass then hands every key below klo to an
+// accumulator and buffers the boundary keys, from which the m smallest are
+// selected exactly.  No per-lane sorted list: about half the shared memory of
+// tile_knn and no O(k^2) sort.
+constexpr int kBoundCap = 32;
+
+__host__ __device__ inline size_t kset_warp_bytes() {
+  const size_t buf = static_cast<size_t>(kBoundCap) * 32 * 8;
+  const size_t hist = static_cast<size_t>(kBins) * 32 * 4;
+  return sizeof(KnnWarp) + (buf > hist ? buf : hist);
+}
+
+// Pruning radius of a boundary key range: its largest distance.
+__device__ __forceinline__ float range_tau(unsigned long long khi) { return key_dist(khi); }
+
+// Refinement pass: per-lane histogram of the keys in [klo, khi] over 64
+// sub-ranges of width 2^sh (lanes with active == false only follow along).
+struct KRefine {
+  float qx, qy, qz;
+  bool qv, active;
+  int lane, sh;
+  unsigned long long klo, khi;
+  float tau;
+  uint32_t* hist;
+  WarpScratch* ws;
+  float R;
+  __device__ __forceinline__ float metric(const float4& lo, const float4& hi) const {
+    return subtile_metric(lo, hi, *ws);
+  }
+  __device__ __forceinline__ bool still(float m) const { return m <= R; }
+  __device__ __forceinline__ bool need(const float4& lo, const float4& hi) const {
+    return active && box_dist2(lo, hi, qx, qy, qz) <= tau;
+  }
+  __device__ __forceinline__ void scan(const float4* st) {
+    for (int j = 0; j < 32; ++j) {
+      const float4 p = st[j];
+      const float d = exact_dist2(qx, qy, qz, p.x, p.y, p.z);
+      if (!(d <= tau)) continue;
+      const unsigned long long k = make_key(d, __float_as_uint(p.w));
+      if (k < klo || k > khi) continue;
+      hist[static_cast<int>((k - klo) >> sh) * 32 + lane] += 1u;
+    }
+  }
+  __device__ __forceinline__ bool skip(int) const { return false; }
+  __device__ __forceinline__ void visited(int) {}
+  __device__ __forceinline__ void refresh() {}
+};
+
+// Collect pass: keys below klo go to the accumulator, keys in [klo, khi] to
+// the boundary buffer.
+template <class Acc>
+struct KSet {
+  float qx, qy, qz;
+  bool qv;
+  int lane, nb;
+  unsigned long long klo, khi;
+  float tau;
+  unsigned long long* bbuf;
+  Acc* acc;
+  WarpScratch* ws;
+  float R;
+
+  __device__ __forceinline__ float metric(const float4& lo, const float4& hi) const {
+    return subtile_metric(lo, hi, *ws);
+  }
+  __device__ __forceinline__ bool still(float m) const { return m <= R; }
+  __device__ __forceinline__ bool need(const float4& lo, const float4& hi) const {
+    return qv && box_dist2(lo, hi, qx, qy, qz) <= tau;
+  }
+  __device__ __forceinline__ void scan(const float4* st) {
+    for (int j = 0; j < 32; ++j) {
+      const float4 p = st[j];
+      const float d = exact_dist2(qx, qy, qz, p.x, p.y, p.z);
+      if (!(d <= tau)) continue;
+      const unsigned long long k = make_key(d, __float_as_uint(p.w));
+      if (k < klo) {
+        acc->add(p, d);
+      } else if (k <= khi) {
+        if (nb < kBoundCap) bbuf[nb * 32 + lane] = k;
+        ++nb;
+      }
+    }
+  }
+  __device__ __forceinline__ bool skip(int) const { return false; }
+  __device__ __forceinline__ void visited(int) {}
+  __device__ __forceinline__ void refresh() {}
+};
+
+// Feeds the k nearest points of each valid lane (exact set under the
+// (distance, index) order; all points if the cloud holds fewer than k) to acc:
+// acc.add(point, d) for points met in the collect pass, acc.add_key(key) for
+// the selected boundary keys.  Queries are the points of leaf self_leaf of ix.
+template <class Acc>
+__device__ __forceinline__ void tile_kset(const IndexView& ix, float qx, float qy, float qz, bool qv, int K,
+                                          const float4& tlo, const float4& thi, KnnWarp& kw, unsigned char* region,
+                                          int self_leaf, Acc& acc) {
+  const int lane = threadIdx.x & 31;
+  KHist h;
+  knn_pass1(ix, qx, qy, qz, qv, K, LCR_INF, tlo, thi, kw, region, self_leaf, h);
+  // boundary range: the bin holding the k-th key (everything if fewer than k)
+  unsigned long long klo = make_key(LCR_INF, 0xffffffffu), khi = klo;  // fewer than k: every key is below klo
+  int m = 0, cnt = 0;
+  if (qv && h.cl >= K) {
+    const int b = h.bs - 1;
+    cnt = static_cast<int>(h.hist[b * 32 + lane]);
+    m = K - (h.cl - cnt);
+    klo = b == 0 ? 0ull : make_key(h.edge(b - 1), 0xffffffffu) + 1ull;
+    khi = make_key(h.edge(b), 0xffffffffu);
+  }
+  __syncwarp();
+  uint32_t* hist = reinterpret_cast<uint32_t*>(region);
+  while (__any_sync(LCR_FULL, cnt > kBoundCap)) {
+    KRefine r;
+    r.qx = qx; r.qy = qy; r.qz = qz; r.qv = qv;
+    r.active = cnt > kBoundCap;
+    r.lane = lane;
+    const unsigned long long span = khi - klo;  // >= cnt - 1 >= 32: keys are unique
+    r.sh = r.active ? max(0, 64 - __clzll(static_cast<long long>(span)) - 6) : 0;
+    r.klo = klo; r.khi = khi;
+    r.tau = r.active ? range_tau(khi) : -1.f;
+    r.hist = hist;
+    r.ws = &kw.ws;
+    r.R = subtile_radius(r.tau, r.active, kw.ws);
+    for (int b = 0; b < kBins; ++b) hist[b * 32 + lane] = 0u;
+    __syncwarp();
+    knn_pass2(ix, h, r, tlo, thi, kw);
+    if (r.active) {
+      int c = 0;
+      for (int j = 0; j < kBins; ++j) {
+        const int hj = static_cast<int>(hist[j * 32 + lane]);
+        if (c + hj >= m) {
+          const unsigned long long lo = klo + (static_cast<unsigned long long>(j) << r.sh);
+          const unsigned long long top = lo + ((1ull << r.sh) - 1ull);
+          klo = lo;
+          if (top < khi && top >= lo) khi = top;
+          m -= c;
+          cnt = hj;
+          break;
+        }
+        c += hj;
+      }
+    }
+    __syncwarp();
+  }
+  KSet<Acc> s;
+  s.qx = qx; s.qy = qy; s.qz = qz; s.qv = qv;
+  s.lane = lane; s.nb = 0;
+  s.klo = klo; s.khi = khi;
+  s.tau = qv ? range_tau(khi) : -1.f;
+  s.bbuf = reinterpret_cast<unsigned long long*>(region);
+  s.acc = &acc;
+  s.ws = &kw.ws;
+  s.R = subtile_radius(s.tau, qv, kw.ws);
+  knn_pass2(ix, h, s, tlo, thi, kw);
+  if (qv && m > 0) {
+    // partial selection sort: the m smallest of the nb (<= kBoundCap) boundary keys
+    unsigned long long* b = s.bbuf;
+    const int nb = min(s.nb, kBoundCap);
+    for (int i = 0; i < m && i < nb; ++i) {
+      int arg = i;
+      unsigned long long best = b[i * 32 + lane];
+      for (int j = i + 1; j < nb; ++j) {
+        const unsigned long long k = b[j * 32 + lane];
+        if (k < best) {
+          best = k;
+          arg = j;
+        }
+      }
+      b[arg * 32 + lane] = b[i * 32 + lane];
+      b[i * 32 + lane] = best;
+      acc.add_key(best);
+    }
   }
   __syncwarp();
 }

@@ -725,6 +725,14 @@ int orc_normals(const orc_point* in, size_t n, int k, const float* vp, int flip_
         for (int b = 0; b < 3; ++b) C[3 * a + b] += d[a] * d[b];
     }
     for (int a = 0; a < 9; ++a) C[a] /= cnt;
+    bool zero = true;
+    for (int a = 0; a < 9; ++a) zero = zero && C[a] == 0.0;
+    if (zero) {  // all neighbours coincide: NaN normal, curvature 0 (as PCL's eigen33 + solvePlaneParameters)
+      o.normal_x = o.normal_y = o.normal_z = nan;
+      o.curvature = 0.f;
+      out[i] = o;
+      continue;
+    }
     double w[3], V[9];
     eig3_jacobi(C, w, V);
     double nx = V[0], ny = V[3], nz = V[6];

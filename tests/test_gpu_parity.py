@@ -192,6 +192,60 @@ def test_sor_bit_exact(ctx, cfg0, k, mul):
     _cmp_points(outl.download(), pts[~okeep])
 
 
+def _stacked_duplicates(seed: int) -> np.ndarray:
+    """A cloud where 80 copies of 3 points make the k-th neighbour of their
+    neighbourhoods fall among dozens of equal distances (the boundary of the
+    unordered k-NN form is then split on the index part of the key)."""
+    pts = random_cloud(3000, seed, scale=0.05)
+    return np.concatenate([pts] + [pts[[7, 1500, 2999]]] * 80)
+
+
+def _dynamic_range_cloud(seed: int) -> np.ndarray:
+    """Neighbour distances 1e-10 beside ~1e-2: the double sum of the SOR mean
+    can round, so only the ascending order gives the reference's value (those
+    tiles take the sorted form)."""
+    pts = random_cloud(2000, seed, scale=0.05)
+    near = pts[:40].copy()
+    near["x"] = np.float32(0.0)
+    near["y"] = np.float32(0.0)
+    near["z"] = (np.arange(40) * 1e-10).astype(np.float32)
+    return np.concatenate([pts, near])
+
+
+@pytest.mark.parametrize("make", [_stacked_duplicates, _dynamic_range_cloud])
+def test_sor_ties_and_dynamic_range_bit_exact(ctx, make):
+    pts = make(3)
+    gd, _ = ctx.sor_distances(ctx.upload(pts), 50)
+    od, _, _ = O.sor(pts, 50, 1.0)
+    np.testing.assert_array_equal(gd.view(np.uint32), od.view(np.uint32))
+
+
+def _eigengap(pts, k):
+    """(l1 - l0) / trace of each point's k-neighbourhood covariance (FP64)."""
+    idx, _ = O.knn(pts, pts, k)
+    x = xyz_of(pts).astype(np.float64)[idx]
+    d = x - x.mean(1, keepdims=True)
+    w = np.linalg.eigvalsh(np.einsum("nki,nkj->nij", d, d) / k)
+    tr = w.sum(1)
+    return np.where(tr > 0, (w[:, 1] - w[:, 0]) / np.where(tr > 0, tr, 1), 0.0)
+
+
+def test_normals_coincident_points(ctx):
+    pts = _stacked_duplicates(4)
+    g = ctx.normals(ctx.upload(pts), 30).download()
+    o = O.normals(pts, 30)
+    ng, no = normals_of(g).astype(np.float64), normals_of(o).astype(np.float64)
+    # coincident neighbourhoods: NaN normal, curvature 0 on both sides
+    zero = ~np.isfinite(no[:, 0])
+    assert zero.sum() >= 240
+    assert np.all(~np.isfinite(ng[zero, 0])) and np.all(g["curvature"][zero] == 0)
+    # elsewhere the normal is defined where the smallest eigenvalue is simple
+    ok = ~zero & (o["curvature"] < 0.2) & (_eigengap(pts, 30) > 1e-3)
+    ang = np.arccos(np.clip(np.abs(np.sum(ng * no, axis=1)[ok]), -1, 1))
+    assert np.percentile(ang, 99.9) < 1e-3
+    np.testing.assert_allclose(g["curvature"][ok], o["curvature"][ok], atol=1e-4)
+
+
 def test_sor_far_point_removed(ctx):
     pts = random_cloud(2000, 31, scale=0.1)
     pts["x"][1234] = 10.0

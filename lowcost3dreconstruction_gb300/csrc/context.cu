@@ -135,17 +135,29 @@ __global__ void k_centroid_partial(const float4* __restrict__ xyz, size_t n, Sum
   }
 }
 
-__global__ void k_centroid_final(const Sum4* __restrict__ part, int nb, double* __restrict__ out) {
-  if (threadIdx.x != 0) return;
-  Sum4 s = Sum4{0, 0, 0, 0};
-  for (int j = 0; j < nb; ++j) {
-    s.x += part[j].x; s.y += part[j].y; s.z += part[j].z; s.w += part[j].w;
+// Sum of the block partials, one warp: lane l adds partials l, l+32, ... in
+// order, then a fixed shuffle tree.  out4 = (mean xyz, count) in FP64; outf
+// (may be null) receives the mean as float.
+__global__ void k_centroid_final(const Sum4* __restrict__ part, int nb, double* __restrict__ out,
+                                 float* __restrict__ outf) {
+  const int lane = threadIdx.x;
+  double x = 0, y = 0, z = 0, w = 0;
+  for (int j = lane; j < nb; j += 32) {
+    const Sum4 p = part[j];
+    x += p.x; y += p.y; z += p.z; w += p.w;
   }
-  const double c = s.w > 0 ? s.w : 1.0;
-  out[0] = s.x / c;
-  out[1] = s.y / c;
-  out[2] = s.z / c;
-  out[3] = s.w;
+  x = warp_sum(x); y = warp_sum(y); z = warp_sum(z); w = warp_sum(w);
+  if (lane != 0) return;
+  const double c = w > 0 ? w : 1.0;
+  out[0] = x / c;
+  out[1] = y / c;
+  out[2] = z / c;
+  out[3] = w;
+  if (outf) {
+    outf[0] = static_cast<float>(out[0]);
+    outf[1] = static_cast<float>(out[1]);
+    outf[2] = static_cast<float>(out[2]);
+  }
 }
 
 }  // namespace
@@ -209,15 +221,20 @@ lcr_cloud* transform_run(lcr_ctx* ctx, const lcr_cloud* in, const float* m) {
   return c;
 }
 
-void centroid_run(lcr_ctx* ctx, const lcr_cloud* in, double* c4) {
+void centroid_device(lcr_ctx* ctx, const lcr_cloud* in, double* out4, float* outf) {
   const int nb = std::max(1, std::min(ctx->sms * 2, static_cast<int>((in->n + 255) / 256)));
-  Sum4* part = static_cast<Sum4*>(dev_alloc(ctx, nb * sizeof(Sum4) + 4 * sizeof(double)));
-  double* out = reinterpret_cast<double*>(part + nb);
+  Sum4* part = static_cast<Sum4*>(dev_alloc(ctx, nb * sizeof(Sum4)));
   LCR_LAUNCH(ctx, k_centroid_partial, nb, 256, 0, in->xyz, in->n, part);
-  LCR_LAUNCH(ctx, k_centroid_final, 1, 32, 0, part, nb, out);
+  LCR_LAUNCH(ctx, k_centroid_final, 1, 32, 0, part, nb, out4, outf);
+  dev_free(ctx, part);
+}
+
+void centroid_run(lcr_ctx* ctx, const lcr_cloud* in, double* c4) {
+  double* out = static_cast<double*>(dev_alloc(ctx, 4 * sizeof(double)));
+  centroid_device(ctx, in, out, nullptr);
   double* h = static_cast<double*>(pinned(ctx, 4 * sizeof(double)));
   CUDA_TRY(cudaMemcpyAsync(h, out, 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  dev_free(ctx, part);
+  dev_free(ctx, out);
   sync(ctx);
   for (int i = 0; i < 4; ++i) c4[i] = h[i];
 }

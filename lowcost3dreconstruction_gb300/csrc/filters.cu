@@ -24,8 +24,10 @@ struct SorAcc {
   double sum;
   float dmin;
   int emin;  // smallest biased exponent (>= 1) of a nonzero term
+  int cnt;
   __device__ __forceinline__ void add_d(float d) {
     const float v = __fsqrt_rn(d);
+    ++cnt;
     sum = __dadd_rn(sum, static_cast<double>(v));
     dmin = fminf(dmin, d);
     if (v > 0.f) emin = min(emin, max(1, static_cast<int>(__float_as_uint(v) >> 23)));
@@ -50,8 +52,11 @@ __device__ __forceinline__ void sor_store(const float4& q, double s, int mean_k,
   atomicAdd(nvalid, 1u);
 }
 
+// too_few is set when a query has fewer than k+1 neighbours (the cloud holds
+// at most k finite points); the host reports it after the pass.
 __global__ void k_sor_dist(IndexView ix, int mean_k, float* __restrict__ dist, uint8_t* __restrict__ valid,
-                           unsigned int* __restrict__ nvalid, uint32_t* __restrict__ redo, unsigned int* nredo) {
+                           unsigned int* __restrict__ nvalid, uint32_t* __restrict__ redo, unsigned int* nredo,
+                           int* too_few) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int K = mean_k + 1;
@@ -66,8 +71,10 @@ __global__ void k_sor_dist(IndexView ix, int mean_k, float* __restrict__ dist, u
   acc.sum = 0.0;
   acc.dmin = LCR_INF;
   acc.emin = 255;
+  acc.cnt = 0;
   tile_kset(ix, q.x, q.y, q.z, qv, K, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), wbase + sizeof(KnnWarp), tile,
             acc);
+  if (qv && acc.cnt < K) *too_few = 1;
   double s = 0.0;
   if (!__all_sync(LCR_FULL, !qv || acc.result(s))) {
     if (lane == 0) redo[atomicAdd(nredo, 1u)] = static_cast<uint32_t>(tile);
@@ -387,11 +394,6 @@ RedoQueue redo_queue(lcr_ctx* ctx, int nleaf) {
   return q;
 }
 
-int finite_count(lcr_ctx* ctx, const lcr_cloud* in) {
-  double c4[4];
-  centroid_run(ctx, in, c4);
-  return static_cast<int>(c4[3] + 0.5);
-}
 
 }  // namespace
 
@@ -400,8 +402,6 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
   if (mean_k <= 0) LCR_THROW(LCR_ERR_INVALID_ARG, "mean_k must be positive");
   const int n = static_cast<int>(in->n);
   if (n == 0) LCR_THROW(LCR_ERR_EMPTY, "statistical outlier removal on an empty cloud");
-  if (mean_k + 1 > finite_count(ctx, in))
-    LCR_THROW(LCR_ERR_TOO_FEW_POINTS, "SOR needs more than %d finite points (k+1 neighbours)", mean_k);
   const IndexView ix = cloud_index(ctx, in).v;
   const int K = mean_k + 1;
   const int nw = K <= 64 ? 4 : 2;
@@ -414,16 +414,17 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
   const int nc0 = (n + 255) / 256;
   double* sums = static_cast<double*>(dev_alloc(ctx, sizeof(double) * (4 * static_cast<size_t>(nc0) + 8)));
   unsigned int* nvalid = reinterpret_cast<unsigned int*>(sums + 4 * nc0 + 4);
+  int* too_few = reinterpret_cast<int*>(nvalid + 1);
   double* st = sums + 4 * nc0;
   CUDA_TRY(cudaMemsetAsync(dist, 0, sizeof(float) * n, ctx->stream));
   CUDA_TRY(cudaMemsetAsync(valid, 0, n, ctx->stream));
-  CUDA_TRY(cudaMemsetAsync(nvalid, 0, sizeof(unsigned int), ctx->stream));
+  CUDA_TRY(cudaMemsetAsync(sums + 4 * nc0 + 4, 0, 2 * sizeof(double), ctx->stream));
   const RedoQueue rq = redo_queue(ctx, ix.nleaf);
   CUDA_TRY(cudaFuncSetAttribute(k_sor_dist, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_set)));
   CUDA_TRY(cudaFuncSetAttribute(k_sor_dist_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 static_cast<int>(smem)));
   LCR_LAUNCH(ctx, k_sor_dist, (ix.nleaf + kSetWarps - 1) / kSetWarps, kSetWarps * 32, smem_set, ix, mean_k, dist,
-             valid, nvalid, rq.tiles(), rq.count());
+             valid, nvalid, rq.tiles(), rq.count(), too_few);
   LCR_LAUNCH(ctx, k_sor_dist_sorted, ctx->sms, nw * 32, smem, ix, mean_k, dist, valid, nvalid, rq.tiles(), rq.count());
   dev_free(ctx, rq.block);
   // blocked sums (ping-pong between two halves of `sums`)
@@ -440,10 +441,22 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
   LCR_LAUNCH(ctx, k_sor_threshold, 1, 32, 0, a, b, nvalid, std_mul, st);
   LCR_LAUNCH(ctx, k_sor_flags, (n + 255) / 256, 256, 0, dist, n, st, keep, drop);
   uint32_t* idx = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * n));
-  const int nkeep = compact_flags(ctx, keep, n, idx);
+  // nvalid and too_few are adjacent: one copy
+  unsigned int* h_chk = reinterpret_cast<unsigned int*>(static_cast<char*>(pinned(ctx, 64)) + 48);
+  CUDA_TRY(cudaMemcpyAsync(h_chk, nvalid, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
+  const int nkeep = compact_flags(ctx, keep, n, idx);  // synchronises
+  if (h_chk[0] == 0 || h_chk[1] != 0) {
+    dev_free(ctx, dist);
+    dev_free(ctx, flags);
+    dev_free(ctx, sums);
+    dev_free(ctx, idx);
+    LCR_THROW(LCR_ERR_TOO_FEW_POINTS, "SOR needs more than %d finite points (k+1 neighbours)", mean_k);
+  }
   if (inliers) {
     *inliers = cloud_alloc(ctx, nkeep);
     gather_cloud(ctx, in, idx, nkeep, *inliers);
+    // the inliers keep the input's sorted order: their index is a compaction
+    if (nkeep > 0) (*inliers)->index = subset_index(ctx, *in->index, keep, idx, nkeep);
   }
   if (outliers) {
     const int ndrop = compact_flags(ctx, drop, n, idx);
@@ -484,6 +497,7 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
   CUDA_TRY(cudaFuncSetAttribute(k_normals, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_set)));
   LCR_LAUNCH(ctx, k_normals, (ix.nleaf + kSetWarps - 1) / kSetWarps, kSetWarps * 32, smem_set, ix, k, in->xyz, vp[0],
              vp[1], vp[2], flip, out->nrm);
+  out->index = share_index(in->index);  // same points in the same order
   return out;
 }
 

@@ -784,8 +784,6 @@ void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr
   const int p2pl = p->method == LCR_ICP_POINT_TO_PLANE ? 1 : 0;
   const Index& si = cloud_index(ctx, src);
   const Index& ti = cloud_index(ctx, tgt);
-  double c4[4];
-  centroid_run(ctx, tgt, c4);
   const int grid = icp_grid(ctx);
   IcpBuffers B = icp_buffers(ctx, grid);
 
@@ -799,7 +797,6 @@ void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr
   hp->src_ntiles = si.v.nleaf;
   hp->tgt_nrm = tgt->nrm;
   hp->cap = float_cap(p->max_correspondence_distance * p->max_correspondence_distance);
-  for (int a = 0; a < 3; ++a) hp->c[a] = static_cast<float>(c4[a]);
   hp->min_corr = 3;
   hp->max_iter = p->max_iterations;
   hp->teps = p->transformation_epsilon;
@@ -823,6 +820,10 @@ void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr
   for (int i = 0; i < 12; ++i) hs->Tf.m[i] = static_cast<float>(hs->T[i]);
   hs->prev_mse = DBL_MAX;
   CUDA_TRY(cudaMemcpyAsync(B.prm, stage, 2048, cudaMemcpyHostToDevice, ctx->stream));
+  // centre of the linear algebra: the target centroid (FP64 sums, cast to float)
+  double* c4 = static_cast<double*>(dev_alloc(ctx, 4 * sizeof(double)));
+  centroid_device(ctx, tgt, c4, &B.prm->c[0]);
+  dev_free(ctx, c4);
 
   if (exec) {
     CUDA_TRY(cudaGraphLaunch(exec, ctx->stream));

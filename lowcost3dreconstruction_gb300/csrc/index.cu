@@ -119,32 +119,69 @@ __global__ void k_level_boxes(const float4* __restrict__ clo, const float4* __re
   }
 }
 
+// Subset index: position of every kept input point among the kept points.
+__global__ void k_rank_of_kept(const uint32_t* __restrict__ kept, int nkeep, uint32_t* __restrict__ rank) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nkeep) rank[kept[j]] = static_cast<uint32_t>(j);
+}
+
+// flags over the sorted slots of the source index: slot holds a kept point
+__global__ void k_slot_kept(const float4* __restrict__ pts, int npad, const uint8_t* __restrict__ keep,
+                            uint8_t* __restrict__ flags) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= npad) return;
+  const uint32_t w = __float_as_uint(pts[s].w);
+  flags[s] = (w != 0xffffffffu && keep[w]) ? 1 : 0;
+}
+
+__global__ void k_gather_subset(const float4* __restrict__ src, const uint32_t* __restrict__ slots, int nkeep,
+                                const uint32_t* __restrict__ rank, int npad, float4* __restrict__ pts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npad) return;
+  float4 o;
+  if (i < nkeep) {
+    const float4 p = src[slots[i]];
+    o = make_float4(p.x, p.y, p.z, __uint_as_float(rank[__float_as_uint(p.w)]));
+  } else {
+    const float nan = __int_as_float(0x7fc00000);
+    o = make_float4(nan, nan, nan, __uint_as_float(0xffffffffu));
+  }
+  pts[i] = o;
+}
+
 inline size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
 }  // namespace
 
-Index* build_index(lcr_ctx* ctx, const float4* xyz, int n) {
+namespace {
+
+// Allocates an index for n points (one block: sorted points, then lo/hi boxes
+// of every level).
+Index* index_alloc(lcr_ctx* ctx, int n) {
   if (n <= 0) LCR_THROW(LCR_ERR_EMPTY, "cannot index an empty cloud");
-  Index* ix = new Index();
-  IndexView& v = ix->v;
-  v.n = n;
-  v.nleaf = (n + 31) / 32;
   int counts[kMaxLevels + 1];
   int levels = 0;
-  counts[0] = v.nleaf;
+  counts[0] = (n + 31) / 32;
   while (counts[levels] > 1) {
-    if (levels + 1 >= kMaxLevels) {
-      delete ix;
-      LCR_THROW(LCR_ERR_INVALID_ARG, "cloud too large for the index (%d points)", n);
-    }
+    if (levels + 1 >= kMaxLevels) LCR_THROW(LCR_ERR_INVALID_ARG, "cloud too large for the index (%d points)", n);
     counts[levels + 1] = (counts[levels] + 31) / 32;
     ++levels;
   }
+  Index* ix = new Index();
+  IndexView& v = ix->v;
+  v.n = n;
+  v.nleaf = counts[0];
   v.top = levels;
   const size_t npad = static_cast<size_t>(v.nleaf) * 32;
   size_t bytes = align256(npad * sizeof(float4));
   for (int l = 0; l <= levels; ++l) bytes += 2 * align256(static_cast<size_t>(counts[l]) * sizeof(float4));
-  char* blk = static_cast<char*>(dev_alloc(ctx, bytes));
+  char* blk = nullptr;
+  try {
+    blk = static_cast<char*>(dev_alloc(ctx, bytes));
+  } catch (...) {
+    delete ix;
+    throw;
+  }
   ix->block = blk;
   ix->bytes = bytes;
   size_t off = 0;
@@ -161,29 +198,72 @@ Index* build_index(lcr_ctx* ctx, const float4* xyz, int n) {
     v.hi[l] = reinterpret_cast<float4*>(blk + off);
     off += align256(static_cast<size_t>(counts[l]) * sizeof(float4));
   }
+  return ix;
+}
 
-  uint32_t* keys = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * static_cast<size_t>(n)));
-  uint32_t* vals = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * static_cast<size_t>(n)));
-  float4* box = static_cast<float4*>(dev_alloc(ctx, 2 * sizeof(float4)));
+// Leaf boxes and the box levels above them, from the sorted points.
+void index_boxes(lcr_ctx* ctx, Index* ix) {
+  IndexView& v = ix->v;
+  LCR_LAUNCH(ctx, k_leaf_boxes, (v.nleaf * 32 + 255) / 256, 256, 0, v.pts, v.nleaf, const_cast<float4*>(v.lo[0]),
+             const_cast<float4*>(v.hi[0]));
+  for (int l = 1; l <= v.top; ++l) {
+    LCR_LAUNCH(ctx, k_level_boxes, (v.count[l] * 32 + 255) / 256, 256, 0, v.lo[l - 1], v.hi[l - 1], v.count[l - 1],
+               v.count[l], const_cast<float4*>(v.lo[l]), const_cast<float4*>(v.hi[l]));
+  }
+}
+
+}  // namespace
+
+Index* build_index(lcr_ctx* ctx, const float4* xyz, int n) {
+  Index* ix = index_alloc(ctx, n);
+  IndexView& v = ix->v;
+  const size_t npad = static_cast<size_t>(v.nleaf) * 32;
+  const size_t kv_bytes = align256(sizeof(uint32_t) * 2 * static_cast<size_t>(n));
+  char* scratch = static_cast<char*>(dev_alloc(ctx, kv_bytes + 2 * sizeof(float4)));
+  uint32_t* keys = reinterpret_cast<uint32_t*>(scratch);
+  uint32_t* vals = keys + n;
+  float4* box = reinterpret_cast<float4*>(scratch + kv_bytes);
   bbox(ctx, xyz, n, box);
   LCR_LAUNCH(ctx, k_curve_keys, (n + 255) / 256, 256, 0, xyz, n, box, keys, vals);
   radix_sort_pairs(ctx, keys, vals, n, 32);
   LCR_LAUNCH(ctx, k_gather_sorted, static_cast<int>((npad + 255) / 256), 256, 0, xyz, keys, vals, n,
              static_cast<int>(npad), const_cast<float4*>(v.pts));
-  LCR_LAUNCH(ctx, k_leaf_boxes, (v.nleaf * 32 + 255) / 256, 256, 0, v.pts, v.nleaf, const_cast<float4*>(v.lo[0]),
-             const_cast<float4*>(v.hi[0]));
-  for (int l = 1; l <= levels; ++l) {
-    LCR_LAUNCH(ctx, k_level_boxes, (counts[l] * 32 + 255) / 256, 256, 0, v.lo[l - 1], v.hi[l - 1], counts[l - 1],
-               counts[l], const_cast<float4*>(v.lo[l]), const_cast<float4*>(v.hi[l]));
-  }
-  dev_free(ctx, keys);
-  dev_free(ctx, vals);
-  dev_free(ctx, box);
+  index_boxes(ctx, ix);
+  dev_free(ctx, scratch);
+  return ix;
+}
+
+// Index of the points of a cloud kept by keep[] (input order; `kept` lists
+// them, nkeep of them), numbered by their position among the kept points --
+// the numbering of the compacted cloud.  No new sort: the source's sorted
+// order restricted to the kept points keeps its spatial coherence.
+Index* subset_index(lcr_ctx* ctx, const Index& src, const uint8_t* keep, const uint32_t* kept, int nkeep) {
+  Index* ix = index_alloc(ctx, nkeep);
+  IndexView& v = ix->v;
+  const int npad_src = src.v.nleaf * 32;
+  const int npad = v.nleaf * 32;
+  char* tmp = static_cast<char*>(dev_alloc(ctx, sizeof(uint32_t) * (static_cast<size_t>(src.v.n) + npad_src) +
+                                                   static_cast<size_t>(npad_src) + 256));
+  uint32_t* rank = reinterpret_cast<uint32_t*>(tmp);
+  uint32_t* slots = rank + src.v.n;
+  uint8_t* flags = reinterpret_cast<uint8_t*>(slots + npad_src);
+  LCR_LAUNCH(ctx, k_rank_of_kept, (nkeep + 255) / 256, 256, 0, kept, nkeep, rank);
+  LCR_LAUNCH(ctx, k_slot_kept, (npad_src + 255) / 256, 256, 0, src.v.pts, npad_src, keep, flags);
+  compact_flags_async(ctx, flags, npad_src, slots);
+  LCR_LAUNCH(ctx, k_gather_subset, (npad + 255) / 256, 256, 0, src.v.pts, slots, nkeep, rank, npad,
+             const_cast<float4*>(v.pts));
+  index_boxes(ctx, ix);
+  dev_free(ctx, tmp);
+  return ix;
+}
+
+Index* share_index(Index* ix) {
+  if (ix) ++ix->refs;
   return ix;
 }
 
 void free_index(lcr_ctx* ctx, Index* ix) {
-  if (!ix) return;
+  if (!ix || --ix->refs > 0) return;
   dev_free(ctx, ix->block);
   delete ix;
 }

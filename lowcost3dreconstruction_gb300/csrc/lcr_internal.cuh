@@ -62,6 +62,7 @@ struct Index {
   IndexView v;
   void* block = nullptr;        // one allocation holding everything
   size_t bytes = 0;
+  int refs = 1;                 // clouds with identical points in the same order share one index
 };
 
 // ------------------------------------------------------------------ cloud
@@ -183,6 +184,7 @@ void radix_sort_pairs(lcr_ctx* ctx, uint32_t* keys, uint32_t* vals, int n, int b
 // Order-preserving compaction: indices of flags[i] != 0 written to out_idx in
 // ascending order.  Returns the count (synchronises).
 int compact_flags(lcr_ctx* ctx, const uint8_t* flags, int n, uint32_t* out_idx);
+void compact_flags_async(lcr_ctx* ctx, const uint8_t* flags, int n, uint32_t* out_idx, uint32_t* count_dev = nullptr);
 // Gathers cloud rows: out[j] = in[idx[j]].
 void gather_cloud(lcr_ctx* ctx, const lcr_cloud* in, const uint32_t* idx, int n, lcr_cloud* out);
 // Device-side bounding box of the finite points of an xyz array: out[0] = lo, out[1] = hi.
@@ -190,6 +192,8 @@ void bbox(lcr_ctx* ctx, const float4* xyz, int n, float4* out2);
 
 // ------------------------------------------------------------ index build
 Index* build_index(lcr_ctx* ctx, const float4* xyz, int n);
+Index* subset_index(lcr_ctx* ctx, const Index& src, const uint8_t* keep, const uint32_t* kept, int nkeep);
+Index* share_index(Index* ix);
 void free_index(lcr_ctx* ctx, Index* ix);
 
 // ----------------------------------------------------- algorithm entry points
@@ -209,6 +213,9 @@ void crop_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, double r
 lcr_cloud* transform_run(lcr_ctx* ctx, const lcr_cloud* in, const float* m);
 // c4 = {x, y, z, finite count}, FP64 accumulation (synchronises).
 void centroid_run(lcr_ctx* ctx, const lcr_cloud* in, double* c4);
+// Same on the device, no synchronisation: out4 (device, 4 doubles) and, if
+// outf is not null, the mean as 3 floats (device).
+void centroid_device(lcr_ctx* ctx, const lcr_cloud* in, double* out4, float* outf);
 lcr_cloud* upload_records(lcr_ctx* ctx, const void* recs, size_t n, bool device_src);
 lcr_cloud* upload_xyz(lcr_ctx* ctx, const float* xyz, size_t n);
 void download_records(lcr_ctx* ctx, const lcr_cloud* c, void* out);

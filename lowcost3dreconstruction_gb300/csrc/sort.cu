@@ -17,9 +17,8 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   return m;
 }
 
-// Per-block digit histogram, written digit-major: hist[d * nblk + b].
-__global__ void k_radix_hist(const uint32_t* __restrict__ keys, int n, int shift, uint32_t* __restrict__ hist,
-                             int nblk) {
+// Per-block digit histogram, written block-major: hist[b * 256 + d].
+__global__ void k_radix_hist(const uint32_t* __restrict__ keys, int n, int shift, uint32_t* __restrict__ hist) {
   __shared__ uint32_t h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -30,11 +29,12 @@ __global__ void k_radix_hist(const uint32_t* __restrict__ keys, int n, int shift
     if (i < static_cast<size_t>(n)) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
   }
   __syncthreads();
-  hist[static_cast<size_t>(threadIdx.x) * nblk + blockIdx.x] = h[threadIdx.x];
+  hist[static_cast<size_t>(blockIdx.x) * 256 + threadIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of m counters by a single block of 1024 threads (each thread
-// owns a contiguous chunk).  total (may be null) receives the sum.
+// Exclusive scan of m counters (block counts of a compaction: m is small) by a
+// single block of 1024 threads, each owning a contiguous chunk.  total (may be
+// null) receives the sum.
 __global__ void k_scan_exclusive(uint32_t* __restrict__ a, int m, uint32_t* __restrict__ total) {
   __shared__ uint32_t warp_sums[32];
   const int t = threadIdx.x;
@@ -72,17 +72,63 @@ __global__ void k_scan_exclusive(uint32_t* __restrict__ a, int m, uint32_t* __re
   }
 }
 
-// Stable scatter.  Elements are ranked round by round (256 at a time, in input
-// order): within a warp by __match_any_sync peers below the lane, across warps
-// by a per-digit prefix over warp counts, across rounds by a running per-digit
-// base, across blocks by the scanned histogram.
+// Per-digit exclusive scan over the blocks, one block per digit (column d of
+// the block-major histogram), in place; totals[d] = number of keys with digit d.
+__global__ void k_radix_offsets(uint32_t* __restrict__ hist, int nblk, uint32_t* __restrict__ totals) {
+  __shared__ uint32_t s_wsum[kSortThreads / 32];
+  const int d = blockIdx.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+  uint32_t carry = 0;
+  for (int j0 = 0; j0 < nblk; j0 += kSortThreads) {
+    const int j = j0 + t;
+    const uint32_t v = j < nblk ? hist[static_cast<size_t>(j) * 256 + d] : 0u;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(LCR_FULL, incl, o);
+      if (lane >= o) incl += u;
+    }
+    if (lane == 31) s_wsum[w] = incl;
+    __syncthreads();
+    uint32_t wbase = 0, all = 0;
+#pragma unroll
+    for (int k = 0; k < kSortThreads / 32; ++k) {
+      wbase += k < w ? s_wsum[k] : 0u;
+      all += s_wsum[k];
+    }
+    if (j < nblk) hist[static_cast<size_t>(j) * 256 + d] = carry + wbase + incl - v;
+    carry += all;
+    __syncthreads();
+  }
+  if (t == 0) totals[d] = carry;
+}
+
+// Stable scatter.  Each block's output base for digit d is the exclusive sum of
+// the digit totals below d plus its own per-digit prefix.  Elements are ranked
+// round by round (256 at a time, in input order): within a warp by
+// __match_any_sync peers below the lane, across warps by a per-digit prefix
+// over warp counts, across rounds by a running per-digit base.
 __global__ void k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                 uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int n, int shift,
-                                const uint32_t* __restrict__ hist, int nblk) {
+                                const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals) {
   __shared__ uint32_t s_off[256];
   __shared__ uint32_t s_w[kSortThreads / 32][256];
+  __shared__ uint32_t s_wsum[kSortThreads / 32];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  s_off[t] = hist[static_cast<size_t>(t) * nblk + blockIdx.x];
+  {
+    const uint32_t total = totals[t];
+    uint32_t incl = total;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_up_sync(LCR_FULL, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) s_wsum[w] = incl;
+    __syncthreads();
+    uint32_t wbase = 0;
+#pragma unroll
+    for (int k = 0; k < kSortThreads / 32; ++k) wbase += k < w ? s_wsum[k] : 0u;
+    s_off[t] = wbase + incl - total + hist[static_cast<size_t>(blockIdx.x) * 256 + t];
+  }
 #pragma unroll
   for (int j = 0; j < kSortThreads / 32; ++j) s_w[j][t] = 0;
   __syncthreads();
@@ -229,14 +275,15 @@ void radix_sort_pairs(lcr_ctx* ctx, uint32_t* keys, uint32_t* vals, int n, int b
   const int nblk = (n + kSortTile - 1) / kSortTile;
   uint32_t* tk = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * static_cast<size_t>(n)));
   uint32_t* tv = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * static_cast<size_t>(n)));
-  uint32_t* hist = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * 256 * static_cast<size_t>(nblk)));
+  uint32_t* hist = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * 256 * (static_cast<size_t>(nblk) + 1)));
+  uint32_t* totals = hist + 256 * static_cast<size_t>(nblk);
   uint32_t *ki = keys, *vi = vals, *ko = tk, *vo = tv;
   const int passes = (std::max(bits, 1) + 7) / 8;
   for (int p = 0; p < passes; ++p) {
     const int shift = 8 * p;
-    LCR_LAUNCH(ctx, k_radix_hist, nblk, kSortThreads, 0, ki, n, shift, hist, nblk);
-    LCR_LAUNCH(ctx, k_scan_exclusive, 1, 1024, 0, hist, 256 * nblk, static_cast<uint32_t*>(nullptr));
-    LCR_LAUNCH(ctx, k_radix_scatter, nblk, kSortThreads, 0, ki, vi, ko, vo, n, shift, hist, nblk);
+    LCR_LAUNCH(ctx, k_radix_hist, nblk, kSortThreads, 0, ki, n, shift, hist);
+    LCR_LAUNCH(ctx, k_radix_offsets, 256, kSortThreads, 0, hist, nblk, totals);
+    LCR_LAUNCH(ctx, k_radix_scatter, nblk, kSortThreads, 0, ki, vi, ko, vo, n, shift, hist, totals);
     std::swap(ki, ko);
     std::swap(vi, vo);
   }
@@ -249,16 +296,24 @@ void radix_sort_pairs(lcr_ctx* ctx, uint32_t* keys, uint32_t* vals, int n, int b
   dev_free(ctx, hist);
 }
 
-int compact_flags(lcr_ctx* ctx, const uint8_t* flags, int n, uint32_t* out_idx) {
-  if (n <= 0) return 0;
+// Writes the count to *count_dev (may be null); no host synchronisation.
+void compact_flags_async(lcr_ctx* ctx, const uint8_t* flags, int n, uint32_t* out_idx, uint32_t* count_dev) {
+  if (n <= 0) return;
   const int nblk = (n + kCompTile - 1) / kCompTile;
   uint32_t* cnt = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * (nblk + 1)));
   LCR_LAUNCH(ctx, k_flag_count, nblk, kCompThreads, 0, flags, n, cnt);
-  LCR_LAUNCH(ctx, k_scan_exclusive, 1, 1024, 0, cnt, nblk, cnt + nblk);
+  LCR_LAUNCH(ctx, k_scan_exclusive, 1, 1024, 0, cnt, nblk, count_dev ? count_dev : cnt + nblk);
   LCR_LAUNCH(ctx, k_flag_scatter, nblk, kCompThreads, 0, flags, n, cnt, out_idx);
-  uint32_t* h = static_cast<uint32_t*>(pinned(ctx, sizeof(uint32_t)));
-  CUDA_TRY(cudaMemcpyAsync(h, cnt + nblk, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
   dev_free(ctx, cnt);
+}
+
+int compact_flags(lcr_ctx* ctx, const uint8_t* flags, int n, uint32_t* out_idx) {
+  if (n <= 0) return 0;
+  uint32_t* d = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t)));
+  compact_flags_async(ctx, flags, n, out_idx, d);
+  uint32_t* h = static_cast<uint32_t*>(pinned(ctx, sizeof(uint32_t)));
+  CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  dev_free(ctx, d);
   sync(ctx);
   return static_cast<int>(*h);
 }

@@ -120,6 +120,7 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     h_frames = [torch.from_numpy(f.view(np.uint8).reshape(-1)).pin_memory() for f in frames]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
     stage_ms = {}
+    sor_n: list[int] = []  # SOR input sizes, one per k_sor_dist launch
 
     def capture(c, src_is_device: bool, k: int, timing: dict | None):
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)] if timing is not None else None
@@ -129,6 +130,7 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
                   else ctx.backproject(h_frames[k].numpy().view(np.uint16), params))
             if ev: ev[1].record()
             v = ctx.voxel_grid(cl, 0.001)
+            sor_n.append(len(v))
             if ev: ev[2].record()
             inl, _, _ = ctx.sor(v, 50, 1.0)
             if ev: ev[3].record()
@@ -185,7 +187,12 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     torch.cuda.synchronize()
     clocks = Clocks(dev)
     clocks.start()
+    sor_n.clear()
+    ctx.kernel_timing(True)
     aligned, dev_ms, launches, last_rmse, last_res = timed(True, stage_ms)
+    sor_ms, sor_launches = ctx.kernel_time(L.KT_SOR_KNN)
+    ctx.kernel_timing(False)
+    sor_sizes = list(sor_n)
     clk = clocks.stop()
     torch.cuda.synchronize()
     e2e_aligned, e2e_ms, _, _, _ = timed(False, None)
@@ -204,16 +211,21 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     steps_total = args.steps * world
     value = aligned / (dev_ms / 1000.0)
     e2e_value = e2e_aligned / (e2e_ms / 1000.0)
-    # Roofline of the dominant kernel: one ICP iteration (fused transform + exact
-    # 1-NN + correspondence terms + FP64 solve), time = ICP stage / iterations.
-    it = max(1, stage_ms.get("icp_iters", 1))
-    iter_ms = stage_ms["icp"] / it
-    nleaf = (ntgt + 31) // 32
-    bytes_per_iter = nsrc * 16 + ntgt * 16 + ntgt * 16 + nleaf * 32  # src xyz, tgt xyz, tgt normals, leaf boxes
+    # Roofline of the dominant kernel, k_sor_dist (the unordered k-NN pass of
+    # StatisticalOutlierRemoval, k = 51 including the point itself): its launches
+    # are bracketed by CUDA events on the library's stream during the timed
+    # region.  Algorithmic bytes per launch on n points in nleaf leaves of 32:
+    # query points 16 n + reference points 16 n + leaf boxes 32 nleaf + output
+    # (mean distance 4 B + valid flag 1 B) 5 n.
+    def sor_bytes(n: int) -> int:
+        return 37 * n + 32 * ((n + 31) // 32)
+    assert sor_launches == len(sor_sizes), (sor_launches, len(sor_sizes))
+    bytes_per_launch = sum(sor_bytes(n) for n in sor_sizes) / max(1, len(sor_sizes))
+    launch_ms = sor_ms / max(1, sor_launches)
     pk = peaks()
-    achieved = bytes_per_iter / (iter_ms * 1e-3) / 1e9
+    achieved = bytes_per_launch / (launch_ms * 1e-3) / 1e9
     ncu_traffic = None
-    tfile = ROOT / "profiles" / "icp_iteration_traffic.json"
+    tfile = ROOT / "profiles" / "k_sor_dist_config1_traffic.json"
     if tfile.exists():
         ncu_traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
     out = {
@@ -226,11 +238,11 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
                    "parallelism": f"replicas x{world}",
                    "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stage_ms.items() if k != "icp_iters"},
                    "icp_iterations_per_step": stage_ms.get("icp_iters", 0) / args.steps},
-        "roofline": {"kernel": "k_icp_iter (one fused ICP iteration)", "bound": "hbm",
+        "roofline": {"kernel": "k_sor_dist (SOR k-NN pass, k=51)", "bound": "hbm",
                      "achieved": round(achieved, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / pk["hbm_gbs"], 5), "peak_src": pk["src"],
-                     "algorithmic_bytes_per_launch": bytes_per_iter, "avg_launch_ms": round(iter_ms, 5),
-                     "traffic": ncu_traffic},
+                     "algorithmic_bytes_per_launch": int(bytes_per_launch), "avg_launch_ms": round(launch_ms, 5),
+                     "launches": int(sor_launches), "traffic": ncu_traffic},
         "e2e": {"value": round(e2e_value, 3), "unit": "pairs/s",
                 "h2d_bytes_per_step": int(sum(f.nbytes for f in frames)), "d2h_bytes_per_step": 4 * 16 + 8 * 16},
         "gpu_launches": int(launches),

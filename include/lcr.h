@@ -76,6 +76,15 @@ LCR_API void* lcr_ctx_stream(lcr_ctx* ctx);
  * kernel node executed per launch as reported by the graph's own counter). */
 LCR_API uint64_t lcr_ctx_launch_count(const lcr_ctx* ctx);
 
+/* Kernel timing (no counterpart in the reference: measurement support).  With
+ * timing enabled, the launches of the listed kernels are bracketed by CUDA
+ * events on the context's stream; lcr_kernel_time synchronises the stream and
+ * returns the summed device time and launch count since timing was enabled.
+ * lcr_kernel_timing(ctx, 1) also resets the sums. */
+enum { LCR_KT_SOR_KNN = 0, LCR_KT_NORMALS_KNN = 1, LCR_KT_COUNT = 2 };
+LCR_API lcr_status lcr_kernel_timing(lcr_ctx* ctx, int enable);
+LCR_API lcr_status lcr_kernel_time(lcr_ctx* ctx, int which, double* ms, uint64_t* launches);
+
 /* ----------------------------------------------------------------- clouds */
 /* Replaces pcl::io::loadPLYFile + the PointCloud<PointXYZRGBNormal> a tool
  * holds (e.g. pcl_tools/fine_registration.cpp:94-102). */

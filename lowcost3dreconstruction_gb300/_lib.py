@@ -58,6 +58,9 @@ class SorStats(C.Structure):
                 ("valid", C.c_size_t), ("kept", C.c_size_t), ("removed", C.c_size_t)]
 
 
+KT_SOR_KNN, KT_NORMALS_KNN = 0, 1
+
+
 class IcpParams(C.Structure):
     _fields_ = [("max_correspondence_distance", C.c_double), ("max_iterations", C.c_int),
                 ("transformation_epsilon", C.c_double), ("euclidean_fitness_epsilon", C.c_double),
@@ -79,6 +82,8 @@ _SIGS = {
     "lcr_ctx_synchronize": (C.c_int, [_VP]),
     "lcr_ctx_stream": (_VP, [_VP]),
     "lcr_ctx_launch_count": (C.c_uint64, [_VP]),
+    "lcr_kernel_timing": (C.c_int, [_VP, C.c_int]),
+    "lcr_kernel_time": (C.c_int, [_VP, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]),
     "lcr_cloud_upload": (C.c_int, [_VP, _VP, C.c_size_t, C.POINTER(_VP)]),
     "lcr_cloud_upload_xyz": (C.c_int, [_VP, _VP, C.c_size_t, C.POINTER(_VP)]),
     "lcr_cloud_from_device": (C.c_int, [_VP, _VP, C.c_size_t, C.POINTER(_VP)]),

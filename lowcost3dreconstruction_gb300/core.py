@@ -124,6 +124,16 @@ class Context:
     def launches(self) -> int:
         return int(self.lib.lcr_ctx_launch_count(self.h))
 
+    def kernel_timing(self, enable: bool) -> None:
+        """Start (and reset) or stop event timing of the k-NN filter kernels."""
+        self._check(self.lib.lcr_kernel_timing(self.h, 1 if enable else 0))
+
+    def kernel_time(self, which: int) -> tuple[float, int]:
+        """(summed device ms, launches) of a timed kernel since timing started."""
+        ms, n = C.c_double(), C.c_uint64()
+        self._check(self.lib.lcr_kernel_time(self.h, which, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
     def synchronize(self) -> None:
         self._check(self.lib.lcr_ctx_synchronize(self.h))
 

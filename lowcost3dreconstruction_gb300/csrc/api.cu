@@ -107,6 +107,12 @@ void lcr_ctx_destroy(lcr_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   for (int m = 0; m < 2; ++m)
     if (ctx->icp_exec[m]) cudaGraphExecDestroy(ctx->icp_exec[m]);
+  for (auto& t : ctx->kt)
+    for (auto& e : t.pending) {
+      cudaEventDestroy(e.first);
+      cudaEventDestroy(e.second);
+    }
+  for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
   if (ctx->icp_block) cudaFree(ctx->icp_block);
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   cudaStreamDestroy(ctx->stream);
@@ -126,6 +132,43 @@ lcr_status lcr_ctx_synchronize(lcr_ctx* ctx) {
 void* lcr_ctx_stream(lcr_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
 
 uint64_t lcr_ctx_launch_count(const lcr_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+lcr_status lcr_kernel_timing(lcr_ctx* ctx, int enable) {
+  API_BEGIN(ctx)
+  sync(ctx);
+  for (auto& t : ctx->kt) {
+    for (auto& e : t.pending) {
+      ctx->event_pool.push_back(e.first);
+      ctx->event_pool.push_back(e.second);
+    }
+    t.pending.clear();
+    t.ms = 0.0;
+    t.launches = 0;
+  }
+  ctx->timing = enable != 0;
+  return LCR_OK;
+  API_END(ctx)
+}
+
+lcr_status lcr_kernel_time(lcr_ctx* ctx, int which, double* ms, uint64_t* launches) {
+  API_BEGIN(ctx)
+  REQUIRE(which >= 0 && which < LCR_KT_COUNT, "unknown timed kernel %d", which);
+  sync(ctx);
+  auto& t = ctx->kt[which];
+  for (auto& e : t.pending) {
+    float v = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&v, e.first, e.second));
+    t.ms += v;
+    t.launches += 1;
+    ctx->event_pool.push_back(e.first);
+    ctx->event_pool.push_back(e.second);
+  }
+  t.pending.clear();
+  if (ms) *ms = t.ms;
+  if (launches) *launches = t.launches;
+  return LCR_OK;
+  API_END(ctx)
+}
 
 // ------------------------------------------------------------------ clouds
 lcr_status lcr_cloud_upload(lcr_ctx* ctx, const lcr_point* pts, size_t n, lcr_cloud** out) {

@@ -18,6 +18,25 @@ void dev_free(lcr_ctx* ctx, void* p) {
   if (p) CUDA_TRY(cudaFreeAsync(p, ctx->stream));
 }
 
+KernelTimer::KernelTimer(lcr_ctx* c, int w) : ctx(c), which(w) {
+  if (!ctx->timing) return;
+  for (cudaEvent_t* e : {&a, &b}) {
+    if (!ctx->event_pool.empty()) {
+      *e = ctx->event_pool.back();
+      ctx->event_pool.pop_back();
+    } else {
+      CUDA_TRY(cudaEventCreate(e));
+    }
+  }
+  CUDA_TRY(cudaEventRecord(a, ctx->stream));
+}
+
+KernelTimer::~KernelTimer() {
+  if (!a) return;
+  cudaEventRecord(b, ctx->stream);
+  ctx->kt[which].pending.emplace_back(a, b);
+}
+
 void* pinned(lcr_ctx* ctx, size_t bytes) {
   if (bytes > ctx->pinned_bytes) {
     sync(ctx);

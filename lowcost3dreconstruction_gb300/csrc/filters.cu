@@ -17,29 +17,68 @@ namespace {
 // round: all terms are non-negative multiples of u = the smallest ulp among the
 // nonzero float terms, so every partial sum is a multiple of u no larger than
 // the total T, and T < 2^53 u makes all of them representable.  Then
-// sum(results 1..k) = T - sqrt(d_min) exactly.  A tile with a lane that fails
-// the test (a dynamic range above ~2^23 between neighbour distances) is
-// queued and redone by k_sor_dist_sorted.
+// sum(results 1..k) = T - sqrt(d_min) exactly.  The terms are added exactly as
+// 64-bit integers on a grid of 2^eg below the largest possible term (integer
+// adds instead of FP64 ones); a term below that grid, or a lane that fails the
+// test (a dynamic range above ~2^23 between neighbour distances), sends the
+// tile to k_sor_dist_sorted.
 struct SorAcc {
-  double sum;
+  long long sum;  // exact sum in units of 2^eg
+  int eg;         // grid exponent
   float dmin;
-  int emin;  // smallest biased exponent (>= 1) of a nonzero term
+  int emin;       // smallest biased exponent (>= 1) of a nonzero term
   int cnt;
+  bool off_grid;
+  __device__ __forceinline__ void init() {
+    sum = 0;
+    eg = 0;
+    dmin = LCR_INF;
+    emin = 255;
+    cnt = 0;
+    off_grid = false;
+  }
+  // tau bounds every d to be added: terms are <= sqrt(tau) < 2^(E+24) with
+  // E = exponent of sqrt(tau) - 150; a term shifted onto the grid stays below
+  // 2^56 and k of them below 2^63 for k < 128 (the shift shrinks beyond).
+  __device__ __forceinline__ void begin(float tau, int K) {
+    const int e = static_cast<int>(__float_as_uint(__fsqrt_rn(tau)) >> 23);
+    int lg = 0;
+    while ((1 << lg) < K) ++lg;
+    eg = max(e, 1) - 150 - (38 - lg);
+  }
+  __device__ __forceinline__ long long units(float v) {
+    const uint32_t bits = __float_as_uint(v);
+    const int e = static_cast<int>(bits >> 23);
+    const long long man = e ? static_cast<long long>((bits & 0x7fffffu) | 0x800000u) : static_cast<long long>(bits);
+    const int sh = max(e, 1) - 150 - eg;
+    if (sh < 0 || sh > 39) {
+      off_grid = true;
+      return 0;
+    }
+    return man << sh;
+  }
   __device__ __forceinline__ void add_d(float d) {
     const float v = __fsqrt_rn(d);
     ++cnt;
-    sum = __dadd_rn(sum, static_cast<double>(v));
     dmin = fminf(dmin, d);
-    if (v > 0.f) emin = min(emin, max(1, static_cast<int>(__float_as_uint(v) >> 23)));
+    if (v > 0.f) {
+      sum += units(v);
+      emin = min(emin, max(1, static_cast<int>(__float_as_uint(v) >> 23)));
+    }
   }
   __device__ __forceinline__ void add(const float4&, float d) { add_d(d); }
   __device__ __forceinline__ void add_key(unsigned long long k) { add_d(key_dist(k)); }
-  // true if the sum is exact; s = sum of all terms but the smallest
-  __device__ __forceinline__ bool result(double& s) const {
-    // ulp of a float with biased exponent e is 2^(max(e,1) - 150); bound 2^(emin - 97)
-    const double bound = emin >= 255 ? LCR_INF : __longlong_as_double(static_cast<long long>(emin - 97 + 1023) << 52);
-    if (!(sum < bound)) return false;
-    s = __dsub_rn(sum, static_cast<double>(__fsqrt_rn(dmin)));
+  // true if the ascending double sum is the exact one; s = that sum of all
+  // terms but the smallest
+  __device__ __forceinline__ bool result(double& s) {
+    if (off_grid) return false;
+    // T < 2^53 u, u = 2^(emin - 150) = 2^(emin - 150 - eg) grid units
+    const int lim = 53 + emin - 150 - eg;
+    if (emin < 255 && lim < 63 && sum >= (1ll << lim)) return false;
+    const float vmin = __fsqrt_rn(dmin);
+    const long long t = sum - (vmin > 0.f ? units(vmin) : 0ll);
+    if (off_grid) return false;
+    s = __dmul_rn(__ll2double_rn(t), __longlong_as_double(static_cast<long long>(eg + 1023) << 52));
     return true;
   }
 };
@@ -68,10 +107,7 @@ __global__ void k_sor_dist(IndexView ix, int mean_k, float* __restrict__ dist, u
   float4 tlo, thi;
   if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
   SorAcc acc;
-  acc.sum = 0.0;
-  acc.dmin = LCR_INF;
-  acc.emin = 255;
-  acc.cnt = 0;
+  acc.init();
   tile_kset(ix, q.x, q.y, q.z, qv, K, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), wbase + sizeof(KnnWarp), tile,
             acc);
   if (qv && acc.cnt < K) *too_few = 1;
@@ -273,6 +309,7 @@ struct NeAcc {
     syy += dy * dy; syz += dy * dz; szz += dz * dz;
     ++m;
   }
+  __device__ __forceinline__ void begin(float, int) {}
   __device__ __forceinline__ void add_key(unsigned long long k) { add(xyz[key_idx(k)], 0.f); }
 };
 
@@ -375,9 +412,9 @@ __global__ void k_crop(IndexView tgt, IndexView src, double r, uint8_t* __restri
 
 size_t list_smem(int nw, int K) { return nw * knn_warp_bytes(K); }
 
-// Warps per block of the unordered k-NN kernels (12 KB of shared memory per
-// warp: 6 warps x 3 blocks = 18 resident warps per SM).
-constexpr int kSetWarps = 6;
+// Warps per block of the unordered k-NN kernels (11 KB of shared memory per
+// warp: 5 warps x 4 blocks = 20 resident warps per SM).
+constexpr int kSetWarps = 5;
 
 // Queue of tiles the unordered form hands to the sorted form: [0] = count,
 // [1..] = tile ids.  Its grid: one block per SM, warps striding the queue.
@@ -423,8 +460,11 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
   CUDA_TRY(cudaFuncSetAttribute(k_sor_dist, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_set)));
   CUDA_TRY(cudaFuncSetAttribute(k_sor_dist_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 static_cast<int>(smem)));
-  LCR_LAUNCH(ctx, k_sor_dist, (ix.nleaf + kSetWarps - 1) / kSetWarps, kSetWarps * 32, smem_set, ix, mean_k, dist,
-             valid, nvalid, rq.tiles(), rq.count(), too_few);
+  {
+    KernelTimer kt(ctx, LCR_KT_SOR_KNN);
+    LCR_LAUNCH(ctx, k_sor_dist, (ix.nleaf + kSetWarps - 1) / kSetWarps, kSetWarps * 32, smem_set, ix, mean_k, dist,
+               valid, nvalid, rq.tiles(), rq.count(), too_few);
+  }
   LCR_LAUNCH(ctx, k_sor_dist_sorted, ctx->sms, nw * 32, smem, ix, mean_k, dist, valid, nvalid, rq.tiles(), rq.count());
   dev_free(ctx, rq.block);
   // blocked sums (ping-pong between two halves of `sums`)
@@ -495,8 +535,11 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
   const size_t smem_set = kSetWarps * kset_warp_bytes();
   const int flip = (flags & LCR_NORMALS_FLIP_ALL) ? 1 : 0;
   CUDA_TRY(cudaFuncSetAttribute(k_normals, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_set)));
-  LCR_LAUNCH(ctx, k_normals, (ix.nleaf + kSetWarps - 1) / kSetWarps, kSetWarps * 32, smem_set, ix, k, in->xyz, vp[0],
-             vp[1], vp[2], flip, out->nrm);
+  {
+    KernelTimer kt(ctx, LCR_KT_NORMALS_KNN);
+    LCR_LAUNCH(ctx, k_normals, (ix.nleaf + kSetWarps - 1) / kSetWarps, kSetWarps * 32, smem_set, ix, k, in->xyz,
+               vp[0], vp[1], vp[2], flip, out->nrm);
+  }
   out->index = share_index(in->index);  // same points in the same order
   return out;
 }

@@ -6,6 +6,8 @@
 
 #include <cstdio>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/lcr.h"
 
@@ -46,7 +48,7 @@ struct LcrError {
 // ---------------------------------------------------------- search index
 // Morton-sorted points grouped into leaves of 32 (one warp-wide float4 load per
 // leaf) with a 32-ary hierarchy of axis-aligned boxes above them.
-constexpr int kMaxLevels = 8;
+constexpr int kMaxLevels = 6;  // root level <= 5: up to 32^6 = 2^30 points per cloud
 
 struct IndexView {
   const float4* pts;            // npad = nleaf*32 sorted points, w = original index (int bits), sentinel NaN / -1
@@ -89,6 +91,23 @@ struct lcr_ctx {
   // captured ICP loops (one per method), reused across calls
   cudaGraphExec_t icp_exec[2] = {nullptr, nullptr};
   int icp_graph_ok = -1;        // -1 unknown, 0 unavailable, 1 usable
+  // optional event timing of selected kernels (lcr_kernel_timing)
+  bool timing = false;
+  struct KTimer {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+    double ms = 0.0;
+    uint64_t launches = 0;
+  } kt[LCR_KT_COUNT];
+  std::vector<cudaEvent_t> event_pool;
+};
+
+// Brackets one launch with events when timing is on (see lcr_kernel_timing).
+struct KernelTimer {
+  lcr_ctx* ctx;
+  int which;
+  cudaEvent_t a = nullptr, b = nullptr;
+  KernelTimer(lcr_ctx* c, int w);
+  ~KernelTimer();
 };
 
 // --------------------------------------------------------- memory helpers

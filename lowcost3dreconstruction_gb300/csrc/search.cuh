@@ -17,7 +17,9 @@
 
 #define LCR_INF __int_as_float(0x7f800000)
 
-constexpr int kStack = 32 * kMaxLevels + 32;
+// Deepest stack: the root, then 31 more entries per level below it (a popped
+// node pushes at most 32 children): 1 + 31 * top <= 156 for top <= 5.
+constexpr int kStack = 32 * (kMaxLevels - 1) + 8;
 
 struct WarpScratch {
   uint32_t node[kStack];
@@ -334,7 +336,7 @@ __device__ __forceinline__ void tile_nn1(const IndexView& ix, float qx, float qy
 //          instead (rare: many points in the boundary bin, e.g. duplicates).
 // The result is the exact first k keys in (distance, index) order, in
 // list[j*32 + lane], j < k.
-constexpr int kLeafList = 256;
+constexpr int kLeafList = 192;
 constexpr int kBins = 64;
 
 __host__ __device__ constexpr int knn_buffer(int K) { return K + 32; }
@@ -381,18 +383,31 @@ struct KHist {
   }
   __device__ __forceinline__ void scan(const float4* st) {
     float tau = bound();
-    for (int j = 0; j < 32; ++j) {
-      const float4 p = st[j];
-      const float d = exact_dist2(qx, qy, qz, p.x, p.y, p.z);
-      if (!(d <= tau)) continue;
-      const int b = bin(d);
-      hist[b * 32 + lane] += 1u;
-      ++cl;
-      while (bs > 1 && cl - static_cast<int>(hist[(bs - 1) * 32 + lane]) >= K) {
-        cl -= static_cast<int>(hist[(bs - 1) * 32 + lane]);
-        --bs;
+    for (int j0 = 0; j0 < 32; j0 += 4) {
+      // four independent distances first (the staged loads and the FP32
+      // chains overlap), then the order-dependent histogram updates
+      float dd[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float4 p = st[j0 + u];
+        dd[u] = exact_dist2(qx, qy, qz, p.x, p.y, p.z);
       }
-      tau = bound();
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+      const float d = dd[u];
+      if (!(d <= tau)) continue;
+      hist[bin(d) * 32 + lane] += 1u;
+      if (++cl >= K) {
+        // drop the top bins while the ones below still hold k candidates
+        while (bs > 1) {
+          const int top = static_cast<int>(hist[(bs - 1) * 32 + lane]);
+          if (cl - top < K) break;
+          cl -= top;
+          --bs;
+        }
+        tau = fminf(edge(bs - 1), cap);
+      }
+      }
     }
   }
   // Leaves [seed_lo, seed_hi] were scanned before the traversal.
@@ -625,6 +640,7 @@ struct KRefine {
     return active && box_dist2(lo, hi, qx, qy, qz) <= tau;
   }
   __device__ __forceinline__ void scan(const float4* st) {
+#pragma unroll 4
     for (int j = 0; j < 32; ++j) {
       const float4 p = st[j];
       const float d = exact_dist2(qx, qy, qz, p.x, p.y, p.z);
@@ -661,9 +677,18 @@ struct KSet {
     return qv && box_dist2(lo, hi, qx, qy, qz) <= tau;
   }
   __device__ __forceinline__ void scan(const float4* st) {
-    for (int j = 0; j < 32; ++j) {
-      const float4 p = st[j];
-      const float d = exact_dist2(qx, qy, qz, p.x, p.y, p.z);
+    for (int j0 = 0; j0 < 32; j0 += 4) {
+      float4 pp[4];
+      float dd[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        pp[u] = st[j0 + u];
+        dd[u] = exact_dist2(qx, qy, qz, pp[u].x, pp[u].y, pp[u].z);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+      const float4 p = pp[u];
+      const float d = dd[u];
       if (!(d <= tau)) continue;
       const unsigned long long k = make_key(d, __float_as_uint(p.w));
       if (k < klo) {
@@ -671,6 +696,7 @@ struct KSet {
       } else if (k <= khi) {
         if (nb < kBoundCap) bbuf[nb * 32 + lane] = k;
         ++nb;
+      }
       }
     }
   }
@@ -681,8 +707,9 @@ struct KSet {
 
 // Feeds the k nearest points of each valid lane (exact set under the
 // (distance, index) order; all points if the cloud holds fewer than k) to acc:
-// acc.add(point, d) for points met in the collect pass, acc.add_key(key) for
-// the selected boundary keys.  Queries are the points of leaf self_leaf of ix.
+// acc.begin(tau, k) with the largest squared distance that can be fed, then
+// acc.add(point, d) for points met in the collect pass and acc.add_key(key)
+// for the selected boundary keys.  Queries are the points of leaf self_leaf of ix.
 template <class Acc>
 __device__ __forceinline__ void tile_kset(const IndexView& ix, float qx, float qy, float qz, bool qv, int K,
                                           const float4& tlo, const float4& thi, KnnWarp& kw, unsigned char* region,
@@ -744,6 +771,7 @@ __device__ __forceinline__ void tile_kset(const IndexView& ix, float qx, float q
   s.acc = &acc;
   s.ws = &kw.ws;
   s.R = subtile_radius(s.tau, qv, kw.ws);
+  acc.begin(s.tau, K);
   knn_pass2(ix, h, s, tlo, thi, kw);
   if (qv && m > 0) {
     // partial selection sort: the m smallest of the nb (<= kBoundCap) boundary keys

@@ -125,6 +125,26 @@ LCR_API lcr_status lcr_backproject(lcr_ctx* ctx, const void* depth, const lcr_de
 /* Same with the depth frames already on the context's device. */
 LCR_API lcr_status lcr_backproject_device(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p,
                                           lcr_cloud** out);
+/* No counterpart in the reference.  lcr_backproject_device for callers that
+ * cannot allocate device memory: a capture loop that runs in a fixed device-
+ * memory budget next to the camera driver, or that must not stall in the
+ * allocator between frames.  It allocates nothing: the kept pixels are written
+ * as lcr_point records, in row-major pixel order, into d_points (caller-owned
+ * device memory, capacity records), and their number to *d_count (a
+ * caller-owned device uint32); records past capacity are not written, so
+ * compare *d_count with capacity (capacity = width*height always suffices).
+ * The points are the ones lcr_backproject_device gives, bit for bit.  The
+ * scratch (the fused image of a burst and the compaction's block counts) is
+ * one static device buffer of 1.2 MB per device, so width*height may be at
+ * most 307200 (640x480); larger images return LCR_ERR_INVALID_ARG.  Nothing
+ * in the scratch carries over between calls (every block count is written
+ * before it is read), so it needs no clearing.  The first call on a device
+ * looks up the scratch's address (cudaGetSymbolAddress): make it before any
+ * stream capture.  All contexts on a device share the scratch: calls that
+ * overlap in time (other streams, contexts or threads) race on it.  Returns
+ * without synchronising; the results are ready when the context's stream is. */
+LCR_API lcr_status lcr_backproject_into(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p,
+                                        lcr_point* d_points, size_t capacity, uint32_t* d_count);
 /* The fused (zero-eliminated mean) depth image alone, host in/out: uint16 for
  * V1 (super_resolution.cpp:295-315), float for V2 (super_resolution_kv2.cpp:287-303). */
 LCR_API lcr_status lcr_burst_fuse(lcr_ctx* ctx, const void* frames, const lcr_depth_params* p, void* fused_out);

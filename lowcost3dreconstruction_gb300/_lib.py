@@ -94,6 +94,7 @@ _SIGS = {
     "lcr_backproject": (C.c_int, [_VP, _VP, C.POINTER(DepthParams), C.POINTER(_VP)]),
     "lcr_backproject_device": (C.c_int, [_VP, _VP, C.POINTER(DepthParams), C.POINTER(_VP)]),
     "lcr_burst_fuse": (C.c_int, [_VP, _VP, C.POINTER(DepthParams), _VP]),
+    "lcr_backproject_into": (C.c_int, [_VP, _VP, C.POINTER(DepthParams), _VP, C.c_size_t, _VP]),
     "lcr_voxel_grid": (C.c_int, [_VP, _VP, C.c_float, C.c_float, C.c_float, C.POINTER(_VP)]),
     "lcr_sor": (C.c_int, [_VP, _VP, C.c_int, C.c_double, C.POINTER(_VP), C.POINTER(_VP), C.POINTER(SorStats)]),
     "lcr_sor_distances": (C.c_int, [_VP, _VP, C.c_int, _VP, C.POINTER(SorStats)]),

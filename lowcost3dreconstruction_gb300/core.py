@@ -171,6 +171,13 @@ class Context:
     def backproject_device(self, dev_ptr: int, params: L.DepthParams) -> Cloud:
         return self._cloud(self.lib.lcr_backproject_device, C.c_void_p(dev_ptr), C.byref(params))
 
+    def backproject_into(self, dev_ptr: int, params: L.DepthParams, points_ptr: int, capacity: int,
+                         count_ptr: int) -> None:
+        """lcr_backproject_into: records into caller-owned device memory, the
+        count into a device uint32; asynchronous on this context's stream."""
+        self._check(self.lib.lcr_backproject_into(self.h, C.c_void_p(dev_ptr), C.byref(params),
+                                                  C.c_void_p(points_ptr), capacity, C.c_void_p(count_ptr)))
+
     def burst_fuse(self, frames: np.ndarray, params: L.DepthParams) -> np.ndarray:
         want = np.uint16 if params.model == L.KINECT_V1 else np.float32
         frames = np.ascontiguousarray(frames, dtype=want)

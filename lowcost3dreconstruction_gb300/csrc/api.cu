@@ -241,6 +241,16 @@ lcr_status lcr_backproject_device(lcr_ctx* ctx, const void* d_depth, const lcr_d
   return LCR_OK;
 }
 
+lcr_status lcr_backproject_into(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p, lcr_point* d_points,
+                                size_t capacity, uint32_t* d_count) {
+  API_BEGIN(ctx)
+  check_depth(p);
+  REQUIRE(d_depth && d_count && (d_points || capacity == 0), "null argument");
+  backproject_into_run(ctx, d_depth, p, d_points, capacity, d_count);
+  API_END(ctx)
+  return LCR_OK;
+}
+
 lcr_status lcr_backproject(lcr_ctx* ctx, const void* depth, const lcr_depth_params* p, lcr_cloud** out) {
   API_BEGIN(ctx)
   check_depth(p);

@@ -2,6 +2,7 @@
 // Kinect v1 / v2 back-projections, reproducing the reference's arithmetic with
 // explicit IEEE intrinsics (no FMA contraction) so results are bit-exact.
 #include <algorithm>
+#include <mutex>
 
 #include "lcr_internal.cuh"
 
@@ -226,4 +227,158 @@ int backproject_run(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p
   dev_free(ctx, fused);
   *out = c;
   return n;
+}
+
+// ------------------------------------------------- allocation-free variant
+// lcr_backproject_into: the same points as backproject_run, written as
+// lcr_point records into caller-owned device memory, with its scratch in one
+// static device buffer (the fused image of a burst and the per-block counts of
+// the compaction) instead of allocations.
+namespace {
+
+constexpr int kIntoMaxPixels = 640 * 480;                   // the largest image the scratch holds
+constexpr int kIntoBlock = 256;                             // pixels per compaction block
+constexpr int kIntoMaxBlocks = kIntoMaxPixels / kIntoBlock;  // 1200
+constexpr size_t kIntoFusedBytes = static_cast<size_t>(kIntoMaxPixels) * 4;  // float (v2) or uint16 (v1)
+constexpr size_t kIntoScratchBytes = kIntoFusedBytes + static_cast<size_t>(kIntoMaxBlocks) * 4;
+constexpr int kIntoMaxDevices = 64;
+
+__device__ __align__(256) unsigned char g_into_scratch[kIntoScratchBytes];
+
+std::mutex g_into_mutex;
+void* g_into_addr[kIntoMaxDevices] = {};
+
+// Device address of the scratch on `device` (looked up once per device).
+unsigned char* into_scratch(int device) {
+  if (device < 0 || device >= kIntoMaxDevices)
+    LCR_THROW(LCR_ERR_INVALID_ARG, "lcr_backproject_into supports devices 0..%d", kIntoMaxDevices - 1);
+  std::lock_guard<std::mutex> lock(g_into_mutex);
+  if (!g_into_addr[device]) {
+    void* a = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&a, g_into_scratch);
+    if (e != cudaSuccess) LCR_THROW(LCR_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+    g_into_addr[device] = a;
+  }
+  return static_cast<unsigned char*>(g_into_addr[device]);
+}
+
+// Kept pixel test of one pixel, and its record, for either camera model.
+template <int V1>
+__device__ __forceinline__ bool into_keep(const void* depth, const BP& b, int p) {
+  const int i = p / b.w, j = p - i * b.w;
+  if (V1) return keep_v1(b, i, j, static_cast<const uint16_t*>(depth)[p]);
+  float3 q;
+  return point_v2(b, static_cast<const float*>(depth), i, j, q);
+}
+
+template <int V1>
+__device__ __forceinline__ void into_record(const void* depth, const BP& b, int p, float4* __restrict__ rec) {
+  const int i = p / b.w, j = p - i * b.w;
+  float4 xyz;
+  float3 nn = make_float3(0.f, 0.f, 0.f);
+  if (V1) {
+    // depth_capture.cpp:294-308, as k_emit_v1
+    const uint16_t* d = static_cast<const uint16_t*>(depth);
+    const int z = d[p];
+    const double vx = __dmul_rn(__dmul_rn(static_cast<double>(z), __dsub_rn(static_cast<double>(j), b.cx)), b.ifx);
+    const double vy = __dmul_rn(__dmul_rn(static_cast<double>(-z), __dsub_rn(static_cast<double>(i), b.cy)), b.ify);
+    const double vz = static_cast<double>(-z);
+    xyz = make_float4(__double2float_rn(__dmul_rn(vx, b.scale)), __double2float_rn(__dmul_rn(vy, b.scale)),
+                      __double2float_rn(__dmul_rn(vz, b.scale)), 1.f);
+    if (b.normals) nn = image_normal(d, b.w, b.h, i, j);
+  } else {
+    float3 q = make_float3(0.f, 0.f, 0.f);
+    point_v2(b, static_cast<const float*>(depth), i, j, q);
+    xyz = make_float4(__fmul_rn(b.scalef, q.x), __fmul_rn(b.scalef, q.y), __fmul_rn(b.scalef, q.z), 1.f);
+  }
+  // lcr_point: {x y z 1} {nx ny nz 0} {rgba curvature 0 0}
+  rec[0] = xyz;
+  rec[1] = make_float4(nn.x, nn.y, nn.z, 0.f);
+  rec[2] = make_float4(__uint_as_float(b.rgb), 0.f, 0.f, 0.f);
+}
+
+template <int V1>
+__global__ void __launch_bounds__(kIntoBlock) k_into_count(const void* depth, BP b, uint32_t* __restrict__ counts) {
+  const int p = blockIdx.x * kIntoBlock + threadIdx.x;
+  const bool k = p < b.w * b.h && into_keep<V1>(depth, b, p);
+  const int c = __syncthreads_count(k);
+  if (threadIdx.x == 0) counts[blockIdx.x] = static_cast<uint32_t>(c);
+}
+
+// Exclusive scan of the block counts in place (one block; nblk <= 1200) and
+// the total into *count.
+__global__ void __launch_bounds__(1024) k_into_scan(uint32_t* __restrict__ counts, int nblk, uint32_t* count) {
+  __shared__ uint32_t s_w[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  uint32_t carry = 0;
+  for (int base = 0; base < nblk; base += 1024) {
+    const int i = base + t;
+    const uint32_t v = i < nblk ? counts[i] : 0u;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(LCR_FULL, incl, o);
+      if (lane >= o) incl += u;
+    }
+    if (lane == 31) s_w[w] = incl;
+    __syncthreads();
+    uint32_t before = 0, all = 0;
+    for (int k = 0; k < 32; ++k) {
+      before += k < w ? s_w[k] : 0u;
+      all += s_w[k];
+    }
+    if (i < nblk) counts[i] = carry + before + incl - v;
+    carry += all;
+    __syncthreads();
+  }
+  if (t == 0) *count = carry;
+}
+
+// Each block recomputes its pixels' keep flags, ranks them in pixel order and
+// writes their records from its scanned offset; nothing past `capacity`.
+template <int V1>
+__global__ void __launch_bounds__(kIntoBlock) k_into_emit(const void* depth, BP b, const uint32_t* __restrict__ offs,
+                                                          float4* __restrict__ rec, size_t capacity) {
+  __shared__ uint32_t s_w[kIntoBlock / 32];
+  const int p = blockIdx.x * kIntoBlock + threadIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const bool k = p < b.w * b.h && into_keep<V1>(depth, b, p);
+  const unsigned m = __ballot_sync(LCR_FULL, k);
+  if (lane == 0) s_w[w] = __popc(m);
+  __syncthreads();
+  uint32_t before = 0;
+  for (int j = 0; j < w; ++j) before += s_w[j];
+  if (!k) return;
+  const size_t pos = static_cast<size_t>(offs[blockIdx.x]) + before + __popc(m & ((1u << lane) - 1u));
+  if (pos < capacity) into_record<V1>(depth, b, p, rec + 3 * pos);
+}
+
+}  // namespace
+
+void backproject_into_run(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p, lcr_point* d_points,
+                          size_t capacity, uint32_t* d_count) {
+  const long long npix = static_cast<long long>(p->width) * p->height;
+  if (npix > kIntoMaxPixels)
+    LCR_THROW(LCR_ERR_INVALID_ARG, "lcr_backproject_into: %dx%d = %lld pixels exceeds its %d-pixel scratch (640x480)",
+              p->width, p->height, npix, kIntoMaxPixels);
+  unsigned char* scratch = into_scratch(ctx->device);
+  void* fused = scratch;
+  uint32_t* counts = reinterpret_cast<uint32_t*>(scratch + kIntoFusedBytes);
+  const BP b = make_bp(p);
+  const void* depth = d_depth;
+  if (p->frames > 1) {
+    burst_fuse_run(ctx, d_depth, p, fused);
+    depth = fused;
+  }
+  const int nblk = static_cast<int>((npix + kIntoBlock - 1) / kIntoBlock);
+  float4* rec = reinterpret_cast<float4*>(d_points);
+  if (p->model == LCR_DEPTH_KINECT_V1) {
+    LCR_LAUNCH(ctx, k_into_count<1>, nblk, kIntoBlock, 0, depth, b, counts);
+    LCR_LAUNCH(ctx, k_into_scan, 1, 1024, 0, counts, nblk, d_count);
+    LCR_LAUNCH(ctx, k_into_emit<1>, nblk, kIntoBlock, 0, depth, b, counts, rec, capacity);
+  } else {
+    LCR_LAUNCH(ctx, k_into_count<0>, nblk, kIntoBlock, 0, depth, b, counts);
+    LCR_LAUNCH(ctx, k_into_scan, 1, 1024, 0, counts, nblk, d_count);
+    LCR_LAUNCH(ctx, k_into_emit<0>, nblk, kIntoBlock, 0, depth, b, counts, rec, capacity);
+  }
 }

@@ -220,6 +220,8 @@ void knn_run(lcr_ctx* ctx, const lcr_cloud* ref, const lcr_cloud* query, int k, 
              float* d_dist);
 int backproject_run(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p, lcr_cloud** out);
 void burst_fuse_run(lcr_ctx* ctx, const void* d_frames, const lcr_depth_params* p, void* d_out);
+void backproject_into_run(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p, lcr_point* d_points,
+                          size_t capacity, uint32_t* d_count);
 lcr_cloud* voxel_run(lcr_ctx* ctx, const lcr_cloud* in, float lx, float ly, float lz);
 void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_cloud** inliers,
              lcr_cloud** outliers, lcr_sor_stats* stats, float* host_dist);

@@ -197,13 +197,11 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     torch.cuda.synchronize()
     e2e_aligned, e2e_ms, _, _, _ = timed(False, None)
     if dist is not None:
+        # replicas: the slowest rank's clock, every rank's aligned pairs
+        from lowcost3dreconstruction_gb300.replicas import combine
         dist.barrier()
-        t = torch.tensor([dev_ms, e2e_ms, float(aligned), float(e2e_aligned)], device=f"cuda:{dev}",
-                         dtype=torch.float64)
-        tmax = t.clone()
-        dist.all_reduce(tmax[:2], op=dist.ReduceOp.MAX)
-        dist.all_reduce(tmax[2:], op=dist.ReduceOp.SUM)
-        dev_ms, e2e_ms, aligned, e2e_aligned = [float(x) for x in tmax.tolist()]
+        (dev_ms, e2e_ms), (aligned, e2e_aligned) = combine(dist, [dev_ms, e2e_ms], [aligned, e2e_aligned],
+                                                           device=f"cuda:{dev}")
     if rank != 0:
         ctx.close()
         return None

@@ -564,9 +564,16 @@ VoxelSetup voxel_setup(const orc_point* in, size_t n, float lx, float ly, float 
   for (int a = 0; a < 3; ++a) {
     float ext = mx[a] - mn[a];
     float cells = ext * s.inv[a];
+    if (!(cells < 9.0e18f)) {  // would not fit int64: PCL's product overflows (undefined); refuse
+      s.overflow = true;
+      return s;
+    }
     d[a] = static_cast<int64_t>(cells) + 1;
   }
-  if (d[0] * d[1] * d[2] > static_cast<int64_t>(std::numeric_limits<int32_t>::max())) {
+  // PCL tests dx*dy*dz > INT32_MAX in int64, which itself overflows for huge
+  // ranges; the product is checked in double first so those refuse as well.
+  const double prod = static_cast<double>(d[0]) * static_cast<double>(d[1]) * static_cast<double>(d[2]);
+  if (prod > 2147483647.0 || d[0] * d[1] * d[2] > static_cast<int64_t>(std::numeric_limits<int32_t>::max())) {
     s.overflow = true;
     return s;
   }

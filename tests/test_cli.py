@@ -1,0 +1,104 @@
+"""The command-line tools are drop-ins for pcl_tools: same flags and defaults,
+`-h` exits 0, usage and load errors exit 255 (the reference's `return -1`)
+with the reference's messages.  CPU tests stop before any GPU work; the
+`gpu` tests run the tools end to end against the oracle."""
+from __future__ import annotations
+
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import random_cloud
+
+ROOT = Path(__file__).resolve().parents[1]
+BIN = ROOT / "lowcost3dreconstruction_gb300" / "bin"
+
+# tool -> flags its help must list (pcl_tools/<tool>.cpp option tables)
+TOOLS = {
+    "cloud_downsampling": ["--input", "--output", "--leaf_size"],
+    "outlier_removal": ["--input", "--output", "--outliers_file", "--neighbors", "--dev_mult"],
+    "normal_estimation": ["--input", "--output", "--neighbors", "--reverse_normals", "--centroid", "--origin"],
+    "fine_registration": ["--input", "--target", "--output", "--accumulated", "--distance_threshold",
+                          "--max_iterations", "--transformation_epsilon", "--euclidean_fitness_epsilon"],
+    "accumulate_clouds": ["--input", "--target", "--output", "--radius", "--clean_neighbors", "--dev_mult",
+                          "--negative", "--all"],
+    "centroid_align": ["--input", "--target", "--output", "--roll", "--pitch", "--yaw", "--elevation"],
+    "transform": ["--input", "--output", "--transform"],
+    "scale": ["--input", "--output", "--scale"],
+}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def tools():
+    from lowcost3dreconstruction_gb300 import build
+    build.build_lib()
+    build.build_tools()
+
+
+def run(tool, *args, cwd=None):
+    return subprocess.run([str(BIN / tool), *map(str, args)], capture_output=True, text=True, timeout=120, cwd=cwd)
+
+
+@pytest.mark.parametrize("tool", sorted(TOOLS))
+def test_help_lists_the_reference_flags(tool):
+    r = run(tool, "-h")
+    assert r.returncode == 0, r.stderr
+    for f in TOOLS[tool]:
+        assert f in r.stdout, (tool, f)
+
+
+@pytest.mark.parametrize("tool", sorted(TOOLS))
+def test_missing_arguments_exit_255_with_usage(tool):
+    r = run(tool)
+    assert r.returncode == 255
+    assert "Correct mode of use" in (r.stdout + r.stderr)
+
+
+@pytest.mark.parametrize("tool", ["outlier_removal", "fine_registration", "cloud_downsampling"])
+def test_unknown_option_exits_255(tool):
+    r = run(tool, "--bogus", "1")
+    assert r.returncode == 255
+
+
+def test_missing_input_file_message(tmp_path):
+    r = run("outlier_removal", "-i", tmp_path / "nope.ply", "-o", tmp_path / "o.ply")
+    assert r.returncode == 255
+    assert "Couldn't load input point cloud" in (r.stdout + r.stderr)
+
+
+def test_fine_registration_rejects_nonpositive_iterations(tmp_path):
+    from lowcost3dreconstruction_gb300 import _lib as L
+    pts = random_cloud(50, 1)
+    L.write_ply(tmp_path / "a.ply", pts)
+    r = run("fine_registration", "-i", tmp_path / "a.ply", "-t", tmp_path / "a.ply", "-o", tmp_path / "o.ply",
+            "--max_iterations", "0")
+    assert r.returncode == 255
+    assert "max_iterations needs to be greater than zero" in (r.stdout + r.stderr)
+
+
+# ------------------------------------------------------------ end to end
+@pytest.mark.gpu
+def test_tools_chain_matches_oracle(tmp_path, cfg0):
+    from lowcost3dreconstruction_gb300 import _lib as L
+    from oracle import oracle as O
+    src, tgt = cfg0["src"], cfg0["tgt"]
+    L.write_ply(tmp_path / "s.ply", src)
+    L.write_ply(tmp_path / "t.ply", tgt)
+    assert run("cloud_downsampling", "-i", tmp_path / "s.ply", "-o", tmp_path / "sv.ply", "-s", "0.002").returncode == 0
+    assert run("cloud_downsampling", "-i", tmp_path / "t.ply", "-o", tmp_path / "tv.ply", "-s", "0.002").returncode == 0
+    sv = L.read_ply(tmp_path / "sv.ply")
+    np.testing.assert_array_equal(sv["x"].view(np.uint32), cfg0["vsrc"]["x"].view(np.uint32))
+    r = run("outlier_removal", "-i", tmp_path / "sv.ply", "-o", tmp_path / "so.ply", "-n", "20", "-d", "2.0")
+    assert r.returncode == 0, r.stderr
+    _, keep, _ = O.sor(cfg0["vsrc"], 20, 2.0)
+    assert len(L.read_ply(tmp_path / "so.ply")) == int(keep.sum())
+    r = run("fine_registration", "-i", tmp_path / "sv.ply", "-t", tmp_path / "tv.ply", "-o", tmp_path / "reg.ply",
+            "--distance_threshold", "0.05", "--max_iterations", "50", "--transformation_epsilon", "1e-8")
+    assert r.returncode == 0, r.stderr
+    assert "Has converged" in r.stdout and "Score" in r.stdout
+    ref = O.icp(cfg0["vsrc"], cfg0["vtgt"], max_corr_dist=0.05, max_iterations=50, transformation_epsilon=1e-8)
+    reg = L.read_ply(tmp_path / "reg.ply")
+    want = O.transform(cfg0["vsrc"], ref["transform"].astype(np.float32))
+    np.testing.assert_allclose(reg["x"], want["x"], atol=2e-5)

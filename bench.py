@@ -22,6 +22,7 @@ import subprocess
 import sys
 import threading
 import time
+from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
 import numpy as np
@@ -111,8 +112,12 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     pr = make_inputs(1 + rank)
-    ctx = Context(dev)
-    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    # The two captures of a pair are independent: each runs on its own context
+    # (CUDA stream) from its own host thread, so their kernels overlap; the
+    # pair's ICP runs on the first context after an event wait on the second.
+    ctxs = [Context(dev), Context(dev)]
+    ctx = ctxs[0]
+    streams = [torch.cuda.ExternalStream(c.stream, device=dev) for c in ctxs]
     params = ctx.depth_params(L.KINECT_V1, 640, 480, frames=10, scale=0.001, depth_max=4000.0, normals=False)
     icp_params = ctx.icp_params(**ICP)
     frames = [np.ascontiguousarray(pr.src_frames), np.ascontiguousarray(pr.tgt_frames)]
@@ -121,37 +126,44 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
     stage_ms = {}
     sor_n: list[int] = []  # SOR input sizes, one per k_sor_dist launch
+    pool = ThreadPoolExecutor(max_workers=2)
 
-    def capture(c, src_is_device: bool, k: int, timing: dict | None):
+    def capture(k: int, src_is_device: bool, timing: dict | None):
+        c, st = ctxs[k], streams[k]
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)] if timing is not None else None
-        with torch.cuda.stream(stream):
-            if ev: ev[0].record()
-            cl = (ctx.backproject_device(d_frames[k].data_ptr(), params) if src_is_device
-                  else ctx.backproject(h_frames[k].numpy().view(np.uint16), params))
-            if ev: ev[1].record()
-            v = ctx.voxel_grid(cl, 0.001)
+        with torch.cuda.stream(st):
+            if ev: ev[0].record(st)
+            cl = (c.backproject_device(d_frames[k].data_ptr(), params) if src_is_device
+                  else c.backproject(h_frames[k].numpy().view(np.uint16), params))
+            if ev: ev[1].record(st)
+            v = c.voxel_grid(cl, 0.001)
             sor_n.append(len(v))
-            if ev: ev[2].record()
-            inl, _, _ = ctx.sor(v, 50, 1.0)
-            if ev: ev[3].record()
-            nrm = ctx.normals(inl, 30)
-            if ev: ev[4].record()
-        if timing is not None:
-            stream.synchronize()
-            for name, a, b in (("backproject", 0, 1), ("voxel", 1, 2), ("sor", 2, 3), ("normals", 3, 4)):
-                timing[name] = timing.get(name, 0.0) + ev[a].elapsed_time(ev[b])
-        return nrm
+            if ev: ev[2].record(st)
+            inl, _, _ = c.sor(v, 50, 1.0)
+            if ev: ev[3].record(st)
+            nrm = c.normals(inl, 30)
+            if ev: ev[4].record(st)
+        return nrm, ev
 
-    def step(device_inputs: bool, timing: dict | None = None):
-        src = capture(ctx, device_inputs, 0, timing)
-        tgt = capture(ctx, device_inputs, 1, timing)
+    def step(device_inputs: bool, timing: dict | None = None, start=None):
+        if start is not None:
+            streams[1].wait_event(start)  # the second stream starts with the timed region
+        futs = [pool.submit(capture, k, device_inputs, timing) for k in (0, 1)]
+        (src, ev0), (tgt, ev1) = [f.result() for f in futs]
+        done1 = torch.cuda.Event()
+        done1.record(streams[1])
+        streams[0].wait_event(done1)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            e0.record()
+        with torch.cuda.stream(streams[0]):
+            e0.record(streams[0])
             res = ctx.icp(src, tgt, icp_params)
-            e1.record()
-        stream.synchronize()
+            e1.record(streams[0])
+        streams[0].synchronize()
         if timing is not None:
+            streams[1].synchronize()
+            for ev in (ev0, ev1):
+                for name, a, b in (("backproject", 0, 1), ("voxel", 1, 2), ("sor", 2, 3), ("normals", 3, 4)):
+                    timing[name] = timing.get(name, 0.0) + ev[a].elapsed_time(ev[b])
             timing["icp"] = timing.get("icp", 0.0) + e0.elapsed_time(e1)
             timing["icp_iters"] = timing.get("icp_iters", 0) + res.iterations
         return src, tgt, res
@@ -168,19 +180,19 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     def timed(device_inputs: bool, timing: dict | None):
         aligned = 0
         total_ms = 0.0
-        launches0 = ctx.launches
+        launches0 = sum(c.launches for c in ctxs)
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize()
             ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            ea.record(stream)
-            _, _, res = step(device_inputs, timing)
-            eb.record(stream)
+            ea.record(streams[0])
+            _, _, res = step(device_inputs, timing, start=ea)
+            eb.record(streams[0])
             eb.synchronize()
             total_ms += ea.elapsed_time(eb)
             r = rmse_from_moments(res.transform64, pr.T_gt, m1, m2, nsrc)
             aligned += int(res.converged and r <= RMSE_LIMIT)
-        return aligned, total_ms, ctx.launches - launches0, r, res
+        return aligned, total_ms, sum(c.launches for c in ctxs) - launches0, r, res
 
     if dist is not None:
         dist.barrier()
@@ -188,10 +200,13 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     clocks = Clocks(dev)
     clocks.start()
     sor_n.clear()
-    ctx.kernel_timing(True)
+    for c in ctxs:
+        c.kernel_timing(True)
     aligned, dev_ms, launches, last_rmse, last_res = timed(True, stage_ms)
-    sor_ms, sor_launches = ctx.kernel_time(L.KT_SOR_KNN)
-    ctx.kernel_timing(False)
+    kt = [c.kernel_time(L.KT_SOR_KNN) for c in ctxs]
+    sor_ms, sor_launches = sum(t[0] for t in kt), sum(t[1] for t in kt)
+    for c in ctxs:
+        c.kernel_timing(False)
     sor_sizes = list(sor_n)
     clk = clocks.stop()
     torch.cuda.synchronize()
@@ -203,7 +218,9 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
         (dev_ms, e2e_ms), (aligned, e2e_aligned) = combine(dist, [dev_ms, e2e_ms], [aligned, e2e_aligned],
                                                            device=f"cuda:{dev}")
     if rank != 0:
-        ctx.close()
+        pool.shutdown()
+        for c in ctxs:
+            c.close()
         return None
 
     steps_total = args.steps * world
@@ -233,8 +250,9 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
         "config": {"workload": WORKLOAD, "points_src": nsrc, "points_tgt": ntgt, "l2": "flushed between steps "
                    "(256 MB write)", "icp": ICP, "rmse_limit_m": RMSE_LIMIT, "pairs_aligned": int(aligned),
                    "pairs_timed": steps_total, "last_rmse_m": last_rmse, "last_icp_iterations": last_res.iterations,
-                   "parallelism": f"replicas x{world}",
+                   "parallelism": f"replicas x{world}; per pair the two captures run concurrently on two streams",
                    "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stage_ms.items() if k != "icp_iters"},
+                   "stage_ms_note": "summed over both captures, which overlap in time",
                    "icp_iterations_per_step": stage_ms.get("icp_iters", 0) / args.steps},
         "roofline": {"kernel": "k_sor_dist (SOR k-NN pass, k=51)", "bound": "hbm",
                      "achieved": round(achieved, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",
@@ -248,7 +266,10 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     }
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(pr, sample_pairs=1)
-    ctx.close()
+    pool.shutdown()
+    del src0, tgt0
+    for c in ctxs:
+        c.close()
     return out
 
 

@@ -215,6 +215,17 @@ LCR_API void lcr_icp_params_default(lcr_icp_params* p);
 LCR_API lcr_status lcr_icp(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr_icp_params* p,
                            const float guess[16], lcr_icp_result* res, lcr_cloud** registered);
 
+/* All pairs of a capture cycle at once (the reference runs fine_registration
+ * once per pair, fine_registration.cpp:105-126): pair i aligns src[i] onto
+ * tgt[i] with the shared parameters, from guesses + 16*i (row-major; guesses
+ * may be NULL for identity).  The pairs iterate together over one work queue
+ * (uneven sizes share the GPU) and each stops at its own convergence; each
+ * result equals what lcr_icp gives for that pair alone.  Returns
+ * LCR_ERR_NO_CORRESPONDENCES if some pair had too few (its result says so). */
+LCR_API lcr_status lcr_icp_batch(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* const* tgt,
+                                 size_t npairs, const lcr_icp_params* p, const float* guesses,
+                                 lcr_icp_result* results);
+
 /* One correspondence pass (for parity tests): source transformed by T
  * (row-major FP64, applied in FP32), exact nearest target within the maximum
  * distance; idx -1 when none.  Host outputs of length n_src. */

@@ -34,6 +34,8 @@ CUDA_ERR, TIMEOUT, OOM, IO, TOO_FEW_POINTS, NO_DEVICE = 5, 6, 7, 8, 9, 10
 
 KINECT_V1, KINECT_V2 = 0, 1
 ICP_POINT_TO_POINT, ICP_POINT_TO_PLANE = 0, 1
+(ICP_STATE_NOT_CONVERGED, ICP_STATE_ITERATIONS, ICP_STATE_TRANSFORM, ICP_STATE_ABS_MSE, ICP_STATE_REL_MSE,
+ ICP_STATE_NO_CORRESPONDENCES) = range(6)
 NORMALS_FLIP_ALL = 1
 ACCUM_ALL = 1
 
@@ -101,6 +103,7 @@ _SIGS = {
     "lcr_normals": (C.c_int, [_VP, _VP, C.c_int, _VP, C.c_int, C.POINTER(_VP)]),
     "lcr_icp_params_default": (None, [C.POINTER(IcpParams)]),
     "lcr_icp": (C.c_int, [_VP, _VP, _VP, C.POINTER(IcpParams), _VP, C.POINTER(IcpResult), C.POINTER(_VP)]),
+    "lcr_icp_batch": (C.c_int, [_VP, _VP, _VP, C.c_size_t, C.POINTER(IcpParams), _VP, _VP]),
     "lcr_correspondences": (C.c_int, [_VP, _VP, _VP, _VP, C.c_double, _VP, _VP]),
     "lcr_knn": (C.c_int, [_VP, _VP, _VP, C.c_int, C.c_float, _VP, _VP]),
     "lcr_accumulate": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_int, C.c_double, C.c_int, C.POINTER(_VP),

@@ -230,6 +230,22 @@ class Context:
                          res.iterations, res.state, res.n_correspondences, res.fitness, res.mse, st)
         return (out, Cloud(self, reg)) if want_registered else out
 
+    def icp_batch(self, srcs: list[Cloud], tgts: list[Cloud], params: L.IcpParams,
+                  guesses: np.ndarray | None = None) -> list[IcpOutcome]:
+        """lcr_icp_batch: pair i aligns srcs[i] onto tgts[i]; all pairs iterate together."""
+        n = len(srcs)
+        assert len(tgts) == n
+        res = (L.IcpResult * max(n, 1))()
+        hs = (C.c_void_p * max(n, 1))(*[c.handle for c in srcs])
+        ht = (C.c_void_p * max(n, 1))(*[c.handle for c in tgts])
+        g = None if guesses is None else np.ascontiguousarray(guesses, dtype=np.float32).reshape(n * 16)
+        st = self._check(self.lib.lcr_icp_batch(self.h, hs, ht, n, C.byref(params),
+                                                L.ptr(g) if g is not None else None, res),
+                         allow=(L.NO_CORRESPONDENCES,))
+        return [IcpOutcome(np.array(r.transform, dtype=np.float32).reshape(4, 4),
+                           np.array(r.transform64, dtype=np.float64).reshape(4, 4), bool(r.converged), r.iterations,
+                           r.state, r.n_correspondences, r.fitness, r.mse, st) for r in res[:n]]
+
     def correspondences(self, src: Cloud, tgt: Cloud, T: np.ndarray, max_dist: float):
         n = len(src)
         idx = np.zeros(n, dtype=np.int32)

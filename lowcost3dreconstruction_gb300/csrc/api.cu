@@ -105,8 +105,9 @@ void lcr_ctx_destroy(lcr_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  for (int m = 0; m < 2; ++m)
-    if (ctx->icp_exec[m]) cudaGraphExecDestroy(ctx->icp_exec[m]);
+  for (auto& per_method : ctx->icp_exec)
+    for (cudaGraphExec_t e : per_method)
+      if (e) cudaGraphExecDestroy(e);
   for (auto& t : ctx->kt)
     for (auto& e : t.pending) {
       cudaEventDestroy(e.first);
@@ -347,6 +348,24 @@ lcr_status lcr_icp(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, con
     ctx->last_error = "not enough correspondences found";
     st = LCR_ERR_NO_CORRESPONDENCES;
   }
+  API_END(ctx)
+  return st;
+}
+
+lcr_status lcr_icp_batch(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* const* tgt, size_t npairs,
+                         const lcr_icp_params* p, const float* guesses, lcr_icp_result* results) {
+  lcr_status st = LCR_OK;
+  API_BEGIN(ctx)
+  REQUIRE(p && (npairs == 0 || (src && tgt && results)), "null argument");
+  REQUIRE(npairs < (1u << 20), "too many pairs (%zu)", npairs);
+  REQUIRE(p->method == LCR_ICP_POINT_TO_POINT || p->method == LCR_ICP_POINT_TO_PLANE, "unknown ICP method");
+  icp_batch_run(ctx, src, tgt, static_cast<int>(npairs), p, guesses, results);
+  for (size_t i = 0; i < npairs; ++i)
+    if (results[i].state == LCR_ICP_STATE_NO_CORRESPONDENCES) {
+      ctx->last_error = "not enough correspondences found (pair " + std::to_string(i) + ")";
+      st = LCR_ERR_NO_CORRESPONDENCES;
+      break;
+    }
   API_END(ctx)
   return st;
 }

@@ -1,26 +1,33 @@
-// pcl::IterativeClosestPoint on the GPU (pcl_tools/fine_registration.cpp:105-126).
+// pcl::IterativeClosestPoint on the GPU (pcl_tools/fine_registration.cpp:105-126),
+// for one pair (lcr_icp) or for many pairs at once (lcr_icp_batch).
 //
-// One ICP iteration is five launches, captured once per context as the body of
-// a CUDA-graph WHILE node (LCR_ICP_GRAPH=0 runs them from a host loop):
-//  1. k_icp_search  warps take tiles of 32 Hilbert-sorted source points,
-//                   transform them by the current FP32 transform, find each
-//                   point's exact nearest target within the correspondence
-//                   distance (one shared warp-tile traversal), form the
-//                   per-correspondence terms in FP32 and reduce them across the
-//                   warp with a transposing reduce-scatter (lane l ends with
-//                   term l) into a per-tile row.  Tiles wider than four search
+// All pairs of a call iterate together; a pair that has converged drops out.
+// One round (one ICP iteration of every live pair) is five launches over work
+// queues that span the pairs, so uneven cloud sizes share the GPU:
+//  1. k_icp_search  warps take tiles of 32 Hilbert-sorted source points from the
+//                   concatenated tile list of all pairs, transform them by their
+//                   pair's FP32 transform, find each point's exact nearest target
+//                   within the correspondence distance (one shared warp-tile
+//                   traversal), form the per-correspondence terms in FP32 and
+//                   reduce them across the warp with a transposing reduce-
+//                   scatter into a per-tile row.  Tiles wider than four search
 //                   radii are deferred.
 //  2. k_icp_hard    one warp per point of a deferred tile (per-query pruning).
 //  3. k_icp_wide    the term rows of the deferred tiles.
-//  4. k_icp_reduce  fixed-order FP64 sums of the tile rows.
-//  5. k_icp_solve   one block: FP64 solve (3x3 SVD for point-to-point, 6x6
-//                   LDL^T for point-to-plane), compose, re-orthonormalise, PCL's
-//                   DefaultConvergenceCriteria, and the WHILE condition.
-// Every sum runs in a fixed order, so the result does not depend on scheduling.
+//  4. k_icp_reduce  fixed-order FP64 sums of chunks of 64 tile rows.
+//  5. k_icp_solve   one block per pair: FP64 solve (3x3 SVD for point-to-point,
+//                   6x6 LDL^T for point-to-plane), compose, re-orthonormalise,
+//                   PCL's DefaultConvergenceCriteria; the last block to finish
+//                   sets the loop condition (some pair still live).
+// The rounds run as the body of a CUDA-graph WHILE node captured once per
+// context (LCR_ICP_GRAPH=0 runs them from a host loop).  Every sum runs in a
+// fixed order per pair, so a pair's result does not depend on scheduling or on
+// the other pairs of the batch.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "search.cuh"
 
@@ -28,36 +35,54 @@ namespace {
 
 constexpr int kIcpThreads = 256;
 constexpr int kIcpWarps = kIcpThreads / 32;
-constexpr int kIcpReduceBlocks = 128;
+constexpr int kChunkTiles = 64;  // tile rows per reduction chunk
 
+// Per pair, written by the host (the centroid by the device).
 struct IcpParams {
   IndexView tgt;
-  const float4* src_pts;  // Morton-sorted source (the source index's points)
-  int src_ntiles;
+  const float4* src_pts;  // Hilbert-sorted source (the source index's points)
   const float4* tgt_nrm;  // target normals by original index
+  int src_ntiles;
+  int tile0, chunk0;      // first global tile / chunk of this pair
   float cap;              // FP32 form of max_correspondence_distance^2
-  float c[3];             // fixed centre of the linear algebra: target centroid (float)
+  float c[3];             // centre of the linear algebra: target centroid (float)
   int min_corr;
   int max_iter;
   double teps, feps;
-  int use_graph;
-  float* fd;              // fitness: squared NN distance per sorted source slot
-  float4* far;            // fitness: queries with no target point inside the cap
-  float* tile_part;       // per-tile FP32 term sums [ntiles][32]
-  uint32_t* hard_q;       // deferred query slots (points of wide tiles)
-  float4* hard_tp;        // per-slot result of a deferred query: target xyz, distance
-  uint32_t* hard_ti;      // per-slot target index (0xffffffff: none within the cap)
-  uint32_t* wide_tiles;   // tiles whose terms wait for the deferred queries
 };
 
+// Per pair, device-resident across rounds.
 struct IcpState {
   double T[16];
   Xf Tf;
   double prev_mse, mse, fitness;
   int iter, done, converged, state, ncorr, launches;
-  unsigned int tile_ctr, blocks_done;
-  unsigned int fit_tile_ctr, fit_blocks_done, nfar, far_ctr;
-  unsigned int nhard, hard_ctr, nwide, wide_ctr;
+};
+
+// The call: pair arrays and the scratch of all pairs (global slot = global
+// tile * 32 + lane).
+struct BatchDesc {
+  int npairs, total_tiles, total_chunks, use_graph;
+  IcpParams* prm;
+  IcpState* st;
+  const int* tile0;       // [npairs + 1] prefix of source tiles
+  const int* chunk0;      // [npairs + 1] prefix of reduction chunks
+  float* tile_part;       // [total_tiles][32] FP32 term rows
+  uint32_t* hard_q;       // deferred query global slots
+  float4* hard_tp;        // per global slot: target xyz, distance of a deferred query
+  uint32_t* hard_ti;      // per global slot: its target index (0xffffffff: none)
+  uint32_t* wide_tiles;   // global tiles whose rows wait for the deferred queries
+  double* red;            // [total_chunks][32] FP64 chunk sums
+  float* fd;              // fitness: squared NN distance per global slot (< 0: not a point)
+  float4* far;            // fitness: queries with no target inside the cap (w = global slot)
+};
+
+// Work-queue counters, reset by the last solve block of every round.
+struct BatchCounters {
+  unsigned int tile_ctr, nhard, hard_ctr, nwide, wide_ctr, chunk_ctr;
+  unsigned int ticket, active, rounds, live;
+  unsigned int fit_tile_ctr, nfar, far_ctr;
+  int max_rounds;
 };
 
 // Transposing warp reduction: on entry every lane holds 32 terms; on exit lane l
@@ -320,7 +345,6 @@ __device__ void icp_update(const double* S, const IcpParams* prm, IcpState* st) 
   }
   st->prev_mse = mse;
 }
-
 // Terms of one correspondence (all zero when the source point has none):
 // point-to-point S[0..2] s', S[3..5] t', S[6+3a+b] t'_a s'_b, S[15] count,
 // S[16] distance; point-to-plane S[0..20] upper A^T A, S[21..26] A^T b,
@@ -364,353 +388,463 @@ __device__ __forceinline__ void corr_terms(float (&t)[32], bool found, const flo
   }
 }
 
-__device__ __forceinline__ bool icp_done(const IcpState* st) {
-  return *reinterpret_cast<const volatile int*>(&st->done) != 0;
+// Pair owning global tile g: the last p with tile0[p] <= g.
+__device__ __forceinline__ int pair_of(const int* __restrict__ pre, int npairs, int g) {
+  int lo = 0, hi = npairs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&pre[mid]) <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
 }
 
-// Pass 1 of an iteration.  Warps take tiles of 32 Morton-sorted source points
-// dynamically; a compact tile shares one capped 1-NN traversal and stores its
-// 32 FP32 term sums (lane l = term l) in tile_part[tile].  A tile wider than
-// four search radii (its queries straddle distant surfaces) is deferred: its
-// points go to the hard-query list and the tile to the wide list.
-template <int P2PL>
-__global__ void __launch_bounds__(kIcpThreads) k_icp_search(const IcpParams* __restrict__ prm, IcpState* st) {
-  __shared__ IndexView s_tgt;
-  __shared__ Xf s_T;
-  __shared__ WarpScratch wss[kIcpWarps];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  if (icp_done(st)) return;
-  if (threadIdx.x == 0) {
-    s_tgt = prm->tgt;
-    s_T = st->Tf;
+// Per-warp cache of the pair being worked on: its target index view and
+// FP32 transform in shared memory (reloaded when the warp moves to another pair).
+struct PairCache {
+  IndexView tgt;
+  Xf T;
+  int pair;
+};
+
+__device__ __forceinline__ void cache_pair(PairCache& pc, const BatchDesc* __restrict__ d, int p, int lane) {
+  if (pc.pair == p) return;
+  __syncwarp();
+  if (lane == 0) {
+    pc.tgt = d->prm[p].tgt;
+    pc.T = d->st[p].Tf;
+    pc.pair = p;
   }
-  __syncthreads();
-  const float4* __restrict__ src = prm->src_pts;
-  const int ntiles = prm->src_ntiles;
-  const float cap = prm->cap;
+  __syncwarp();
+}
+
+__device__ __forceinline__ unsigned vload(const unsigned* p) { return *reinterpret_cast<const volatile unsigned*>(p); }
+
+// 1. Tiles of the live pairs: compact ones searched and reduced to a row,
+// wide ones deferred.
+template <int P2PL>
+__global__ void __launch_bounds__(kIcpThreads) k_icp_search(const BatchDesc* __restrict__ d, BatchCounters* cnt) {
+  __shared__ WarpScratch wss[kIcpWarps];
+  __shared__ PairCache pcs[kIcpWarps];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  if (lane == 0) pcs[wib].pair = -1;
+  __syncwarp();
+  const int total = d->total_tiles, npairs = d->npairs;
   for (;;) {
-    int tile = 0;
-    if (lane == 0) tile = static_cast<int>(atomicAdd(&st->tile_ctr, 1u));
-    tile = __shfl_sync(LCR_FULL, tile, 0);
-    if (tile >= ntiles) break;
-    const int slot = tile * 32 + lane;
-    const float4 p = src[slot];
-    const bool pv = finite3(p.x, p.y, p.z);
+    int g = 0;
+    if (lane == 0) g = static_cast<int>(atomicAdd(&cnt->tile_ctr, 1u));
+    g = __shfl_sync(LCR_FULL, g, 0);
+    if (g >= total) break;
+    const int p = pair_of(d->tile0, npairs, g);
+    const IcpParams* __restrict__ prm = d->prm + p;
+    if (d->st[p].done) continue;  // its rows are not read this round
+    cache_pair(pcs[wib], d, p, lane);
+    const int gslot = g * 32 + lane;
+    const float4 pt = prm->src_pts[(g - prm->tile0) * 32 + lane];
+    const bool pv = finite3(pt.x, pt.y, pt.z);
     float3 q = make_float3(0.f, 0.f, 0.f);
-    if (pv) q = xf_apply(s_T, p.x, p.y, p.z);
+    if (pv) q = xf_apply(pcs[wib].T, pt.x, pt.y, pt.z);
     float4 tlo, thi;
     if (!tile_box(q.x, q.y, q.z, pv, tlo, thi)) {
-      prm->tile_part[slot] = 0.f;
+      d->tile_part[gslot] = 0.f;
       continue;
     }
+    const float cap = prm->cap;
     const float dx = thi.x - tlo.x, dy = thi.y - tlo.y, dz = thi.z - tlo.z;
     if (dx * dx + dy * dy + dz * dz > 16.f * cap) {
       const unsigned valid = __ballot_sync(LCR_FULL, pv);
       unsigned base = 0;
       if (lane == 0) {
-        base = atomicAdd(&st->nhard, static_cast<unsigned>(__popc(valid)));
-        prm->wide_tiles[atomicAdd(&st->nwide, 1u)] = static_cast<uint32_t>(tile);
+        base = atomicAdd(&cnt->nhard, static_cast<unsigned>(__popc(valid)));
+        d->wide_tiles[atomicAdd(&cnt->nwide, 1u)] = static_cast<uint32_t>(g);
       }
       base = __shfl_sync(LCR_FULL, base, 0);
-      if (pv) prm->hard_q[base + __popc(valid & ((1u << lane) - 1u))] = static_cast<uint32_t>(slot);
+      if (pv) d->hard_q[base + __popc(valid & ((1u << lane) - 1u))] = static_cast<uint32_t>(gslot);
       continue;
     }
     NN1 v;
     v.init(q.x, q.y, q.z, pv, cap, wss[wib]);
-    tile_traverse(s_tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), wss[wib]);
+    tile_traverse(pcs[wib].tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), wss[wib]);
     float t[32];
     corr_terms<P2PL>(t, pv && v.found(), q, v.bp, key_dist(v.best), key_idx(v.best), prm);
-    prm->tile_part[slot] = reduce_scatter32(t, lane);
+    d->tile_part[gslot] = reduce_scatter32(t, lane);
   }
 }
 
-// Pass 2: the deferred queries, one per warp (exact per-query pruning), spread
-// over the whole grid; results land in per-point slots.
-__global__ void __launch_bounds__(kIcpThreads) k_icp_hard(const IcpParams* __restrict__ prm, IcpState* st) {
-  __shared__ IndexView s_tgt;
-  __shared__ Xf s_T;
+// 2. The deferred queries, one per warp (exact per-query pruning); results
+// land in per-slot arrays.
+__global__ void __launch_bounds__(kIcpThreads) k_icp_hard(const BatchDesc* __restrict__ d, BatchCounters* cnt) {
   __shared__ WarpScratch wss[kIcpWarps];
+  __shared__ PairCache pcs[kIcpWarps];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  if (icp_done(st)) return;
-  if (threadIdx.x == 0) {
-    s_tgt = prm->tgt;
-    s_T = st->Tf;
-  }
-  __syncthreads();
-  const unsigned nhard = *reinterpret_cast<volatile unsigned*>(&st->nhard);
+  if (lane == 0) pcs[wib].pair = -1;
+  __syncwarp();
+  const unsigned nhard = vload(&cnt->nhard);
   for (;;) {
     unsigned i = 0;
-    if (lane == 0) i = atomicAdd(&st->hard_ctr, 1u);
+    if (lane == 0) i = atomicAdd(&cnt->hard_ctr, 1u);
     i = __shfl_sync(LCR_FULL, i, 0);
     if (i >= nhard) break;
-    const uint32_t slot = prm->hard_q[i];
-    const float4 p = prm->src_pts[slot];
-    const float3 q = xf_apply(s_T, p.x, p.y, p.z);
+    const uint32_t gslot = d->hard_q[i];
+    const int g = static_cast<int>(gslot >> 5);
+    const int p = pair_of(d->tile0, d->npairs, g);
+    const IcpParams* __restrict__ prm = d->prm + p;
+    cache_pair(pcs[wib], d, p, lane);
+    const float4 pt = prm->src_pts[(g - prm->tile0) * 32 + (gslot & 31u)];
+    const float3 q = xf_apply(pcs[wib].T, pt.x, pt.y, pt.z);
     unsigned long long best;
     float4 bp;
-    warp_query_nn(s_tgt, q.x, q.y, q.z, prm->cap, wss[wib], best, bp);
+    warp_query_nn(pcs[wib].tgt, q.x, q.y, q.z, prm->cap, wss[wib], best, bp);
     if (lane == 0) {
-      prm->hard_tp[slot] = make_float4(bp.x, bp.y, bp.z, key_dist(best));
-      prm->hard_ti[slot] = key_idx(best);
+      d->hard_tp[gslot] = make_float4(bp.x, bp.y, bp.z, key_dist(best));
+      d->hard_ti[gslot] = key_idx(best);
     }
   }
 }
 
-// Pass 3: term sums of the wide tiles from the per-point results.
+// 3. Rows of the deferred tiles from the per-slot results.
 template <int P2PL>
-__global__ void __launch_bounds__(kIcpThreads) k_icp_wide(const IcpParams* __restrict__ prm, IcpState* st) {
-  __shared__ Xf s_T;
+__global__ void __launch_bounds__(kIcpThreads) k_icp_wide(const BatchDesc* __restrict__ d, BatchCounters* cnt) {
   const int lane = threadIdx.x & 31;
-  if (icp_done(st)) return;
-  if (threadIdx.x == 0) s_T = st->Tf;
-  __syncthreads();
-  const unsigned nwide = *reinterpret_cast<volatile unsigned*>(&st->nwide);
+  const unsigned nwide = vload(&cnt->nwide);
   for (;;) {
     unsigned i = 0;
-    if (lane == 0) i = atomicAdd(&st->wide_ctr, 1u);
+    if (lane == 0) i = atomicAdd(&cnt->wide_ctr, 1u);
     i = __shfl_sync(LCR_FULL, i, 0);
     if (i >= nwide) break;
-    const int slot = static_cast<int>(prm->wide_tiles[i]) * 32 + lane;
-    const float4 p = prm->src_pts[slot];
-    const bool pv = finite3(p.x, p.y, p.z);
+    const int g = static_cast<int>(d->wide_tiles[i]);
+    const int p = pair_of(d->tile0, d->npairs, g);
+    const IcpParams* __restrict__ prm = d->prm + p;
+    const int gslot = g * 32 + lane;
+    const float4 pt = prm->src_pts[(g - prm->tile0) * 32 + lane];
+    const bool pv = finite3(pt.x, pt.y, pt.z);
     float3 q = make_float3(0.f, 0.f, 0.f);
     float4 tp = make_float4(0.f, 0.f, 0.f, 0.f);
     uint32_t ti = 0xffffffffu;
     if (pv) {
-      q = xf_apply(s_T, p.x, p.y, p.z);
-      tp = prm->hard_tp[slot];
-      ti = prm->hard_ti[slot];
+      q = xf_apply(d->st[p].Tf, pt.x, pt.y, pt.z);
+      tp = d->hard_tp[gslot];
+      ti = d->hard_ti[gslot];
     }
     float t[32];
     corr_terms<P2PL>(t, pv && ti != 0xffffffffu, q, tp, tp.w, ti, prm);
-    prm->tile_part[slot] = reduce_scatter32(t, lane);
+    d->tile_part[gslot] = reduce_scatter32(t, lane);
   }
 }
 
-// Pass 4: fixed-order FP64 reduction of the per-tile sums: block b owns a
-// contiguous range of tiles, 8 sub-slices x 32 terms per block.
-__global__ void __launch_bounds__(256) k_icp_reduce(const IcpParams* __restrict__ prm, const IcpState* st,
-                                                   double* __restrict__ red) {
-  __shared__ double s[8][32];
-  if (icp_done(st)) return;
-  const int ntiles = prm->src_ntiles;
-  const int chunk = (ntiles + gridDim.x - 1) / gridDim.x;
-  const int t0 = blockIdx.x * chunk, t1 = min(ntiles, t0 + chunk);
+// 4. Fixed-order FP64 sums: chunk c of pair p covers its tiles
+// [64 (c - chunk0[p]), +64); within a chunk warp w adds tiles w, w+8, ...
+__global__ void __launch_bounds__(kIcpThreads) k_icp_reduce(const BatchDesc* __restrict__ d, BatchCounters* cnt) {
+  __shared__ double s[kIcpWarps][32];
   const int term = threadIdx.x & 31, sub = threadIdx.x >> 5;
-  double acc = 0.0;
-  for (int t = t0 + sub; t < t1; t += 8) acc += static_cast<double>(prm->tile_part[t * 32 + term]);
-  s[sub][term] = acc;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double v = 0.0;
+  for (int c = blockIdx.x; c < d->total_chunks; c += gridDim.x) {
+    const int p = pair_of(d->chunk0, d->npairs, c);
+    if (d->st[p].done) continue;
+    const IcpParams* __restrict__ prm = d->prm + p;
+    const int t0 = prm->tile0 + (c - prm->chunk0) * kChunkTiles;
+    const int t1 = min(prm->tile0 + prm->src_ntiles, t0 + kChunkTiles);
+    double acc = 0.0;
+    for (int t = t0 + sub; t < t1; t += kIcpWarps) acc += static_cast<double>(d->tile_part[t * 32 + term]);
+    s[sub][term] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double v = 0.0;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) v += s[k][threadIdx.x];
-    red[blockIdx.x * 32 + threadIdx.x] = v;
+      for (int k = 0; k < kIcpWarps; ++k) v += s[k][threadIdx.x];
+      d->red[static_cast<size_t>(c) * 32 + threadIdx.x] = v;
+    }
+    __syncthreads();
   }
 }
 
-// Pass 5, one block: sum of the block partials in order, FP64 solve, compose,
-// convergence test, counters reset, and the loop condition for the graph.
+// 5. One block per live pair (blocks stride over the pairs): its chunk sums in
+// order, the FP64 update; the last block to finish decides whether another
+// round runs and resets the queues.
 template <int P2PL>
-__global__ void __launch_bounds__(kIcpThreads) k_icp_solve(const IcpParams* __restrict__ prm, IcpState* st,
-                                                           const double* __restrict__ red, int nred,
+__global__ void __launch_bounds__(kIcpThreads) k_icp_solve(const BatchDesc* __restrict__ d, BatchCounters* cnt,
                                                            cudaGraphConditionalHandle h) {
-  __shared__ double s_acc[kIcpWarps][32];
-  if (icp_done(st)) {
-    if (threadIdx.x == 0 && prm->use_graph) cudaGraphSetConditional(h, 0u);
-    return;
-  }
-  const int term = threadIdx.x & 31, slice = threadIdx.x >> 5;
-  double s = 0.0;
-  for (int b = slice; b < nred; b += kIcpWarps) s += red[static_cast<size_t>(b) * 32 + term];
-  s_acc[slice][term] = s;
+  __shared__ double S[32];
+  __shared__ double s_sl[kIcpWarps][32];
+  __shared__ unsigned s_live;
+  if (threadIdx.x == 0) s_live = 0;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double S[32];
-    for (int t = 0; t < 32; ++t) {
+  for (int p = blockIdx.x; p < d->npairs; p += gridDim.x) {
+    IcpState* st = d->st + p;
+    if (st->done) continue;
+    const IcpParams* __restrict__ prm = d->prm + p;
+    {
+      // chunk sums in a fixed order: slice k adds chunks k, k+8, ...; then the 8 slices
+      const int term = threadIdx.x & 31, slice = threadIdx.x >> 5;
+      const int c0 = prm->chunk0, c1 = d->chunk0[p + 1];
       double v = 0.0;
-      for (int w = 0; w < kIcpWarps; ++w) v += s_acc[w][t];
-      S[t] = v;
+      for (int c = c0 + slice; c < c1; c += kIcpWarps) v += d->red[static_cast<size_t>(c) * 32 + term];
+      s_sl[slice][term] = v;
+      __syncthreads();
+      if (threadIdx.x < 32) {
+        double w = 0.0;
+#pragma unroll
+        for (int k = 0; k < kIcpWarps; ++k) w += s_sl[k][threadIdx.x];
+        S[threadIdx.x] = w;
+      }
+      __syncthreads();
     }
-    icp_update<P2PL>(S, prm, st);
-    st->launches += 1;
-    if (st->launches > prm->max_iter + 1) st->done = 1;  // hard bound on the device loop
-    st->tile_ctr = 0;
-    st->nhard = 0;
-    st->hard_ctr = 0;
-    st->nwide = 0;
-    st->wide_ctr = 0;
-    if (prm->use_graph) cudaGraphSetConditional(h, st->done ? 0u : 1u);
+    if (threadIdx.x == 0) {
+      icp_update<P2PL>(S, prm, st);
+      st->launches += 1;
+      if (st->launches > prm->max_iter + 1) st->done = 1;  // hard bound on the device loop
+      if (!st->done) ++s_live;
+    }
+    __syncthreads();
   }
+  if (threadIdx.x != 0) return;
+  if (s_live) atomicAdd(&cnt->active, s_live);
+  __threadfence();
+  const unsigned ticket = atomicAdd(&cnt->ticket, 1u);
+  if (ticket != gridDim.x - 1) return;
+  __threadfence();
+  const unsigned live = vload(&cnt->active);
+  const unsigned rounds = cnt->rounds + 1;
+  cnt->rounds = rounds;
+  cnt->live = live;
+  cnt->tile_ctr = 0;
+  cnt->nhard = 0;
+  cnt->hard_ctr = 0;
+  cnt->nwide = 0;
+  cnt->wide_ctr = 0;
+  cnt->active = 0;
+  cnt->ticket = 0;
+  if (d->use_graph) cudaGraphSetConditional(h, (live > 0 && static_cast<int>(rounds) < cnt->max_rounds) ? 1u : 0u);
 }
 
 // getFitnessScore(): mean squared distance from every transformed source point
-// to its exact (uncapped) nearest target point.  Phase 1 searches the tiles with
-// the correspondence cap (a far lane would otherwise widen its whole tile's
-// search); lanes with no target point inside the cap are queued and phase 2
-// finds their nearest point with one warp per query (per-query pruning, the 32
-// lanes scan a leaf together).  Distances land in fd[] by sorted source
-// position and are summed in a fixed order.  The points of a tile wider than
-// four search radii go straight to phase 2.
-__global__ void __launch_bounds__(kIcpThreads) k_fitness(const IcpParams* __restrict__ prm, IcpState* st) {
-  __shared__ IndexView s_tgt;
-  __shared__ Xf s_T;
+// to its exact (uncapped) nearest target point.  Phase 1 searches the tiles
+// with the correspondence cap (a far lane would otherwise widen its whole
+// tile's search); lanes with no target inside the cap, and all points of a
+// tile wider than four search radii, are queued, and phase 2 finds their
+// nearest point with one warp per query.  Distances land in fd[] by global
+// slot and are summed per pair in a fixed order.
+__global__ void __launch_bounds__(kIcpThreads) k_fitness(const BatchDesc* __restrict__ d, BatchCounters* cnt) {
   __shared__ WarpScratch wss[kIcpWarps];
+  __shared__ PairCache pcs[kIcpWarps];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  if (threadIdx.x == 0) {
-    s_tgt = prm->tgt;
-    s_T = st->Tf;
-  }
-  __syncthreads();
-  const float4* __restrict__ src = prm->src_pts;
-  const int ntiles = prm->src_ntiles;
-  float* __restrict__ fd = prm->fd;
+  if (lane == 0) pcs[wib].pair = -1;
+  __syncwarp();
+  float* __restrict__ fd = d->fd;
   for (;;) {
-    int tile = 0;
-    if (lane == 0) tile = static_cast<int>(atomicAdd(&st->fit_tile_ctr, 1u));
-    tile = __shfl_sync(LCR_FULL, tile, 0);
-    if (tile >= ntiles) break;
-    const int pos = tile * 32 + lane;
-    const float4 p = src[pos];
-    const bool pv = finite3(p.x, p.y, p.z);
+    int g = 0;
+    if (lane == 0) g = static_cast<int>(atomicAdd(&cnt->fit_tile_ctr, 1u));
+    g = __shfl_sync(LCR_FULL, g, 0);
+    if (g >= d->total_tiles) break;
+    const int p = pair_of(d->tile0, d->npairs, g);
+    const IcpParams* __restrict__ prm = d->prm + p;
+    cache_pair(pcs[wib], d, p, lane);
+    const int gslot = g * 32 + lane;
+    const float4 pt = prm->src_pts[(g - prm->tile0) * 32 + lane];
+    const bool pv = finite3(pt.x, pt.y, pt.z);
     float3 q = make_float3(0.f, 0.f, 0.f);
-    if (pv) q = xf_apply(s_T, p.x, p.y, p.z);
+    if (pv) q = xf_apply(pcs[wib].T, pt.x, pt.y, pt.z);
     float4 tlo, thi;
     if (!tile_box(q.x, q.y, q.z, pv, tlo, thi)) {
-      fd[pos] = -1.f;
+      fd[gslot] = -1.f;
       continue;
     }
     const float dx = thi.x - tlo.x, dy = thi.y - tlo.y, dz = thi.z - tlo.z;
-    if (dx * dx + dy * dy + dz * dz > 16.f * prm->cap) {
-      // wide tile: every point goes to the per-query phase (same exact result)
-      if (pv) prm->far[atomicAdd(&st->nfar, 1u)] = make_float4(q.x, q.y, q.z, __int_as_float(pos));
-      else fd[pos] = -1.f;
-      continue;
+    bool found = false;
+    float dist = 0.f;
+    if (!(dx * dx + dy * dy + dz * dz > 16.f * prm->cap)) {
+      NN1 v;
+      v.init(q.x, q.y, q.z, pv, prm->cap, wss[wib]);
+      tile_traverse(pcs[wib].tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z),
+                    wss[wib]);
+      found = v.found();
+      dist = key_dist(v.best);
     }
-    NN1 v;
-    v.init(q.x, q.y, q.z, pv, prm->cap, wss[wib]);
-    tile_traverse(s_tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), wss[wib]);
     if (!pv) {
-      fd[pos] = -1.f;  // not a point
-    } else if (v.found()) {
-      fd[pos] = key_dist(v.best);
-    } else {
-      const unsigned slot = atomicAdd(&st->nfar, 1u);
-      prm->far[slot] = make_float4(q.x, q.y, q.z, __int_as_float(pos));
+      fd[gslot] = -1.f;  // not a point
+    } else if (found) {
+      fd[gslot] = dist;
     }
+    // queue the rest, one reservation per warp
+    const bool far = pv && !found;
+    const unsigned m = __ballot_sync(LCR_FULL, far);
+    unsigned base = 0;
+    if (lane == 0 && m) base = atomicAdd(&cnt->nfar, static_cast<unsigned>(__popc(m)));
+    base = __shfl_sync(LCR_FULL, base, 0);
+    if (far) d->far[base + __popc(m & ((1u << lane) - 1u))] = make_float4(q.x, q.y, q.z, __int_as_float(gslot));
   }
 }
 
-__global__ void __launch_bounds__(kIcpThreads) k_fitness_far(const IcpParams* __restrict__ prm, IcpState* st) {
-  __shared__ IndexView s_tgt;
+__global__ void __launch_bounds__(kIcpThreads) k_fitness_far(const BatchDesc* __restrict__ d, BatchCounters* cnt) {
   __shared__ WarpScratch wss[kIcpWarps];
+  __shared__ PairCache pcs[kIcpWarps];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  if (threadIdx.x == 0) s_tgt = prm->tgt;
-  __syncthreads();
-  const unsigned nfar = *reinterpret_cast<volatile unsigned*>(&st->nfar);
+  if (lane == 0) pcs[wib].pair = -1;
+  __syncwarp();
+  const unsigned nfar = vload(&cnt->nfar);
   for (;;) {
     unsigned i = 0;
-    if (lane == 0) i = atomicAdd(&st->far_ctr, 1u);
+    if (lane == 0) i = atomicAdd(&cnt->far_ctr, 1u);
     i = __shfl_sync(LCR_FULL, i, 0);
     if (i >= nfar) break;
-    const float4 q = prm->far[i];
+    const float4 q = d->far[i];
+    const int gslot = __float_as_int(q.w);
+    const int p = pair_of(d->tile0, d->npairs, gslot >> 5);
+    cache_pair(pcs[wib], d, p, lane);
     unsigned long long best;
     float4 bp;
-    warp_query_nn(s_tgt, q.x, q.y, q.z, LCR_INF, wss[wib], best, bp);
-    if (lane == 0) prm->fd[__float_as_int(q.w)] = key_dist(best);
+    warp_query_nn(pcs[wib].tgt, q.x, q.y, q.z, LCR_INF, wss[wib], best, bp);
+    if (lane == 0) d->fd[gslot] = key_dist(best);
   }
 }
 
-// Fixed-order FP64 sum of fd[] (negative entries are not points): contiguous
-// chunks per block, fixed tree inside the block, blocks added in order by the
-// last block.
-__global__ void __launch_bounds__(256) k_fitness_reduce(const IcpParams* __restrict__ prm, IcpState* st,
-                                                        double* __restrict__ part) {
-  __shared__ double s_s[8], s_c[8];
-  __shared__ int s_flag;
-  const int n = prm->src_ntiles * 32;
-  const int chunk = (n + gridDim.x - 1) / gridDim.x;
-  const int b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
-  double s = 0.0, c = 0.0;
-  for (int i = b0 + static_cast<int>(threadIdx.x); i < b1; i += blockDim.x) {
-    const float d = prm->fd[i];
-    if (d >= 0.f) {
-      s += d;
-      c += 1.0;
+// Per reduction chunk (64 tiles of one pair): sum and count of the valid
+// distances, threads striding the chunk's slots, then a fixed tree; the chunk
+// pairs (sum, count) land in red[] (reused: the rounds are over).
+__global__ void __launch_bounds__(kIcpThreads) k_fitness_chunks(const BatchDesc* __restrict__ d) {
+  __shared__ double s_s[kIcpWarps], s_c[kIcpWarps];
+  for (int c = blockIdx.x; c < d->total_chunks; c += gridDim.x) {
+    const int p = pair_of(d->chunk0, d->npairs, c);
+    const IcpParams* __restrict__ prm = d->prm + p;
+    const int t0 = prm->tile0 + (c - prm->chunk0) * kChunkTiles;
+    const int t1 = min(prm->tile0 + prm->src_ntiles, t0 + kChunkTiles);
+    double s = 0.0, n = 0.0;
+    for (int i = t0 * 32 + static_cast<int>(threadIdx.x); i < t1 * 32; i += blockDim.x) {
+      const float v = d->fd[i];
+      if (v >= 0.f) {
+        s += v;
+        n += 1.0;
+      }
     }
-  }
-  s = warp_sum(s);
-  c = warp_sum(c);
-  if ((threadIdx.x & 31) == 0) {
-    s_s[threadIdx.x >> 5] = s;
-    s_c[threadIdx.x >> 5] = c;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double ts = 0.0, tc = 0.0;
-    for (int w = 0; w < 8; ++w) {
-      ts += s_s[w];
-      tc += s_c[w];
+    s = warp_sum(s);
+    n = warp_sum(n);
+    if ((threadIdx.x & 31) == 0) {
+      s_s[threadIdx.x >> 5] = s;
+      s_c[threadIdx.x >> 5] = n;
     }
-    part[2 * blockIdx.x] = ts;
-    part[2 * blockIdx.x + 1] = tc;
-    __threadfence();
-    s_flag = (atomicAdd(&st->fit_blocks_done, 1u) == gridDim.x - 1) ? 1 : 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double ts = 0.0, tc = 0.0;
+      for (int w = 0; w < kIcpWarps; ++w) {
+        ts += s_s[w];
+        tc += s_c[w];
+      }
+      d->red[2 * static_cast<size_t>(c)] = ts;
+      d->red[2 * static_cast<size_t>(c) + 1] = tc;
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  if (!s_flag || threadIdx.x != 0) return;
-  __threadfence();
-  double ts = 0.0, tc = 0.0;
-  for (int b = 0; b < static_cast<int>(gridDim.x); ++b) {
-    ts += __ldcg(&part[2 * b]);
-    tc += __ldcg(&part[2 * b + 1]);
-  }
-  st->fitness = tc > 0 ? ts / tc : DBL_MAX;
-  st->fit_tile_ctr = 0;
-  st->fit_blocks_done = 0;
-  st->nfar = 0;
-  st->far_ctr = 0;
 }
 
-struct IcpBuffers {
-  IcpParams* prm;
-  IcpState* st;
-  double* part;
-};
-
-IcpBuffers icp_buffers(lcr_ctx* ctx, int grid) {
-  const size_t need = 1024 + 1024 + static_cast<size_t>(grid) * 32 * sizeof(double);
-  if (ctx->icp_bytes < need) {
-    if (ctx->icp_block) {
-      sync(ctx);
-      CUDA_TRY(cudaFree(ctx->icp_block));
-      for (int m = 0; m < 2; ++m)
-        if (ctx->icp_exec[m]) {
-          cudaGraphExecDestroy(ctx->icp_exec[m]);
-          ctx->icp_exec[m] = nullptr;
-        }
+// One warp per pair: its chunks in order (lane l adds chunks l, l+32, ...),
+// then the fixed shuffle tree.
+__global__ void __launch_bounds__(kIcpThreads) k_fitness_reduce(const BatchDesc* __restrict__ d, BatchCounters* cnt) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int p = warp; p < d->npairs; p += nwarps) {
+    double s = 0.0, n = 0.0;
+    for (int c = d->prm[p].chunk0 + lane; c < d->chunk0[p + 1]; c += 32) {
+      s += d->red[2 * static_cast<size_t>(c)];
+      n += d->red[2 * static_cast<size_t>(c) + 1];
     }
-    CUDA_TRY(cudaMalloc(&ctx->icp_block, need));
-    CUDA_TRY(cudaMemsetAsync(ctx->icp_block, 0, need, ctx->stream));
-    ctx->icp_bytes = need;
+    s = warp_sum(s);
+    n = warp_sum(n);
+    if (lane == 0) d->st[p].fitness = n > 0 ? s / n : DBL_MAX;
   }
-  char* b = static_cast<char*>(ctx->icp_block);
-  static_assert(sizeof(IcpParams) <= 1024 && sizeof(IcpState) <= 1024, "ICP structs must fit their slots");
-  return IcpBuffers{reinterpret_cast<IcpParams*>(b), reinterpret_cast<IcpState*>(b + 1024),
-                    reinterpret_cast<double*>(b + 2048)};
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cnt->fit_tile_ctr = 0;
+    cnt->nfar = 0;
+    cnt->far_ctr = 0;
+  }
+}
+
+// Target centroids of every pair (the centre of the linear algebra), FP64:
+// chunks of 2048 target points give partial (x, y, z, count) sums (threads
+// stride the chunk, fixed tree), then one warp per pair adds its chunks in
+// order and writes the mean as float into prm.
+constexpr int kCentroidChunk = 2048;
+
+__global__ void __launch_bounds__(kIcpThreads) k_centroid_chunks(const float4* const* __restrict__ xyz,
+                                                                 const int* __restrict__ npts,
+                                                                 const int* __restrict__ cc0, int npairs,
+                                                                 double* __restrict__ part) {
+  __shared__ double s[4][kIcpWarps];
+  for (int c = blockIdx.x; c < cc0[npairs]; c += gridDim.x) {
+    const int p = pair_of(cc0, npairs, c);
+    const float4* __restrict__ x = xyz[p];
+    const int i0 = (c - cc0[p]) * kCentroidChunk, i1 = min(npts[p], i0 + kCentroidChunk);
+    double a = 0, b = 0, z = 0, w = 0;
+    for (int i = i0 + static_cast<int>(threadIdx.x); i < i1; i += blockDim.x) {
+      const float4 v = x[i];
+      if (!finite3(v.x, v.y, v.z)) continue;
+      a += v.x; b += v.y; z += v.z; w += 1.0;
+    }
+    a = warp_sum(a); b = warp_sum(b); z = warp_sum(z); w = warp_sum(w);
+    if ((threadIdx.x & 31) == 0) {
+      s[0][threadIdx.x >> 5] = a; s[1][threadIdx.x >> 5] = b;
+      s[2][threadIdx.x >> 5] = z; s[3][threadIdx.x >> 5] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+      double v = 0.0;
+      for (int k = 0; k < kIcpWarps; ++k) v += s[threadIdx.x][k];
+      part[4 * static_cast<size_t>(c) + threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kIcpThreads) k_centroid_final(const BatchDesc* __restrict__ d,
+                                                                const int* __restrict__ cc0,
+                                                                const double* __restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int p = warp; p < d->npairs; p += nwarps) {
+    double v[4] = {0, 0, 0, 0};
+    for (int c = cc0[p] + lane; c < cc0[p + 1]; c += 32)
+      for (int k = 0; k < 4; ++k) v[k] += part[4 * static_cast<size_t>(c) + k];
+    for (int k = 0; k < 4; ++k) v[k] = warp_sum(v[k]);
+    if (lane < 3) {
+      const double m = v[3] > 0 ? v[lane] / v[3] : 0.0;
+      d->prm[p].c[lane] = static_cast<float>(m);
+    }
+  }
 }
 
 int icp_grid(lcr_ctx* ctx) { return ctx->sms * 4; }
+int reduce_grid(lcr_ctx* ctx) { return ctx->sms * 2; }
 
-// Builds (once per context and method) the graph WHILE(cond) { iteration }.
-// Returns nullptr if conditional nodes are unavailable.
-cudaGraphExec_t icp_graph(lcr_ctx* ctx, int p2pl, const IcpBuffers& B) {
-  // LCR_ICP_GRAPH=0 runs the same iteration kernels from a host loop instead
-  // (profilers do not see kernels inside conditional graph bodies).
+// Persistent per-context block: the descriptor, then the counters.
+struct IcpBuffers {
+  BatchDesc* desc;
+  BatchCounters* cnt;
+};
+
+IcpBuffers icp_buffers(lcr_ctx* ctx) {
+  static_assert(sizeof(BatchDesc) <= 512 && sizeof(BatchCounters) <= 512, "ICP structs must fit their slots");
+  if (!ctx->icp_block) {
+    CUDA_TRY(cudaMalloc(&ctx->icp_block, 1024));
+    CUDA_TRY(cudaMemsetAsync(ctx->icp_block, 0, 1024, ctx->stream));
+    ctx->icp_bytes = 1024;
+  }
+  char* b = static_cast<char*>(ctx->icp_block);
+  return IcpBuffers{reinterpret_cast<BatchDesc*>(b), reinterpret_cast<BatchCounters*>(b + 512)};
+}
+
+// Solve blocks of a round: one per pair, up to 1024 (more pairs loop).
+int solve_blocks(int npairs) { return npairs <= 1 ? 1 : (npairs <= 64 ? 64 : 1024); }
+int solve_slot(int blocks) { return blocks == 1 ? 0 : (blocks == 64 ? 1 : 2); }
+
+// Builds (once per context, method and solve width) the graph
+// WHILE(cond) { search; hard; wide; reduce; solve }.  Returns nullptr if
+// conditional nodes are unavailable.
+cudaGraphExec_t icp_graph(lcr_ctx* ctx, int p2pl, int sblocks, const IcpBuffers& B) {
+  // LCR_ICP_GRAPH=0 runs the same kernels from a host loop instead (profilers
+  // do not see kernels inside conditional graph bodies).
   const char* env = std::getenv("LCR_ICP_GRAPH");
   if (env && env[0] == '0') return nullptr;
   if (ctx->icp_graph_ok == 0) return nullptr;
-  if (ctx->icp_exec[p2pl]) return ctx->icp_exec[p2pl];
+  cudaGraphExec_t& slot = ctx->icp_exec[p2pl][solve_slot(sblocks)];
+  if (slot) return slot;
   cudaGraph_t g = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
@@ -729,23 +863,18 @@ cudaGraphExec_t icp_graph(lcr_ctx* ctx, int p2pl, const IcpBuffers& B) {
     ok = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
   }
   if (ok) {
-    // body: search, deferred queries, wide-tile terms, fixed-order reduction,
-    // then the one-block FP64 solve that sets the loop condition.
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    const IcpParams* a0 = B.prm;
-    IcpState* a1 = B.st;
-    double* a2 = B.part;
-    int a3 = kIcpReduceBlocks;
+    const BatchDesc* a0 = B.desc;
+    BatchCounters* a1 = B.cnt;
     void* args2[] = {&a0, &a1};
-    void* args_red[] = {&a0, &a1, &a2};
-    void* args_solve[] = {&a0, &a1, &a2, &a3, &h};
+    void* args3[] = {&a0, &a1, &h};
     struct NodeSpec { void* fn; int grid; void** args; };
     const NodeSpec specs[5] = {
         {p2pl ? reinterpret_cast<void*>(k_icp_search<1>) : reinterpret_cast<void*>(k_icp_search<0>), icp_grid(ctx), args2},
         {reinterpret_cast<void*>(k_icp_hard), icp_grid(ctx), args2},
         {p2pl ? reinterpret_cast<void*>(k_icp_wide<1>) : reinterpret_cast<void*>(k_icp_wide<0>), icp_grid(ctx), args2},
-        {reinterpret_cast<void*>(k_icp_reduce), kIcpReduceBlocks, args_red},
-        {p2pl ? reinterpret_cast<void*>(k_icp_solve<1>) : reinterpret_cast<void*>(k_icp_solve<0>), 1, args_solve}};
+        {reinterpret_cast<void*>(k_icp_reduce), reduce_grid(ctx), args2},
+        {p2pl ? reinterpret_cast<void*>(k_icp_solve<1>) : reinterpret_cast<void*>(k_icp_solve<0>), sblocks, args3}};
     cudaGraphNode_t prev = nullptr;
     for (int k = 0; k < 5 && ok; ++k) {
       cudaKernelNodeParams kp;
@@ -768,102 +897,185 @@ cudaGraphExec_t icp_graph(lcr_ctx* ctx, int p2pl, const IcpBuffers& B) {
     return nullptr;
   }
   ctx->icp_graph_ok = 1;
-  ctx->icp_exec[p2pl] = exec;
+  slot = exec;
   return exec;
 }
+
+inline size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
 }  // namespace
 
 float float_cap(double v);
 
-void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr_icp_params* p, const float* guess,
-             lcr_icp_result* res) {
+void icp_batch_run(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* const* tgt, int npairs,
+                   const lcr_icp_params* p, const float* guesses, lcr_icp_result* res) {
   if (p->max_iterations <= 0) LCR_THROW(LCR_ERR_INVALID_ARG, "max_iterations needs to be greater than zero");
   if (!(p->max_correspondence_distance >= 0)) LCR_THROW(LCR_ERR_INVALID_ARG, "negative correspondence distance");
-  if (src->n == 0 || tgt->n == 0) LCR_THROW(LCR_ERR_EMPTY, "ICP needs non-empty source and target clouds");
+  if (npairs <= 0) return;
+  for (int i = 0; i < npairs; ++i)
+    if (!src[i] || !tgt[i]) LCR_THROW(LCR_ERR_INVALID_ARG, "null cloud in pair %d", i);
+  for (int i = 0; i < npairs; ++i)
+    if (src[i]->n == 0 || tgt[i]->n == 0) LCR_THROW(LCR_ERR_EMPTY, "ICP needs non-empty source and target clouds (pair %d)", i);
   const int p2pl = p->method == LCR_ICP_POINT_TO_PLANE ? 1 : 0;
-  const Index& si = cloud_index(ctx, src);
-  const Index& ti = cloud_index(ctx, tgt);
-  const int grid = icp_grid(ctx);
-  IcpBuffers B = icp_buffers(ctx, grid);
+  const IcpBuffers B = icp_buffers(ctx);
+  const int sblocks = solve_blocks(npairs);
+  cudaGraphExec_t exec = icp_graph(ctx, p2pl, sblocks, B);
 
-  cudaGraphExec_t exec = icp_graph(ctx, p2pl, B);
-  char* stage = static_cast<char*>(pinned(ctx, 2048));
-  IcpParams* hp = reinterpret_cast<IcpParams*>(stage);
-  IcpState* hs = reinterpret_cast<IcpState*>(stage + 1024);
-  std::memset(stage, 0, 2048);
-  hp->tgt = ti.v;
-  hp->src_pts = si.v.pts;
-  hp->src_ntiles = si.v.nleaf;
-  hp->tgt_nrm = tgt->nrm;
-  hp->cap = float_cap(p->max_correspondence_distance * p->max_correspondence_distance);
-  hp->min_corr = 3;
-  hp->max_iter = p->max_iterations;
-  hp->teps = p->transformation_epsilon;
-  hp->feps = p->euclidean_fitness_epsilon;
-  hp->use_graph = exec ? 1 : 0;
-  const size_t nslots = static_cast<size_t>(si.v.nleaf) * 32;
-  // per-call scratch: fitness slots + far list, tile sums, deferred queries
-  const size_t b_fd = nslots * 4, b_far = nslots * 16, b_part = nslots * 4, b_hq = nslots * 4, b_htp = nslots * 16,
-               b_hti = nslots * 4, b_wide = static_cast<size_t>(si.v.nleaf) * 4;
-  char* callbuf = static_cast<char*>(dev_alloc(ctx, b_fd + b_far + b_part + b_hq + b_htp + b_hti + b_wide + 256));
-  char* cur = callbuf;
-  hp->far = reinterpret_cast<float4*>(cur); cur += b_far;
-  hp->hard_tp = reinterpret_cast<float4*>(cur); cur += b_htp;
-  hp->fd = reinterpret_cast<float*>(cur); cur += b_fd;
-  hp->tile_part = reinterpret_cast<float*>(cur); cur += b_part;
-  hp->hard_q = reinterpret_cast<uint32_t*>(cur); cur += b_hq;
-  hp->hard_ti = reinterpret_cast<uint32_t*>(cur); cur += b_hti;
-  hp->wide_tiles = reinterpret_cast<uint32_t*>(cur);
-  const double I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
-  for (int i = 0; i < 16; ++i) hs->T[i] = guess ? static_cast<double>(guess[i]) : I[i];
-  for (int i = 0; i < 12; ++i) hs->Tf.m[i] = static_cast<float>(hs->T[i]);
-  hs->prev_mse = DBL_MAX;
-  CUDA_TRY(cudaMemcpyAsync(B.prm, stage, 2048, cudaMemcpyHostToDevice, ctx->stream));
-  // centre of the linear algebra: the target centroid (FP64 sums, cast to float)
-  double* c4 = static_cast<double*>(dev_alloc(ctx, 4 * sizeof(double)));
-  centroid_device(ctx, tgt, c4, &B.prm->c[0]);
-  dev_free(ctx, c4);
+  // host staging: pair parameters, states, prefixes, centroid inputs
+  std::vector<IcpParams> hp(npairs);
+  std::vector<IcpState> hs(npairs);
+  std::vector<int> tile0(npairs + 1), chunk0(npairs + 1), npts(npairs), cc0(npairs + 1, 0);
+  std::vector<const float4*> txyz(npairs);
+  const float cap = float_cap(p->max_correspondence_distance * p->max_correspondence_distance);
+  int tiles = 0, chunks = 0;
+  for (int i = 0; i < npairs; ++i) {
+    const Index& si = cloud_index(ctx, src[i]);
+    const Index& ti = cloud_index(ctx, tgt[i]);
+    IcpParams& q = hp[i];
+    std::memset(&q, 0, sizeof(q));
+    q.tgt = ti.v;
+    q.src_pts = si.v.pts;
+    q.tgt_nrm = tgt[i]->nrm;
+    q.src_ntiles = si.v.nleaf;
+    q.tile0 = tiles;
+    q.chunk0 = chunks;
+    q.cap = cap;
+    q.min_corr = 3;
+    q.max_iter = p->max_iterations;
+    q.teps = p->transformation_epsilon;
+    q.feps = p->euclidean_fitness_epsilon;
+    tile0[i] = tiles;
+    chunk0[i] = chunks;
+    tiles += si.v.nleaf;
+    chunks += (si.v.nleaf + kChunkTiles - 1) / kChunkTiles;
+    IcpState& s = hs[i];
+    std::memset(&s, 0, sizeof(s));
+    const double I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    for (int k = 0; k < 16; ++k) s.T[k] = guesses ? static_cast<double>(guesses[16 * i + k]) : I[k];
+    for (int k = 0; k < 12; ++k) s.Tf.m[k] = static_cast<float>(s.T[k]);
+    s.prev_mse = DBL_MAX;
+    txyz[i] = tgt[i]->xyz;
+    npts[i] = static_cast<int>(tgt[i]->n);
+    cc0[i + 1] = cc0[i] + (npts[i] + kCentroidChunk - 1) / kCentroidChunk;
+  }
+  tile0[npairs] = tiles;
+  chunk0[npairs] = chunks;
+  const int cchunks = cc0[npairs];
+  const size_t slots = static_cast<size_t>(tiles) * 32;
+
+  // one device block for the call: pair arrays, then the scratch
+  const size_t b_prm = align256(sizeof(IcpParams) * npairs), b_st = align256(sizeof(IcpState) * npairs),
+               b_pre = align256(sizeof(int) * (npairs + 1)), b_xyz = align256(sizeof(float4*) * npairs),
+               b_npts = align256(sizeof(int) * npairs), b_part = align256(slots * 4), b_hq = align256(slots * 4),
+               b_htp = align256(slots * 16), b_hti = align256(slots * 4), b_wide = align256(sizeof(uint32_t) * tiles),
+               b_red = align256(sizeof(double) * 32 * chunks), b_fd = align256(slots * 4),
+               b_far = align256(slots * 16), b_cpart = align256(sizeof(double) * 4 * cchunks);
+  const size_t hdr = b_prm + b_st + 3 * b_pre + b_xyz + b_npts;
+  char* blk = static_cast<char*>(
+      dev_alloc(ctx, hdr + b_part + b_hq + b_htp + b_hti + b_wide + b_red + b_fd + b_far + b_cpart));
+  char* cur = blk;
+  BatchDesc hd;
+  std::memset(&hd, 0, sizeof(hd));
+  hd.npairs = npairs;
+  hd.total_tiles = tiles;
+  hd.total_chunks = chunks;
+  hd.use_graph = exec ? 1 : 0;
+  hd.prm = reinterpret_cast<IcpParams*>(cur); cur += b_prm;
+  hd.st = reinterpret_cast<IcpState*>(cur); cur += b_st;
+  int* d_tile0 = reinterpret_cast<int*>(cur); cur += b_pre;
+  int* d_chunk0 = reinterpret_cast<int*>(cur); cur += b_pre;
+  const float4** d_xyz = reinterpret_cast<const float4**>(cur); cur += b_xyz;
+  int* d_npts = reinterpret_cast<int*>(cur); cur += b_npts;
+  int* d_cc0 = reinterpret_cast<int*>(cur); cur += b_pre;
+  hd.tile0 = d_tile0;
+  hd.chunk0 = d_chunk0;
+  hd.tile_part = reinterpret_cast<float*>(cur); cur += b_part;
+  hd.hard_q = reinterpret_cast<uint32_t*>(cur); cur += b_hq;
+  hd.hard_tp = reinterpret_cast<float4*>(cur); cur += b_htp;
+  hd.hard_ti = reinterpret_cast<uint32_t*>(cur); cur += b_hti;
+  hd.wide_tiles = reinterpret_cast<uint32_t*>(cur); cur += b_wide;
+  hd.red = reinterpret_cast<double*>(cur); cur += b_red;
+  hd.fd = reinterpret_cast<float*>(cur); cur += b_fd;
+  hd.far = reinterpret_cast<float4*>(cur); cur += b_far;
+  double* d_cpart = reinterpret_cast<double*>(cur);
+
+  // stage everything in one pinned buffer and copy it in one go
+  const size_t stage_bytes = hdr + 1024 + 256;
+  char* stage = static_cast<char*>(pinned(ctx, stage_bytes));
+  std::memset(stage, 0, stage_bytes);
+  std::memcpy(stage, hp.data(), sizeof(IcpParams) * npairs);
+  std::memcpy(stage + b_prm, hs.data(), sizeof(IcpState) * npairs);
+  std::memcpy(stage + b_prm + b_st, tile0.data(), sizeof(int) * (npairs + 1));
+  std::memcpy(stage + b_prm + b_st + b_pre, chunk0.data(), sizeof(int) * (npairs + 1));
+  std::memcpy(stage + b_prm + b_st + 2 * b_pre, txyz.data(), sizeof(float4*) * npairs);
+  std::memcpy(stage + b_prm + b_st + 2 * b_pre + b_xyz, npts.data(), sizeof(int) * npairs);
+  std::memcpy(stage + b_prm + b_st + 2 * b_pre + b_xyz + b_npts, cc0.data(), sizeof(int) * (npairs + 1));
+  BatchCounters hc;
+  std::memset(&hc, 0, sizeof(hc));
+  hc.max_rounds = p->max_iterations + 1;
+  std::memcpy(stage + hdr, &hd, sizeof(hd));
+  std::memcpy(stage + hdr + 512, &hc, sizeof(hc));
+  CUDA_TRY(cudaMemcpyAsync(blk, stage, hdr, cudaMemcpyHostToDevice, ctx->stream));
+  CUDA_TRY(cudaMemcpyAsync(B.desc, stage + hdr, 1024, cudaMemcpyHostToDevice, ctx->stream));
+  const int pair_blocks = std::min((npairs + kIcpWarps - 1) / kIcpWarps, 128);  // one warp per pair
+  LCR_LAUNCH(ctx, k_centroid_chunks, std::min(cchunks, icp_grid(ctx)), kIcpThreads, 0, d_xyz, d_npts, d_cc0, npairs,
+             d_cpart);
+  LCR_LAUNCH(ctx, k_centroid_final, pair_blocks, kIcpThreads, 0, B.desc, d_cc0, d_cpart);
 
   if (exec) {
     CUDA_TRY(cudaGraphLaunch(exec, ctx->stream));
   } else {
     cudaGraphConditionalHandle none = 0;
-    for (int it = 0; it < p->max_iterations; ++it) {
-      if (p2pl) LCR_LAUNCH(ctx, k_icp_search<1>, grid, kIcpThreads, 0, B.prm, B.st);
-      else LCR_LAUNCH(ctx, k_icp_search<0>, grid, kIcpThreads, 0, B.prm, B.st);
-      LCR_LAUNCH(ctx, k_icp_hard, grid, kIcpThreads, 0, B.prm, B.st);
-      if (p2pl) LCR_LAUNCH(ctx, k_icp_wide<1>, grid, kIcpThreads, 0, B.prm, B.st);
-      else LCR_LAUNCH(ctx, k_icp_wide<0>, grid, kIcpThreads, 0, B.prm, B.st);
-      LCR_LAUNCH(ctx, k_icp_reduce, kIcpReduceBlocks, 256, 0, B.prm, B.st, B.part);
-      if (p2pl) LCR_LAUNCH(ctx, k_icp_solve<1>, 1, kIcpThreads, 0, B.prm, B.st, B.part, kIcpReduceBlocks, none);
-      else LCR_LAUNCH(ctx, k_icp_solve<0>, 1, kIcpThreads, 0, B.prm, B.st, B.part, kIcpReduceBlocks, none);
-      if ((it & 7) == 7) {
-        int* hd = static_cast<int*>(pinned(ctx, 2048)) + 384;
-        CUDA_TRY(cudaMemcpyAsync(hd, &B.st->done, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    const int grid = icp_grid(ctx);
+    unsigned* hlive = reinterpret_cast<unsigned*>(stage + hdr + 1024);
+    for (int it = 0; it < p->max_iterations + 1; ++it) {
+      if (p2pl) LCR_LAUNCH(ctx, k_icp_search<1>, grid, kIcpThreads, 0, B.desc, B.cnt);
+      else LCR_LAUNCH(ctx, k_icp_search<0>, grid, kIcpThreads, 0, B.desc, B.cnt);
+      LCR_LAUNCH(ctx, k_icp_hard, grid, kIcpThreads, 0, B.desc, B.cnt);
+      if (p2pl) LCR_LAUNCH(ctx, k_icp_wide<1>, grid, kIcpThreads, 0, B.desc, B.cnt);
+      else LCR_LAUNCH(ctx, k_icp_wide<0>, grid, kIcpThreads, 0, B.desc, B.cnt);
+      LCR_LAUNCH(ctx, k_icp_reduce, reduce_grid(ctx), kIcpThreads, 0, B.desc, B.cnt);
+      if (p2pl) LCR_LAUNCH(ctx, k_icp_solve<1>, sblocks, kIcpThreads, 0, B.desc, B.cnt, none);
+      else LCR_LAUNCH(ctx, k_icp_solve<0>, sblocks, kIcpThreads, 0, B.desc, B.cnt, none);
+      if ((it & 7) == 7 || it == p->max_iterations) {
+        CUDA_TRY(cudaMemcpyAsync(hlive, &B.cnt->live, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
         sync(ctx);
-        if (*hd) break;
+        if (*hlive == 0) break;
       }
     }
   }
   if (p->compute_fitness) {
-    LCR_LAUNCH(ctx, k_fitness, grid, kIcpThreads, 0, B.prm, B.st);
-    LCR_LAUNCH(ctx, k_fitness_far, grid, kIcpThreads, 0, B.prm, B.st);
-    LCR_LAUNCH(ctx, k_fitness_reduce, std::min(grid, 256), 256, 0, B.prm, B.st, B.part);
+    const int grid = icp_grid(ctx);
+    LCR_LAUNCH(ctx, k_fitness, grid, kIcpThreads, 0, B.desc, B.cnt);
+    LCR_LAUNCH(ctx, k_fitness_far, grid, kIcpThreads, 0, B.desc, B.cnt);
+    LCR_LAUNCH(ctx, k_fitness_chunks, reduce_grid(ctx), kIcpThreads, 0, B.desc);
+    LCR_LAUNCH(ctx, k_fitness_reduce, pair_blocks, kIcpThreads, 0, B.desc, B.cnt);
   }
-  CUDA_TRY(cudaMemcpyAsync(hs, B.st, sizeof(IcpState), cudaMemcpyDeviceToHost, ctx->stream));
-  dev_free(ctx, callbuf);
+  IcpState* out = reinterpret_cast<IcpState*>(stage);  // after the staged copy in stream order
+  unsigned* hrounds = reinterpret_cast<unsigned*>(reinterpret_cast<char*>(out) + b_st);
+  CUDA_TRY(cudaMemcpyAsync(out, hd.st, sizeof(IcpState) * npairs, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaMemcpyAsync(hrounds, &B.cnt->rounds, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  dev_free(ctx, blk);
   sync(ctx);
-  if (exec) ctx->launches += 5 * static_cast<uint64_t>(hs->launches);  // five kernels per body run
-  std::memset(res, 0, sizeof(*res));
-  for (int i = 0; i < 16; ++i) {
-    res->transform64[i] = hs->T[i];
-    res->transform[i] = static_cast<float>(hs->T[i]);
+  if (exec) ctx->launches += 5 * static_cast<uint64_t>(*hrounds);  // five kernels per body run
+  for (int i = 0; i < npairs; ++i) {
+    const IcpState& s = out[i];
+    lcr_icp_result& r = res[i];
+    std::memset(&r, 0, sizeof(r));
+    for (int k = 0; k < 16; ++k) {
+      r.transform64[k] = s.T[k];
+      r.transform[k] = static_cast<float>(s.T[k]);
+    }
+    r.converged = s.converged;
+    r.iterations = s.iter;
+    r.state = s.state;
+    r.n_correspondences = s.ncorr;
+    r.fitness = p->compute_fitness ? s.fitness : 0.0;
+    r.mse = s.mse;
   }
-  res->converged = hs->converged;
-  res->iterations = hs->iter;
-  res->state = hs->state;
-  res->n_correspondences = hs->ncorr;
-  res->fitness = p->compute_fitness ? hs->fitness : 0.0;
-  res->mse = hs->mse;
+}
+
+void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr_icp_params* p, const float* guess,
+             lcr_icp_result* res) {
+  icp_batch_run(ctx, &src, &tgt, 1, p, guess, res);
 }

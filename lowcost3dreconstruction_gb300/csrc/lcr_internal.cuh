@@ -89,7 +89,7 @@ struct lcr_ctx {
   void* icp_block = nullptr;
   size_t icp_bytes = 0;
   // captured ICP loops (one per method), reused across calls
-  cudaGraphExec_t icp_exec[2] = {nullptr, nullptr};
+  cudaGraphExec_t icp_exec[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};  // [method][solve width]
   int icp_graph_ok = -1;        // -1 unknown, 0 unavailable, 1 usable
   // optional event timing of selected kernels (lcr_kernel_timing)
   bool timing = false;
@@ -228,6 +228,8 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
 lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[3], int flags);
 void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr_icp_params* p, const float* guess,
              lcr_icp_result* res);
+void icp_batch_run(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* const* tgt, int npairs,
+                   const lcr_icp_params* p, const float* guesses, lcr_icp_result* res);
 void corr_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const double* T, double dmax, int32_t* d_idx,
               float* d_dist);
 void crop_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, double radius, uint8_t* d_removed);

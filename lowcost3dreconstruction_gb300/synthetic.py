@@ -226,6 +226,24 @@ def config1_pair(seed: int = 1) -> Pair:
     return make_pair(sphere_on_cube_room(), 20.0, (0.03, 0.0, 0.0), 10, seed, dropout=0.03)
 
 
+def turntable_cycle(seed: int = 2, views: int = 36, step_deg: float = 10.0, frames: int = 1,
+                    cam: dict = KINECT_V1) -> tuple[np.ndarray, list[np.ndarray]]:
+    """A seeded superquadric object on a turntable, captured every `step_deg`
+    degrees about its vertical axis: (frames-per-view depth bursts [views, F, H, W],
+    ground-truth pose of each view relative to view 0).  Consecutive views
+    overlap by 360/views degrees less than a full turn, so each pair sees part
+    of the surface the other does not (self-occlusion)."""
+    rng = np.random.default_rng(seed)
+    obj = superquadric_object(rng)
+    caps, poses = [], []
+    for v in range(views):
+        T = turntable(step_deg * v, OBJECT_AXIS)
+        d = raycast(obj, cam, T)
+        caps.append(kinect_frames(d, frames, rng, 0.0))
+        poses.append(T)
+    return np.stack(caps), poses
+
+
 def rmse(T_est: np.ndarray, T_gt: np.ndarray, xyz: np.ndarray) -> float:
     p = np.c_[np.asarray(xyz, np.float64), np.ones(len(xyz))]
     d = p @ (np.asarray(T_est, np.float64) - np.asarray(T_gt, np.float64)).T

@@ -177,33 +177,47 @@ __device__ double det3(const double M[9]) {
 
 // SPD 6x6 solve by LDL^T; pivots below 1e-12 of the largest diagonal count as
 // singular (degenerate correspondence geometry).
-__device__ bool ldlt6(const double M[36], const double b[6], double x[6]) {
+__device__ __forceinline__ bool ldlt6(const double M[36], const double b[6], double x[6]) {
+  // fully unrolled: every index is a constant, so M, L, D stay in registers
   double L[36], D[6];
   double dmax = 0;
+#pragma unroll
   for (int i = 0; i < 6; ++i) dmax = fmax(dmax, fabs(M[7 * i]));
   if (!(dmax > 0)) return false;
+#pragma unroll
   for (int i = 0; i < 36; ++i) L[i] = 0;
+  bool ok = true;
+#pragma unroll
   for (int j = 0; j < 6; ++j) {
     double d = M[6 * j + j];
+#pragma unroll
     for (int k = 0; k < j; ++k) d -= L[6 * j + k] * L[6 * j + k] * D[k];
-    if (!(d > 1e-12 * dmax)) return false;
+    ok = ok && d > 1e-12 * dmax;
     D[j] = d;
     L[6 * j + j] = 1.0;
+#pragma unroll
     for (int i = j + 1; i < 6; ++i) {
       double v = M[6 * i + j];
+#pragma unroll
       for (int k = 0; k < j; ++k) v -= L[6 * i + k] * L[6 * j + k] * D[k];
       L[6 * i + j] = v / d;
     }
   }
+  if (!ok) return false;
   double y[6];
+#pragma unroll
   for (int i = 0; i < 6; ++i) {
     double v = b[i];
+#pragma unroll
     for (int k = 0; k < i; ++k) v -= L[6 * i + k] * y[k];
     y[i] = v;
   }
+#pragma unroll
   for (int i = 0; i < 6; ++i) y[i] /= D[i];
+#pragma unroll
   for (int i = 5; i >= 0; --i) {
     double v = y[i];
+#pragma unroll
     for (int k = i + 1; k < 6; ++k) v -= L[6 * k + i] * x[k];
     x[i] = v;
   }
@@ -235,15 +249,18 @@ __device__ bool solve_point(const double* S, const double c[3], double n, double
 
 // Point-to-plane linear least squares about c: S[0..20] upper triangle of A^T A,
 // S[21..26] A^T b, rows A = [ s' x n, n ], b = n.(t' - s').  R = Rz Ry Rx.
-__device__ bool solve_plane(const double* S, const double c[3], double dT[16]) {
+__device__ __forceinline__ bool solve_plane(const double* S, const double c[3], double dT[16]) {
   double M[36], b[6], x[6];
   int k = 0;
+#pragma unroll
   for (int i = 0; i < 6; ++i)
+#pragma unroll
     for (int j = i; j < 6; ++j) {
       M[6 * i + j] = S[k];
       M[6 * j + i] = S[k];
       ++k;
     }
+#pragma unroll
   for (int i = 0; i < 6; ++i) b[i] = S[21 + i];
   if (!ldlt6(M, b, x)) return false;
   double sa, ca, sb, cb, sg, cg;
@@ -262,7 +279,7 @@ __device__ bool solve_plane(const double* S, const double c[3], double dT[16]) {
   return true;
 }
 
-__device__ void orthonormalize(double T[16]) {
+__device__ __forceinline__ void orthonormalize(double T[16]) {
   double r0[3] = {T[0], T[1], T[2]}, r1[3] = {T[4], T[5], T[6]};
   const double n0 = sqrt(r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2]);
   for (int i = 0; i < 3; ++i) r0[i] /= n0;
@@ -280,7 +297,7 @@ __device__ void orthonormalize(double T[16]) {
 // One ICP iteration's bookkeeping (PCL computeTransformation loop body with
 // DefaultConvergenceCriteria as the reference tool configures it).
 template <int P2PL>
-__device__ void icp_update(const double* S, const IcpParams* prm, IcpState* st) {
+__device__ __forceinline__ void icp_update(const double* S, const IcpParams* prm, IcpState* st) {
   const double cnt = P2PL ? S[27] : S[15];
   const double dsum = P2PL ? S[28] : S[16];
   const int ncorr = static_cast<int>(cnt + 0.5);
@@ -302,11 +319,16 @@ __device__ void icp_update(const double* S, const IcpParams* prm, IcpState* st) 
     st->done = 1;
     return;
   }
-  double T[16];
+  double T[16], T0[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) T0[i] = st->T[i];
+#pragma unroll
   for (int i = 0; i < 4; ++i)
+#pragma unroll
     for (int j = 0; j < 4; ++j) {
       double s = 0;
-      for (int k = 0; k < 4; ++k) s += dT[4 * i + k] * st->T[4 * k + j];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) s += dT[4 * i + k] * T0[4 * k + j];
       T[4 * i + j] = s;
     }
   orthonormalize(T);

@@ -282,13 +282,18 @@ void svd3(const double A[9], double U[9], double s[3], double V[9]) {
 }
 
 /* Solve the SPD 6x6 system M x = b by LDL^T. Returns false if singular. */
+/* SPD 6x6 solve by LDL^T; a pivot below 1e-12 of the largest diagonal entry
+ * counts as singular (degenerate correspondence geometry). */
 bool ldlt6(const double M[36], const double b[6], double x[6]) {
   double L[36] = {0}, D[6];
+  double dmax = 0;
+  for (int i = 0; i < 6; ++i) dmax = std::max(dmax, std::fabs(M[7 * i]));
+  if (!(dmax > 0)) return false;
   for (int j = 0; j < 6; ++j) {
     double d = M[6 * j + j];
     for (int k = 0; k < j; ++k) d -= L[6 * j + k] * L[6 * j + k] * D[k];
     D[j] = d;
-    if (!(std::fabs(d) > 0)) return false;
+    if (!(d > 1e-12 * dmax)) return false;
     L[6 * j + j] = 1.0;
     for (int i = j + 1; i < 6; ++i) {
       double v = M[6 * i + j];

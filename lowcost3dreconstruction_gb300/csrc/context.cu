@@ -65,6 +65,10 @@ lcr_cloud* cloud_alloc(lcr_ctx* ctx, size_t n) {
 void cloud_release(lcr_ctx* ctx, lcr_cloud* c) {
   if (!c) return;
   free_index(ctx, c->index);
+  if (c->nbr) {
+    dev_free(ctx, c->nbr->block);
+    delete c->nbr;
+  }
   dev_free(ctx, c->xyz);
   delete c;
 }

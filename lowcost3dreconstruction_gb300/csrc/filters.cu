@@ -29,7 +29,8 @@ struct SorAcc {
   int emin;       // smallest biased exponent (>= 1) of a nonzero term
   int cnt;
   bool off_grid;
-  __device__ __forceinline__ void init() {
+  __device__ __forceinline__ void init(unsigned long long* list) {
+    out = list;
     sum = 0;
     eg = 0;
     dmin = LCR_INF;
@@ -66,8 +67,16 @@ struct SorAcc {
       emin = min(emin, max(1, static_cast<int>(__float_as_uint(v) >> 23)));
     }
   }
-  __device__ __forceinline__ void add(const float4&, float d) { add_d(d); }
-  __device__ __forceinline__ void add_key(unsigned long long k) { add_d(key_dist(k)); }
+  // the neighbour list of the query (may be null): the keys as they come
+  unsigned long long* out;
+  __device__ __forceinline__ void add(const float4& p, float d) {
+    if (out) out[cnt] = make_key(d, __float_as_uint(p.w));
+    add_d(d);
+  }
+  __device__ __forceinline__ void add_key(unsigned long long k) {
+    if (out) out[cnt] = k;
+    add_d(key_dist(k));
+  }
   // true if the ascending double sum is the exact one; s = that sum of all
   // terms but the smallest
   __device__ __forceinline__ bool result(double& s) {
@@ -95,7 +104,7 @@ __device__ __forceinline__ void sor_store(const float4& q, double s, int mean_k,
 // at most k finite points); the host reports it after the pass.
 __global__ void k_sor_dist(IndexView ix, int mean_k, float* __restrict__ dist, uint8_t* __restrict__ valid,
                            unsigned int* __restrict__ nvalid, uint32_t* __restrict__ redo, unsigned int* nredo,
-                           int* too_few) {
+                           int* too_few, unsigned long long* __restrict__ lists) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int K = mean_k + 1;
@@ -107,7 +116,7 @@ __global__ void k_sor_dist(IndexView ix, int mean_k, float* __restrict__ dist, u
   float4 tlo, thi;
   if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
   SorAcc acc;
-  acc.init();
+  acc.init(lists && qv ? lists + static_cast<size_t>(__float_as_uint(q.w)) * K : nullptr);
   tile_kset(ix, q.x, q.y, q.z, qv, K, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), wbase + sizeof(KnnWarp), tile,
             acc);
   if (qv && acc.cnt < K) *too_few = 1;
@@ -123,7 +132,7 @@ __global__ void k_sor_dist(IndexView ix, int mean_k, float* __restrict__ dist, u
 // k+1 nearest, one warp per tile, warps striding over the queue.
 __global__ void k_sor_dist_sorted(IndexView ix, int mean_k, float* __restrict__ dist, uint8_t* __restrict__ valid,
                                   unsigned int* __restrict__ nvalid, const uint32_t* __restrict__ redo,
-                                  const unsigned int* nredo) {
+                                  const unsigned int* nredo, unsigned long long* __restrict__ lists) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int K = mean_k + 1;
@@ -142,6 +151,8 @@ __global__ void k_sor_dist_sorted(IndexView ix, int mean_k, float* __restrict__ 
       double s = 0.0;
       for (int j = 1; j < K; ++j) s = __dadd_rn(s, static_cast<double>(__fsqrt_rn(key_dist(list[j * 32 + lane]))));
       sor_store(q, s, mean_k, dist, valid, nvalid);
+      if (lists)
+        for (int j = 0; j < K; ++j) lists[static_cast<size_t>(__float_as_uint(q.w)) * K + j] = list[j * 32 + lane];
     }
     __syncwarp();
   }
@@ -354,6 +365,142 @@ __global__ void k_normals(IndexView ix, int K, const float4* __restrict__ xyz, f
   if (qv) normal_store(acc, vx, vy, vz, flip_all, __float_as_uint(q.w), onrm);
 }
 
+// Normals of SOR inliers from SOR's neighbour lists (no search).  A warp takes
+// 32 inliers; for each, its source's list (K <= 64 unordered keys, two per
+// lane) is masked to the inliers and bitonic-sorted across the warp, and the
+// first k inlier keys -- the exact k nearest inliers when the list holds at
+// least k of them -- give the covariance (FP32 sums over the warp, fixed
+// shuffle tree); then every lane solves its own point's eigenproblem.  A point
+// whose list holds fewer than k inliers is queued for k_normals_queued.
+__device__ __forceinline__ void cswap(unsigned long long& x, unsigned long long u, bool keep_min) {
+  x = keep_min ? (u < x ? u : x) : (u > x ? u : x);
+}
+
+__global__ void __launch_bounds__(256) k_normals_list(const unsigned long long* __restrict__ keys, int K,
+                                                      const uint8_t* __restrict__ keep,
+                                                      const uint32_t* __restrict__ rank,
+                                                      const uint32_t* __restrict__ kept, int n, int k,
+                                                      const float4* __restrict__ xyz, float vx, float vy, float vz,
+                                                      int flip_all, float4* __restrict__ onrm,
+                                                      uint32_t* __restrict__ queue, unsigned int* nqueue) {
+  const int lane = threadIdx.x & 31;
+  const int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+  if (base >= n) return;
+  const unsigned long long none = ~0ull;
+  NeAcc mine;
+  mine.init(0.f, 0.f, 0.f, xyz);
+  bool have = false;
+  const int cnt_pts = min(32, n - base);
+  // the lists of the warp's points are read one point ahead
+  unsigned long long na = none, nb = none;
+  float4 nq = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto fetch = [&](int j) {
+    nq = xyz[base + j];
+    na = nb = none;
+    if (finite3(nq.x, nq.y, nq.z)) {
+      const size_t o = kept[base + j];
+      if (lane < K) na = keys[o * K + lane];
+      if (lane + 32 < K) nb = keys[o * K + lane + 32];
+    }
+  };
+  fetch(0);
+  for (int j = 0; j < cnt_pts; ++j) {
+    const float4 q = nq;
+    unsigned long long a = na, b = nb;
+    if (j + 1 < cnt_pts) fetch(j + 1);
+    if (!finite3(q.x, q.y, q.z)) continue;  // not searched: stays NaN
+    if (a != none && !keep[key_idx(a)]) a = none;
+    if (b != none && !keep[key_idx(b)]) b = none;
+    const int inl = __popc(__ballot_sync(LCR_FULL, a != none)) + __popc(__ballot_sync(LCR_FULL, b != none));
+    if (inl < k) {
+      if (lane == 0) queue[atomicAdd(nqueue, 1u)] = static_cast<uint32_t>(base + j);
+      continue;
+    }
+    // ascending bitonic sort of the 64 keys: element lane in a, lane+32 in b
+#pragma unroll
+    for (int w = 2; w <= 64; w <<= 1) {
+#pragma unroll
+      for (int st = w >> 1; st > 0; st >>= 1) {
+        if (st == 32) {
+          const unsigned long long lo = a < b ? a : b, hi = a < b ? b : a;
+          a = lo;
+          b = hi;
+        } else {
+          const bool lower = (lane & st) == 0;
+          const unsigned long long ua = __shfl_xor_sync(LCR_FULL, a, st);
+          cswap(a, ua, lower == ((lane & w) == 0));
+          const unsigned long long ub = __shfl_xor_sync(LCR_FULL, b, st);
+          cswap(b, ub, lower == (((lane + 32) & w) == 0));
+        }
+      }
+    }
+    // covariance over the first k: elements lane (< k) and lane + 32 (< k)
+    float t[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (lane < k) {
+      const float4 p = xyz[rank[key_idx(a)]];
+      const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+      t[0] = dx; t[1] = dy; t[2] = dz;
+      t[3] = dx * dx; t[4] = dx * dy; t[5] = dx * dz; t[6] = dy * dy; t[7] = dy * dz; t[8] = dz * dz;
+    }
+    if (lane + 32 < k) {
+      const float4 p = xyz[rank[key_idx(b)]];
+      const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+      t[0] += dx; t[1] += dy; t[2] += dz;
+      t[3] += dx * dx; t[4] += dx * dy; t[5] += dx * dz; t[6] += dy * dy; t[7] += dy * dz; t[8] += dz * dz;
+    }
+#pragma unroll
+    for (int c = 0; c < 9; ++c) t[c] = warp_sum(t[c]);
+    if (lane == j) {
+      mine.qx = q.x; mine.qy = q.y; mine.qz = q.z;
+      mine.sx = t[0]; mine.sy = t[1]; mine.sz = t[2];
+      mine.sxx = t[3]; mine.sxy = t[4]; mine.sxz = t[5]; mine.syy = t[6]; mine.syz = t[7]; mine.szz = t[8];
+      mine.m = k;
+      have = true;
+    }
+  }
+  if (have) normal_store(mine, vx, vy, vz, flip_all, static_cast<uint32_t>(base + lane), onrm);
+}
+
+// Position of every point in the index's sorted order.
+__global__ void k_index_pos(IndexView ix, uint32_t* __restrict__ pos) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= ix.nleaf * 32) return;
+  const uint32_t w = __float_as_uint(ix.pts[s].w);
+  if (w != 0xffffffffu) pos[w] = static_cast<uint32_t>(s);
+}
+
+// Queued points (their list held fewer than k inliers): one warp per point, a
+// search with that point as the tile's only query, seeded with its own leaf
+// and two either side; its histogram range is set from its list's farthest
+// entry (the k-th inlier lies beyond it).
+__global__ void k_normals_queued(IndexView ix, int K, const float4* __restrict__ xyz, float vx, float vy, float vz,
+                                 int flip_all, float4* __restrict__ onrm, const uint32_t* __restrict__ queue,
+                                 const unsigned int* nqueue, const unsigned long long* __restrict__ keys, int LK,
+                                 const uint32_t* __restrict__ kept, const uint32_t* __restrict__ pos) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned char* wbase = smem + wib * kset_warp_bytes();
+  const unsigned count = *nqueue;
+  for (unsigned w = blockIdx.x * nw + wib; w < count; w += gridDim.x * nw) {
+    const uint32_t i = queue[w];
+    const float4 p = xyz[i];
+    const size_t o = kept[i];
+    float far2 = 0.f;
+    for (int j = lane; j < LK; j += 32) far2 = fmaxf(far2, key_dist(keys[o * LK + j]));
+    far2 = warp_max(far2);
+    const bool qv = lane == 0;
+    const float qx = qv ? p.x : 0.f, qy = qv ? p.y : 0.f, qz = qv ? p.z : 0.f;
+    float4 tlo, thi;
+    tile_box(qx, qy, qz, qv, tlo, thi);
+    NeAcc acc;
+    acc.init(qx, qy, qz, xyz);
+    tile_kset(ix, qx, qy, qz, qv, K, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), wbase + sizeof(KnnWarp),
+              static_cast<int>(pos[i] >> 5), acc, 256.f * fmaxf(far2, 1e-30f));
+    if (qv) normal_store(acc, vx, vy, vz, flip_all, i, onrm);
+    __syncwarp();
+  }
+}
+
 // ----------------------------------------------------------------- crop
 // accumulate_clouds.cpp:100-111: a source point p is redundant when some target
 // q has float(q - r) <= p <= float(q + r) on every axis (the CropBox bounds are
@@ -412,6 +559,15 @@ __global__ void k_crop(IndexView tgt, IndexView src, double r, uint8_t* __restri
 
 size_t list_smem(int nw, int K) { return nw * knn_warp_bytes(K); }
 
+constexpr int kListMaxK = 64;  // neighbour lists handed to the inliers hold at most this many keys
+
+inline size_t align_up(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+__global__ void k_rank_of(const uint32_t* __restrict__ kept, int nkeep, uint32_t* __restrict__ rank) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nkeep) rank[kept[j]] = static_cast<uint32_t>(j);
+}
+
 // Warps per block of the unordered k-NN kernels (11 KB of shared memory per
 // warp: 5 warps x 4 blocks = 20 resident warps per SM).
 constexpr int kSetWarps = 5;
@@ -457,15 +613,33 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
   CUDA_TRY(cudaMemsetAsync(valid, 0, n, ctx->stream));
   CUDA_TRY(cudaMemsetAsync(sums + 4 * nc0 + 4, 0, 2 * sizeof(double), ctx->stream));
   const RedoQueue rq = redo_queue(ctx, ix.nleaf);
+  // neighbour lists for the inliers' normals (k <= 64 only: two keys per lane there)
+  NbrHint* hint = nullptr;
+  unsigned long long* lists = nullptr;
+  if (inliers && K <= kListMaxK) {
+    hint = new NbrHint();
+    const size_t b_keys = align_up(sizeof(unsigned long long) * K * static_cast<size_t>(n)),
+                 b_keep = align_up(static_cast<size_t>(n)), b_rank = align_up(sizeof(uint32_t) * n);
+    char* blk = static_cast<char*>(dev_alloc(ctx, b_keys + b_keep + 2 * b_rank));
+    hint->block = blk;
+    lists = reinterpret_cast<unsigned long long*>(blk);
+    hint->keys = lists;
+    hint->keep = reinterpret_cast<uint8_t*>(blk + b_keys);
+    hint->rank = reinterpret_cast<uint32_t*>(blk + b_keys + b_keep);
+    hint->kept = reinterpret_cast<uint32_t*>(blk + b_keys + b_keep + b_rank);
+    hint->K = K;
+    hint->n_src = n;
+  }
   CUDA_TRY(cudaFuncSetAttribute(k_sor_dist, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_set)));
   CUDA_TRY(cudaFuncSetAttribute(k_sor_dist_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 static_cast<int>(smem)));
   {
     KernelTimer kt(ctx, LCR_KT_SOR_KNN);
     LCR_LAUNCH(ctx, k_sor_dist, (ix.nleaf + kSetWarps - 1) / kSetWarps, kSetWarps * 32, smem_set, ix, mean_k, dist,
-               valid, nvalid, rq.tiles(), rq.count(), too_few);
+               valid, nvalid, rq.tiles(), rq.count(), too_few, lists);
   }
-  LCR_LAUNCH(ctx, k_sor_dist_sorted, ctx->sms, nw * 32, smem, ix, mean_k, dist, valid, nvalid, rq.tiles(), rq.count());
+  LCR_LAUNCH(ctx, k_sor_dist_sorted, ctx->sms, nw * 32, smem, ix, mean_k, dist, valid, nvalid, rq.tiles(), rq.count(),
+             lists);
   dev_free(ctx, rq.block);
   // blocked sums (ping-pong between two halves of `sums`)
   double *a = sums, *b = sums + nc0, *a2 = sums + 2 * nc0, *b2 = sums + 3 * nc0;
@@ -490,6 +664,10 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
     dev_free(ctx, flags);
     dev_free(ctx, sums);
     dev_free(ctx, idx);
+    if (hint) {
+      dev_free(ctx, hint->block);
+      delete hint;
+    }
     LCR_THROW(LCR_ERR_TOO_FEW_POINTS, "SOR needs more than %d finite points (k+1 neighbours)", mean_k);
   }
   if (inliers) {
@@ -497,6 +675,18 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
     gather_cloud(ctx, in, idx, nkeep, *inliers);
     // the inliers keep the input's sorted order: their index is a compaction
     if (nkeep > 0) (*inliers)->index = subset_index(ctx, *in->index, keep, idx, nkeep);
+    if (hint && nkeep > 0) {
+      CUDA_TRY(cudaMemcpyAsync(const_cast<uint8_t*>(hint->keep), keep, n, cudaMemcpyDeviceToDevice, ctx->stream));
+      CUDA_TRY(cudaMemcpyAsync(const_cast<uint32_t*>(hint->kept), idx, sizeof(uint32_t) * nkeep,
+                               cudaMemcpyDeviceToDevice, ctx->stream));
+      LCR_LAUNCH(ctx, k_rank_of, (nkeep + 255) / 256, 256, 0, hint->kept, nkeep, const_cast<uint32_t*>(hint->rank));
+      (*inliers)->nbr = hint;
+      hint = nullptr;
+    }
+  }
+  if (hint) {
+    dev_free(ctx, hint->block);
+    delete hint;
   }
   if (outliers) {
     const int ndrop = compact_flags(ctx, drop, n, idx);
@@ -534,6 +724,29 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
   CUDA_TRY(cudaMemsetAsync(out->nrm, 0xff, sizeof(float4) * n, ctx->stream));
   const size_t smem_set = kSetWarps * kset_warp_bytes();
   const int flip = (flags & LCR_NORMALS_FLIP_ALL) ? 1 : 0;
+  const NbrHint* h = in->nbr;
+  if (h && k <= h->K && h->K <= kListMaxK) {
+    // SOR inliers: select from SOR's neighbour lists; points whose list holds
+    // fewer than k inliers are searched one per warp
+    char* tmp = static_cast<char*>(dev_alloc(ctx, 2 * align_up(sizeof(uint32_t) * n) + 256));
+    uint32_t* queue = reinterpret_cast<uint32_t*>(tmp);
+    uint32_t* pos = reinterpret_cast<uint32_t*>(tmp + align_up(sizeof(uint32_t) * n));
+    unsigned int* nq = reinterpret_cast<unsigned int*>(tmp + 2 * align_up(sizeof(uint32_t) * n));
+    CUDA_TRY(cudaMemsetAsync(nq, 0, sizeof(unsigned int), ctx->stream));
+    {
+      KernelTimer kt(ctx, LCR_KT_NORMALS_KNN);
+      LCR_LAUNCH(ctx, k_normals_list, (n + 255) / 256, 256, 0, h->keys, h->K, h->keep, h->rank, h->kept, n, k,
+                 in->xyz, vp[0], vp[1], vp[2], flip, out->nrm, queue, nq);
+    }
+    CUDA_TRY(cudaFuncSetAttribute(k_normals_queued, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(smem_set)));
+    LCR_LAUNCH(ctx, k_index_pos, (ix.nleaf * 32 + 255) / 256, 256, 0, ix, pos);
+    LCR_LAUNCH(ctx, k_normals_queued, ctx->sms * 2, kSetWarps * 32, smem_set, ix, k, in->xyz, vp[0], vp[1], vp[2],
+               flip, out->nrm, queue, nq, h->keys, h->K, h->kept, pos);
+    dev_free(ctx, tmp);
+    out->index = share_index(in->index);
+    return out;
+  }
   CUDA_TRY(cudaFuncSetAttribute(k_normals, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_set)));
   {
     KernelTimer kt(ctx, LCR_KT_NORMALS_KNN);

@@ -68,12 +68,30 @@ struct Index {
 };
 
 // ------------------------------------------------------------------ cloud
+// The exact k nearest neighbours (unordered (distance, index) keys, index in
+// the numbering of the cloud they were searched in) that StatisticalOutlier-
+// Removal found for every input point, handed to its inlier cloud: the k'
+// nearest inliers of an inlier are the first k' inliers of its list whenever
+// the list holds at least k' of them, so NormalEstimation on the inliers can
+// select instead of searching again.  One allocation: keys, then keep flags,
+// rank (input index -> inlier index), kept (inlier index -> input index).
+struct NbrHint {
+  void* block = nullptr;
+  const unsigned long long* keys;  // [n_src][K]
+  const uint8_t* keep;             // [n_src]
+  const uint32_t* rank;            // [n_src], valid where keep
+  const uint32_t* kept;            // [n_kept]
+  int K = 0;
+  int n_src = 0;
+};
+
 struct lcr_cloud {
   size_t n = 0;
   float4* xyz = nullptr;        // x y z 0
   float4* nrm = nullptr;        // nx ny nz curvature
   uint32_t* rgb = nullptr;      // packed b g r a (little-endian PCL rgba)
   Index* index = nullptr;       // built on first search, freed with the cloud
+  NbrHint* nbr = nullptr;       // SOR inliers only: their source's neighbour lists
 };
 
 struct lcr_ctx {

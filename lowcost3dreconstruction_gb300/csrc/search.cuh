@@ -362,15 +362,18 @@ struct KHist {
   uint32_t* leaves;
   WarpScratch* ws;
   float R;
+  float top_max;  // largest candidate binned into the last (open) bin
 
   __device__ __forceinline__ int bin(float d) const {
     const int b = static_cast<int>(__float_as_uint(d) >> 21) - e0;
     return min(max(b, 0), kBins - 1);
   }
-  // Largest float of bin b; the last bin is unbounded.
+  // Largest float of bin b; the last bin is open above, so its edge is the
+  // largest candidate it received (a valid bound once the k-th lies in it).
   __device__ __forceinline__ float edge(int b) const {
     const int top = b + e0 + 1;
-    if (b >= kBins - 1 || top >= 1020) return LCR_INF;
+    if (b >= kBins - 1) return top_max;
+    if (top >= 1020) return LCR_INF;
     return __uint_as_float((static_cast<uint32_t>(top) << 21) - 1u);
   }
   __device__ __forceinline__ float bound() const { return cl >= K ? fminf(edge(bs - 1), cap) : cap; }
@@ -396,7 +399,9 @@ struct KHist {
       for (int u = 0; u < 4; ++u) {
       const float d = dd[u];
       if (!(d <= tau)) continue;
-      hist[bin(d) * 32 + lane] += 1u;
+      const int b = bin(d);
+      if (b == kBins - 1) top_max = fmaxf(top_max, d);
+      hist[b * 32 + lane] += 1u;
       if (++cl >= K) {
         // drop the top bins while the ones below still hold k candidates
         while (bs > 1) {
@@ -484,7 +489,7 @@ struct KCollect {
 // seeding.  Afterwards kw.leaves holds the scanned leaves (h.nleaves of them).
 __device__ __forceinline__ void knn_pass1(const IndexView& ix, float qx, float qy, float qz, bool qv, int K, float cap,
                                           const float4& tlo, const float4& thi, KnnWarp& kw, unsigned char* region,
-                                          int self_leaf, KHist& h) {
+                                          int self_leaf, KHist& h, float top_hint = 0.f) {
   const int lane = threadIdx.x & 31;
   // Each lane's bins span 16 octaves of d^2 below min(16 x the tile diagonal,
   // 64 x the distance to the nearer of its two neighbours along the Hilbert
@@ -505,11 +510,12 @@ __device__ __forceinline__ void knn_pass1(const IndexView& ix, float qx, float q
     if (qv && wv) sp = fminf(sp, exact_dist2(qx, qy, qz, wx, wy, wz));
     if (sp > 0.f && sp < LCR_INF) top2 = fminf(top2, 4096.f * sp);
   }
+  if (top_hint > 0.f) top2 = top_hint;  // the caller knows the lane's scale
   top2 = fmaxf(top2, 1e-30f);
   h.qx = qx; h.qy = qy; h.qz = qz; h.qv = qv;
   h.K = K; h.lane = lane;
   h.e0 = static_cast<int>(__float_as_uint(top2) >> 21) - (kBins - 1);
-  h.bs = kBins; h.cl = 0; h.nleaves = 0;
+  h.bs = kBins; h.cl = 0; h.nleaves = 0; h.top_max = 0.f;
   h.cap = cap;
   h.hist = reinterpret_cast<uint32_t*>(region);
   h.leaves = kw.leaves;
@@ -706,17 +712,18 @@ struct KSet {
 };
 
 // Feeds the k nearest points of each valid lane (exact set under the
-// (distance, index) order; all points if the cloud holds fewer than k) to acc:
+// (distance, index) order; all points if the cloud holds fewer than k) to acc.
+// top_hint > 0 sets the top of the lanes' histogram range (squared distance).
 // acc.begin(tau, k) with the largest squared distance that can be fed, then
 // acc.add(point, d) for points met in the collect pass and acc.add_key(key)
 // for the selected boundary keys.  Queries are the points of leaf self_leaf of ix.
 template <class Acc>
 __device__ __forceinline__ void tile_kset(const IndexView& ix, float qx, float qy, float qz, bool qv, int K,
                                           const float4& tlo, const float4& thi, KnnWarp& kw, unsigned char* region,
-                                          int self_leaf, Acc& acc) {
+                                          int self_leaf, Acc& acc, float top_hint = 0.f) {
   const int lane = threadIdx.x & 31;
   KHist h;
-  knn_pass1(ix, qx, qy, qz, qv, K, LCR_INF, tlo, thi, kw, region, self_leaf, h);
+  knn_pass1(ix, qx, qy, qz, qv, K, LCR_INF, tlo, thi, kw, region, self_leaf, h, top_hint);
   // boundary range: the bin holding the k-th key (everything if fewer than k)
   unsigned long long klo = make_key(LCR_INF, 0xffffffffu), khi = klo;  // fewer than k: every key is below klo
   int m = 0, cnt = 0;

@@ -283,6 +283,30 @@ def test_normals_vs_fp64_oracle(ctx, cfg0, k):
     np.testing.assert_allclose(g["curvature"][ok], o["curvature"][ok], atol=1e-4)
 
 
+@pytest.mark.parametrize("k", [30, 51])
+def test_normals_of_sor_inliers_from_neighbour_lists(ctx, cfg0, k):
+    # SOR hands its exact 51-NN lists to the inliers; normals select from them
+    # (k=51 leaves every point with an outlier in its list to the search)
+    pts = cfg0["vsrc"]
+    inl, _, _ = ctx.sor(ctx.upload(pts), 50, 1.0)
+    g = ctx.normals(inl, k).download()
+    _, okeep, _ = O.sor(pts, 50, 1.0)
+    o = O.normals(pts[okeep], k)
+    _cmp_points(g, o, fields=("x", "y", "z", "r", "g", "b"))
+    ng, no = normals_of(g).astype(np.float64), normals_of(o).astype(np.float64)
+    dot = np.sum(ng * no, axis=1)
+    ok = o["curvature"] < 0.2
+    ang = np.arccos(np.clip(np.abs(dot[ok]), -1, 1))
+    assert np.percentile(ang, 99.9) < 1e-3, np.percentile(ang, 99.9)
+    assert np.mean(dot[ok] > 0) > 0.999
+    np.testing.assert_allclose(g["curvature"][ok], o["curvature"][ok], atol=1e-4)
+    # the same cloud without the lists (searched): same neighbours, FP32 sums in
+    # another order -- agreement at the normals' FP32 bar
+    s = ctx.normals(ctx.upload(inl.download()), k).download()
+    cos = np.abs(np.sum(normals_of(s).astype(np.float64) * ng, axis=1))
+    assert np.percentile(np.arccos(np.clip(cos[ok], -1, 1)), 99.9) < 1e-3
+
+
 def test_normals_plane_known_answer(ctx):
     rng = np.random.default_rng(5)
     xy = rng.uniform(-0.1, 0.1, size=(4000, 2))

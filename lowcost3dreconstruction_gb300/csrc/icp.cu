@@ -42,6 +42,7 @@ struct IcpParams {
   IndexView tgt;
   const float4* src_pts;  // Hilbert-sorted source (the source index's points)
   const float4* tgt_nrm;  // target normals by original index
+  const float4* tgt_xyz;  // target points by original index
   int src_ntiles;
   int tile0, chunk0;      // first global tile / chunk of this pair
   float cap;              // FP32 form of max_correspondence_distance^2
@@ -75,6 +76,7 @@ struct BatchDesc {
   double* red;            // [total_chunks][32] FP64 chunk sums
   float* fd;              // fitness: squared NN distance per global slot (< 0: not a point)
   float4* far;            // fitness: queries with no target inside the cap (w = global slot)
+  uint32_t* prev_ti;      // per global slot: last round's correspondence (0xffffffff: none)
 };
 
 // Work-queue counters, reset by the last solve block of every round.
@@ -442,6 +444,22 @@ __device__ __forceinline__ void cache_pair(PairCache& pc, const BatchDesc* __res
 
 __device__ __forceinline__ unsigned vload(const unsigned* p) { return *reinterpret_cast<const volatile unsigned*>(p); }
 
+// Last round's correspondence of a slot as a starting candidate for this
+// round's search: key (distance under the current transform, index) if it is
+// still within the cap, else "none".
+__device__ __forceinline__ void prev_candidate(const BatchDesc* __restrict__ d, const IcpParams* __restrict__ prm,
+                                               int gslot, bool pv, const float3& q, unsigned long long& key,
+                                               float4& p) {
+  key = ~0ull;
+  p = make_float4(0.f, 0.f, 0.f, 0.f);
+  const uint32_t prev = pv ? d->prev_ti[gslot] : 0xffffffffu;
+  if (prev == 0xffffffffu) return;
+  p = prm->tgt_xyz[prev];
+  const float dd = exact_dist2(q.x, q.y, q.z, p.x, p.y, p.z);
+  if (dd <= prm->cap) key = make_key(dd, prev);
+  p.w = __uint_as_float(prev);
+}
+
 // 1. Tiles of the live pairs: compact ones searched and reduced to a row,
 // wide ones deferred.
 template <int P2PL>
@@ -486,7 +504,12 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_search(const BatchDesc* __r
     }
     NN1 v;
     v.init(q.x, q.y, q.z, pv, cap, wss[wib]);
+    unsigned long long sk;
+    float4 sp;
+    prev_candidate(d, prm, gslot, pv, q, sk, sp);
+    v.seed(sk, sp);
     tile_traverse(pcs[wib].tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), wss[wib]);
+    d->prev_ti[gslot] = key_idx(v.best);
     float t[32];
     corr_terms<P2PL>(t, pv && v.found(), q, v.bp, key_dist(v.best), key_idx(v.best), prm);
     d->tile_part[gslot] = reduce_scatter32(t, lane);
@@ -514,12 +537,16 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_hard(const BatchDesc* __res
     cache_pair(pcs[wib], d, p, lane);
     const float4 pt = prm->src_pts[(g - prm->tile0) * 32 + (gslot & 31u)];
     const float3 q = xf_apply(pcs[wib].T, pt.x, pt.y, pt.z);
+    unsigned long long sk;
+    float4 sp;
+    prev_candidate(d, prm, static_cast<int>(gslot), true, q, sk, sp);
     unsigned long long best;
     float4 bp;
-    warp_query_nn(pcs[wib].tgt, q.x, q.y, q.z, prm->cap, wss[wib], best, bp);
+    warp_query_nn(pcs[wib].tgt, q.x, q.y, q.z, prm->cap, wss[wib], best, bp, sk, sp);
     if (lane == 0) {
       d->hard_tp[gslot] = make_float4(bp.x, bp.y, bp.z, key_dist(best));
       d->hard_ti[gslot] = key_idx(best);
+      d->prev_ti[gslot] = key_idx(best);
     }
   }
 }
@@ -676,6 +703,10 @@ __global__ void __launch_bounds__(kIcpThreads) k_fitness(const BatchDesc* __rest
     if (!(dx * dx + dy * dy + dz * dz > 16.f * prm->cap)) {
       NN1 v;
       v.init(q.x, q.y, q.z, pv, prm->cap, wss[wib]);
+      unsigned long long sk;
+      float4 sp;
+      prev_candidate(d, prm, gslot, pv, q, sk, sp);
+      v.seed(sk, sp);
       tile_traverse(pcs[wib].tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z),
                     wss[wib]);
       found = v.found();
@@ -958,6 +989,7 @@ void icp_batch_run(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* c
     q.tgt = ti.v;
     q.src_pts = si.v.pts;
     q.tgt_nrm = tgt[i]->nrm;
+    q.tgt_xyz = tgt[i]->xyz;
     q.src_ntiles = si.v.nleaf;
     q.tile0 = tiles;
     q.chunk0 = chunks;
@@ -991,10 +1023,11 @@ void icp_batch_run(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* c
                b_npts = align256(sizeof(int) * npairs), b_part = align256(slots * 4), b_hq = align256(slots * 4),
                b_htp = align256(slots * 16), b_hti = align256(slots * 4), b_wide = align256(sizeof(uint32_t) * tiles),
                b_red = align256(sizeof(double) * 32 * chunks), b_fd = align256(slots * 4),
-               b_far = align256(slots * 16), b_cpart = align256(sizeof(double) * 4 * cchunks);
+               b_far = align256(slots * 16), b_cpart = align256(sizeof(double) * 4 * cchunks),
+               b_prev = align256(slots * 4);
   const size_t hdr = b_prm + b_st + 3 * b_pre + b_xyz + b_npts;
   char* blk = static_cast<char*>(
-      dev_alloc(ctx, hdr + b_part + b_hq + b_htp + b_hti + b_wide + b_red + b_fd + b_far + b_cpart));
+      dev_alloc(ctx, hdr + b_part + b_hq + b_htp + b_hti + b_wide + b_red + b_fd + b_far + b_cpart + b_prev));
   char* cur = blk;
   BatchDesc hd;
   std::memset(&hd, 0, sizeof(hd));
@@ -1019,7 +1052,9 @@ void icp_batch_run(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* c
   hd.red = reinterpret_cast<double*>(cur); cur += b_red;
   hd.fd = reinterpret_cast<float*>(cur); cur += b_fd;
   hd.far = reinterpret_cast<float4*>(cur); cur += b_far;
-  double* d_cpart = reinterpret_cast<double*>(cur);
+  double* d_cpart = reinterpret_cast<double*>(cur); cur += b_cpart;
+  hd.prev_ti = reinterpret_cast<uint32_t*>(cur);
+  CUDA_TRY(cudaMemsetAsync(hd.prev_ti, 0xff, slots * 4, ctx->stream));
 
   // stage everything in one pinned buffer and copy it in one go
   const size_t stage_bytes = hdr + 1024 + 256;

@@ -186,6 +186,16 @@ struct NN1 {
     subtile_setup(x, y, z, v, w);
     refresh();
   }
+  // Starts from a known candidate (warp-collective): the result is still the
+  // exact nearest -- the candidate is one of the points -- but the search
+  // prunes with its distance from the first node on.
+  __device__ __forceinline__ void seed(unsigned long long k, const float4& p) {
+    if (k < best) {
+      best = k;
+      bp = p;
+    }
+    refresh();
+  }
   __device__ __forceinline__ float bound() const { return key_dist(best); }
   __device__ __forceinline__ float metric(const float4& lo, const float4& hi) const {
     return subtile_metric(lo, hi, *ws);
@@ -260,12 +270,17 @@ struct WarpNN {
 };
 
 __device__ __forceinline__ void warp_query_nn(const IndexView& ix, float qx, float qy, float qz, float cap,
-                                              WarpScratch& ws, unsigned long long& best, float4& bp) {
+                                              WarpScratch& ws, unsigned long long& best, float4& bp,
+                                              unsigned long long seed = ~0ull, float4 seed_p = float4()) {
   WarpNN v;
   v.qx = qx; v.qy = qy; v.qz = qz;
   v.best = make_key(cap, 0xffffffffu);
   v.bp = make_float4(0.f, 0.f, 0.f, 0.f);
-  v.R = cap;
+  if (seed < v.best) {  // a known candidate (warp-uniform): exact result, earlier pruning
+    v.best = seed;
+    v.bp = seed_p;
+  }
+  v.R = key_dist(v.best);
   tile_traverse(ix, v, qx, qy, qz, ws);
   best = v.best;
   bp = v.bp;

@@ -230,10 +230,11 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     # StatisticalOutlierRemoval, k = 51 including the point itself): its launches
     # are bracketed by CUDA events on the library's stream during the timed
     # region.  Algorithmic bytes per launch on n points in nleaf leaves of 32:
-    # query points 16 n + reference points 16 n + leaf boxes 32 nleaf + output
-    # (mean distance 4 B + valid flag 1 B) 5 n.
+    # query points 16 n + reference points 16 n + leaf boxes 32 nleaf + outputs:
+    # mean distance 4 B + valid flag 1 B + the 51 neighbour keys handed to the
+    # inliers' normals (8 B each) per point.
     def sor_bytes(n: int) -> int:
-        return 37 * n + 32 * ((n + 31) // 32)
+        return (37 + 51 * 8) * n + 32 * ((n + 31) // 32)
     assert sor_launches == len(sor_sizes), (sor_launches, len(sor_sizes))
     bytes_per_launch = sum(sor_bytes(n) for n in sor_sizes) / max(1, len(sor_sizes))
     launch_ms = sor_ms / max(1, sor_launches)

@@ -234,7 +234,19 @@ def turntable_cycle(seed: int = 2, views: int = 36, step_deg: float = 10.0, fram
     overlap by 360/views degrees less than a full turn, so each pair sees part
     of the surface the other does not (self-occlusion)."""
     rng = np.random.default_rng(seed)
+    # a seeded superquadric with a block and two balls attached around it: a
+    # lone superquadric is often nearly symmetric about some axis, which leaves
+    # ICP a sliding direction
     obj = superquadric_object(rng)
+    sq = obj[0]
+    a0 = rng.uniform(0, 360)
+    r = sq.axes.max()
+    for k, (dy, size) in enumerate(((-0.02, 0.03), (0.03, 0.025), (-0.05, 0.035))):
+        side = rot_y(a0 + 120.0 * k)
+        if k == 0:
+            obj.append(Box(sq.center + side @ np.array([r + 0.03, dy, 0.0]), np.array([0.03, 0.05, 0.02]), side))
+        else:
+            obj.append(Sphere(sq.center + side @ np.array([r + 0.02, dy, 0.0]), size))
     caps, poses = [], []
     for v in range(views):
         T = turntable(step_deg * v, OBJECT_AXIS)

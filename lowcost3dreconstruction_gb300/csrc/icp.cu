@@ -734,19 +734,33 @@ __global__ void __launch_bounds__(kIcpThreads) k_fitness_far(const BatchDesc* __
   if (lane == 0) pcs[wib].pair = -1;
   __syncwarp();
   const unsigned nfar = vload(&cnt->nfar);
+  constexpr unsigned kRun = 8;  // consecutive queue entries per grab: neighbours of one tile
   for (;;) {
-    unsigned i = 0;
-    if (lane == 0) i = atomicAdd(&cnt->far_ctr, 1u);
-    i = __shfl_sync(LCR_FULL, i, 0);
-    if (i >= nfar) break;
-    const float4 q = d->far[i];
-    const int gslot = __float_as_int(q.w);
-    const int p = pair_of(d->tile0, d->npairs, gslot >> 5);
-    cache_pair(pcs[wib], d, p, lane);
-    unsigned long long best;
-    float4 bp;
-    warp_query_nn(pcs[wib].tgt, q.x, q.y, q.z, LCR_INF, wss[wib], best, bp);
-    if (lane == 0) d->fd[gslot] = key_dist(best);
+    unsigned i0 = 0;
+    if (lane == 0) i0 = atomicAdd(&cnt->far_ctr, kRun);
+    i0 = __shfl_sync(LCR_FULL, i0, 0);
+    if (i0 >= nfar) break;
+    // each query starts from the previous query's nearest point (same pair):
+    // an exact search with a near bound from the first node on
+    unsigned long long prev_key = ~0ull;
+    float4 prev_p = make_float4(0.f, 0.f, 0.f, 0.f);
+    int prev_pair = -1;
+    for (unsigned i = i0; i < min(nfar, i0 + kRun); ++i) {
+      const float4 q = d->far[i];
+      const int gslot = __float_as_int(q.w);
+      const int p = pair_of(d->tile0, d->npairs, gslot >> 5);
+      cache_pair(pcs[wib], d, p, lane);
+      unsigned long long seed = ~0ull;
+      if (p == prev_pair && prev_key != ~0ull)
+        seed = make_key(exact_dist2(q.x, q.y, q.z, prev_p.x, prev_p.y, prev_p.z), key_idx(prev_key));
+      unsigned long long best;
+      float4 bp;
+      warp_query_nn(pcs[wib].tgt, q.x, q.y, q.z, LCR_INF, wss[wib], best, bp, seed, prev_p);
+      if (lane == 0) d->fd[gslot] = key_dist(best);
+      prev_key = best;
+      prev_p = bp;
+      prev_pair = p;
+    }
   }
 }
 

@@ -158,36 +158,58 @@ __global__ void k_sor_dist_sorted(IndexView ix, int mean_k, float* __restrict__ 
   }
 }
 
-// Fixed blocked order: chunks of 256 consecutive terms summed sequentially
-// from 0.0 (level 0 sums d and float(d*d)), repeated until one value remains.
+// Fixed blocked order, one warp per chunk of 256 consecutive terms: lane l
+// adds terms 8l .. 8l+7 of the chunk in order from 0.0, then the lanes combine
+// by the xor butterfly 16, 8, 4, 2, 1 and lane 0's value is the chunk's sum
+// (level 0 sums d and float(d*d)); repeated until one value remains.
+__device__ __forceinline__ double butterfly_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(LCR_FULL, v, o));
+  return v;
+}
+
 __global__ void k_bsum_level0(const float* __restrict__ d, int n, double* __restrict__ oa, double* __restrict__ ob) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int b = c * 256;
   if (b >= n) return;
-  const int e = min(n, b + 256);
   double sa = 0.0, sb = 0.0;
-  for (int i = b; i < e; ++i) {
-    const float v = d[i];
-    sa = __dadd_rn(sa, static_cast<double>(v));
-    sb = __dadd_rn(sb, static_cast<double>(__fmul_rn(v, v)));
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int i = b + lane * 8 + j;
+    if (i < n) {
+      const float v = d[i];
+      sa = __dadd_rn(sa, static_cast<double>(v));
+      sb = __dadd_rn(sb, static_cast<double>(__fmul_rn(v, v)));
+    }
   }
-  oa[c] = sa;
-  ob[c] = sb;
+  sa = butterfly_sum(sa);
+  sb = butterfly_sum(sb);
+  if (lane == 0) {
+    oa[c] = sa;
+    ob[c] = sb;
+  }
 }
 
 __global__ void k_bsum_level(const double* __restrict__ a, const double* __restrict__ b, int n,
                              double* __restrict__ oa, double* __restrict__ ob) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  const int s = c * 256;
-  if (s >= n) return;
-  const int e = min(n, s + 256);
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int s0 = c * 256;
+  if (s0 >= n) return;
   double sa = 0.0, sb = 0.0;
-  for (int i = s; i < e; ++i) {
-    sa = __dadd_rn(sa, a[i]);
-    sb = __dadd_rn(sb, b[i]);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int i = s0 + lane * 8 + j;
+    if (i < n) {
+      sa = __dadd_rn(sa, a[i]);
+      sb = __dadd_rn(sb, b[i]);
+    }
   }
-  oa[c] = sa;
-  ob[c] = sb;
+  sa = butterfly_sum(sa);
+  sb = butterfly_sum(sb);
+  if (lane == 0) {
+    oa[c] = sa;
+    ob[c] = sb;
+  }
 }
 
 // mean = sum/nv; variance = (sq - sum*sum/nv)/(nv-1); threshold = mean + mul*stddev.
@@ -644,10 +666,10 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
   // blocked sums (ping-pong between two halves of `sums`)
   double *a = sums, *b = sums + nc0, *a2 = sums + 2 * nc0, *b2 = sums + 3 * nc0;
   int m = nc0;
-  LCR_LAUNCH(ctx, k_bsum_level0, (m + 127) / 128, 128, 0, dist, n, a, b);
+  LCR_LAUNCH(ctx, k_bsum_level0, (m + 7) / 8, 256, 0, dist, n, a, b);  // a warp per chunk
   while (m > 1) {
     const int m2 = (m + 255) / 256;
-    LCR_LAUNCH(ctx, k_bsum_level, (m2 + 127) / 128, 128, 0, a, b, m, a2, b2);
+    LCR_LAUNCH(ctx, k_bsum_level, (m2 + 7) / 8, 256, 0, a, b, m, a2, b2);
     std::swap(a, a2);
     std::swap(b, b2);
     m = m2;

@@ -153,15 +153,31 @@ float float_cap(double v) {
 
 /* Fixed blocked summation order shared with the GPU reduction: blocks of 256
  * consecutive terms summed sequentially from 0.0, repeated until one value. */
+/* The GPU's fixed order (the reference sums sequentially; the order only
+ * moves the last bits of the SOR mean/stddev): chunks of 256 consecutive
+ * terms; within a chunk, 32 partial sums p[l] of terms 8l..8l+7 in order from
+ * 0.0, combined by the xor butterfly p[l] += p[l ^ o] for o = 16, 8, 4, 2, 1;
+ * the chunk's sum is p[0].  Repeated until one value remains. */
 double blocked_sum(std::vector<double> v) {
   if (v.empty()) return 0.0;
   while (v.size() > 1) {
     std::vector<double> next((v.size() + 255) / 256, 0.0);
     for (size_t b = 0; b < next.size(); ++b) {
-      double s = 0.0;
-      size_t e = std::min(v.size(), (b + 1) * 256);
-      for (size_t i = b * 256; i < e; ++i) s += v[i];
-      next[b] = s;
+      double p[32];
+      for (int l = 0; l < 32; ++l) {
+        double s = 0.0;
+        for (int j = 0; j < 8; ++j) {
+          const size_t i = b * 256 + static_cast<size_t>(l) * 8 + j;
+          if (i < v.size()) s += v[i];
+        }
+        p[l] = s;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        double q[32];
+        for (int l = 0; l < 32; ++l) q[l] = p[l] + p[l ^ o];
+        for (int l = 0; l < 32; ++l) p[l] = q[l];
+      }
+      next[b] = p[0];
     }
     v.swap(next);
   }

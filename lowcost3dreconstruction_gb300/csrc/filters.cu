@@ -766,6 +766,11 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
     LCR_LAUNCH(ctx, k_normals_queued, ctx->sms * 2, kSetWarps * 32, smem_set, ix, k, in->xyz, vp[0], vp[1], vp[2],
                flip, out->nrm, queue, nq, h->keys, h->K, h->kept, pos);
     dev_free(ctx, tmp);
+    // the lists (8 B x (k+1) per point) are released once consumed: a second
+    // normals call on this cloud searches
+    dev_free(ctx, h->block);
+    delete h;
+    const_cast<lcr_cloud*>(in)->nbr = nullptr;
     out->index = share_index(in->index);
     return out;
   }

@@ -73,8 +73,9 @@ struct Index {
 // Removal found for every input point, handed to its inlier cloud: the k'
 // nearest inliers of an inlier are the first k' inliers of its list whenever
 // the list holds at least k' of them, so NormalEstimation on the inliers can
-// select instead of searching again.  One allocation: keys, then keep flags,
-// rank (input index -> inlier index), kept (inlier index -> input index).
+// select instead of searching again (the first normals call on the cloud
+// consumes and releases them).  One allocation: keys, then keep flags, rank
+// (input index -> inlier index), kept (inlier index -> input index).
 struct NbrHint {
   void* block = nullptr;
   const unsigned long long* keys;  // [n_src][K]

@@ -307,6 +307,27 @@ def test_normals_of_sor_inliers_from_neighbour_lists(ctx, cfg0, k):
     assert np.percentile(np.arccos(np.clip(cos[ok], -1, 1)), 99.9) < 1e-3
 
 
+def test_normals_of_sor_inliers_without_usable_lists(ctx, cfg0):
+    # SOR k=10 hands lists of 11 keys: they cannot serve normals k=30 (searched),
+    # they serve k=8 once (consumed), and a second k=8 call searches
+    pts = cfg0["vsrc"]
+    inl, _, _ = ctx.sor(ctx.upload(pts), 10, 1.0)
+    _, okeep, _ = O.sor(pts, 10, 1.0)
+
+    def check(g, k):
+        o = O.normals(pts[okeep], k)
+        ng, no = normals_of(g).astype(np.float64), normals_of(o).astype(np.float64)
+        ok = o["curvature"] < 0.2
+        ang = np.arccos(np.clip(np.abs(np.sum(ng * no, axis=1)[ok]), -1, 1))
+        assert np.percentile(ang, 99.9) < 1e-3, (k, np.percentile(ang, 99.9))
+
+    check(ctx.normals(inl, 30).download(), 30)
+    listed = ctx.normals(inl, 8).download()
+    searched = ctx.normals(inl, 8).download()
+    check(listed, 8)
+    check(searched, 8)
+
+
 def test_normals_plane_known_answer(ctx):
     rng = np.random.default_rng(5)
     xy = rng.uniform(-0.1, 0.1, size=(4000, 2))

@@ -352,7 +352,7 @@ __device__ __forceinline__ void tile_nn1(const IndexView& ix, float qx, float qy
 // The result is the exact first k keys in (distance, index) order, in
 // list[j*32 + lane], j < k.
 constexpr int kLeafList = 192;
-constexpr int kBins = 64;
+constexpr int kBins = 64;  // 16 octaves of d^2, 8 of distance
 
 __host__ __device__ constexpr int knn_buffer(int K) { return K + 32; }
 
@@ -631,7 +631,9 @@ __device__ __forceinline__ void tile_knn(const IndexView& ix, float qx, float qy
 // accumulator and buffers the boundary keys, from which the m smallest are
 // selected exactly.  No per-lane sorted list: about half the shared memory of
 // tile_knn and no O(k^2) sort.
-constexpr int kBoundCap = 32;
+constexpr int kBoundCap = 32;  // boundary keys kept per lane: 8 KB per warp, as the histogram
+constexpr int kRefineBits = 6;  // a refinement pass splits the boundary range into 64 sub-ranges
+static_assert((1 << kRefineBits) <= kBins, "refinement sub-ranges must fit the histogram region");
 
 __host__ __device__ inline size_t kset_warp_bytes() {
   const size_t buf = static_cast<size_t>(kBoundCap) * 32 * 8;
@@ -756,19 +758,20 @@ __device__ __forceinline__ void tile_kset(const IndexView& ix, float qx, float q
     r.qx = qx; r.qy = qy; r.qz = qz; r.qv = qv;
     r.active = cnt > kBoundCap;
     r.lane = lane;
-    const unsigned long long span = khi - klo;  // >= cnt - 1 >= 32: keys are unique
-    r.sh = r.active ? max(0, 64 - __clzll(static_cast<long long>(span)) - 6) : 0;
+    const unsigned long long span = khi - klo;  // >= cnt - 1 >= kBoundCap: keys are unique
+    // (k - klo) >> sh <= span >> sh < 2^kRefineBits
+    r.sh = r.active ? max(0, 64 - __clzll(static_cast<long long>(span)) - kRefineBits) : 0;
     r.klo = klo; r.khi = khi;
     r.tau = r.active ? range_tau(khi) : -1.f;
     r.hist = hist;
     r.ws = &kw.ws;
     r.R = subtile_radius(r.tau, r.active, kw.ws);
-    for (int b = 0; b < kBins; ++b) hist[b * 32 + lane] = 0u;
+    for (int b = 0; b < (1 << kRefineBits); ++b) hist[b * 32 + lane] = 0u;
     __syncwarp();
     knn_pass2(ix, h, r, tlo, thi, kw);
     if (r.active) {
       int c = 0;
-      for (int j = 0; j < kBins; ++j) {
+      for (int j = 0; j < (1 << kRefineBits); ++j) {
         const int hj = static_cast<int>(hist[j * 32 + lane]);
         if (c + hj >= m) {
           const unsigned long long lo = klo + (static_cast<unsigned long long>(j) << r.sh);

@@ -81,7 +81,7 @@ LCR_API uint64_t lcr_ctx_launch_count(const lcr_ctx* ctx);
  * events on the context's stream; lcr_kernel_time synchronises the stream and
  * returns the summed device time and launch count since timing was enabled.
  * lcr_kernel_timing(ctx, 1) also resets the sums. */
-enum { LCR_KT_SOR_KNN = 0, LCR_KT_NORMALS_KNN = 1, LCR_KT_COUNT = 2 };
+enum { LCR_KT_SOR_KNN = 0, LCR_KT_NORMALS_KNN = 1, LCR_KT_ENCODE = 2, LCR_KT_COUNT = 3 };
 LCR_API lcr_status lcr_kernel_timing(lcr_ctx* ctx, int enable);
 LCR_API lcr_status lcr_kernel_time(lcr_ctx* ctx, int which, double* ms, uint64_t* launches);
 
@@ -237,6 +237,56 @@ LCR_API lcr_status lcr_correspondences(lcr_ctx* ctx, const lcr_cloud* src, const
  * uncapped.  Host outputs n_query*k, missing entries idx -1, dist +inf. */
 LCR_API lcr_status lcr_knn(lcr_ctx* ctx, const lcr_cloud* ref, const lcr_cloud* query, int k, float max_dist_sq,
                            int32_t* idx, float* dist);
+
+/* ------------------------------------------------- learned pose proposal */
+/* A shared-MLP point encoder (3 -> 64 -> 128 -> 1024 with ReLU, max over
+ * LCR_POSENET_POINTS points sampled from each cloud, centred on its centroid
+ * and scaled by 4/m) and a pair head (2048 -> 512 -> 256 -> 9: the first two
+ * columns of R and a residual translation) propose the source-to-target
+ * transform ICP starts from, in place of centroid_align's guess
+ * (pcl_tools/centroid_align.cpp:102-130, alignment.sh:106-113).  bf16 weights
+ * and activations with fp32 accumulation (the encoder on the tensor cores);
+ * fp32 master weights, gradients and AdamW state, all on the GPU.  The
+ * reference has no learned component: this is an addition beside the plain
+ * path, which it leaves unchanged.  Parameters are one fp32 vector of
+ * LCR_POSENET_PARAMS values: W1[64][3] b1 W2[128][64] b2 W3[1024][128] b3
+ * H1[512][2048] c1 H2[256][512] c2 H3[9][256] c3 (row-major [out][in]). */
+#define LCR_POSENET_PARAMS 1323401
+#define LCR_POSENET_POINTS 1024
+typedef struct lcr_posenet lcr_posenet;
+typedef struct lcr_adamw_params {
+  float lr, beta1, beta2, eps, weight_decay;
+} lcr_adamw_params;
+
+/* He-uniform initialisation from seed. */
+LCR_API lcr_status lcr_posenet_create(lcr_ctx* ctx, uint64_t seed, lcr_posenet** net);
+LCR_API lcr_status lcr_posenet_free(lcr_ctx* ctx, lcr_posenet* net);
+/* Host copies of the fp32 parameter vector (LCR_POSENET_PARAMS floats). */
+LCR_API lcr_status lcr_posenet_get_params(lcr_ctx* ctx, const lcr_posenet* net, float* params);
+LCR_API lcr_status lcr_posenet_set_params(lcr_ctx* ctx, lcr_posenet* net, const float* params);
+/* The network input of n clouds: pts [n][LCR_POSENET_POINTS][4] (x y z 0,
+ * centred, scaled, bf16-valued) and centroids [n][3] (FP64), either may be NULL. */
+LCR_API lcr_status lcr_posenet_sample(lcr_ctx* ctx, const lcr_cloud* const* clouds, size_t n, uint64_t seed,
+                                      float* pts, double* centroids);
+/* Forward pass on sampled input: pts [2*npairs][POINTS][4], the npairs source
+ * clouds then the npairs target clouds.  Outputs (each may be NULL):
+ * features [2*npairs][1024] pooled encoder outputs, argmax [2*npairs][1024]
+ * winning point per channel (train = 1 only), out [npairs][9]. */
+LCR_API lcr_status lcr_posenet_forward(lcr_ctx* ctx, lcr_posenet* net, const float* pts, size_t npairs, int train,
+                                       float* features, int32_t* argmax, float* out);
+/* Loss (mean over pairs of the squared error of the 9 outputs against labels
+ * [npairs][9]) and its gradient (LCR_POSENET_PARAMS floats), no update. */
+LCR_API lcr_status lcr_posenet_gradients(lcr_ctx* ctx, lcr_posenet* net, const float* pts, const float* labels,
+                                         size_t npairs, float* loss, float* grads);
+/* One AdamW step on a batch of pairs whose source-to-target transforms are
+ * known (transforms [npairs][16], row-major). */
+LCR_API lcr_status lcr_posenet_train_step(lcr_ctx* ctx, lcr_posenet* net, const lcr_cloud* const* src,
+                                          const lcr_cloud* const* tgt, const float* transforms, size_t npairs,
+                                          uint64_t seed, const lcr_adamw_params* opt, float* loss);
+/* Proposed source-to-target transforms, guesses [npairs][16] row-major: the
+ * input lcr_icp_batch takes. */
+LCR_API lcr_status lcr_posenet_propose(lcr_ctx* ctx, lcr_posenet* net, const lcr_cloud* const* src,
+                                       const lcr_cloud* const* tgt, size_t npairs, uint64_t seed, float* guesses);
 
 /* ------------------------------------------------------------ accumulate */
 enum { LCR_ACCUM_ALL = 1 };

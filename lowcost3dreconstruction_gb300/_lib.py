@@ -60,7 +60,8 @@ class SorStats(C.Structure):
                 ("valid", C.c_size_t), ("kept", C.c_size_t), ("removed", C.c_size_t)]
 
 
-KT_SOR_KNN, KT_NORMALS_KNN = 0, 1
+KT_SOR_KNN, KT_NORMALS_KNN, KT_ENCODE = 0, 1, 2
+POSENET_PARAMS, POSENET_POINTS = 1323401, 1024
 
 
 class IcpParams(C.Structure):
@@ -73,6 +74,11 @@ class IcpResult(C.Structure):
     _fields_ = [("transform", C.c_float * 16), ("transform64", C.c_double * 16), ("converged", C.c_int),
                 ("iterations", C.c_int), ("state", C.c_int), ("n_correspondences", C.c_int),
                 ("fitness", C.c_double), ("mse", C.c_double)]
+
+
+class AdamwParams(C.Structure):
+    _fields_ = [("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
+                ("weight_decay", C.c_float)]
 
 
 _VP = C.c_void_p
@@ -113,6 +119,16 @@ _SIGS = {
     "lcr_centroid": (C.c_int, [_VP, _VP, _VP]),
     "lcr_centroid_align": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_double, C.c_double, C.c_double,
                                      C.POINTER(_VP), _VP]),
+    "lcr_posenet_create": (C.c_int, [_VP, C.c_uint64, C.POINTER(_VP)]),
+    "lcr_posenet_free": (C.c_int, [_VP, _VP]),
+    "lcr_posenet_get_params": (C.c_int, [_VP, _VP, _VP]),
+    "lcr_posenet_set_params": (C.c_int, [_VP, _VP, _VP]),
+    "lcr_posenet_sample": (C.c_int, [_VP, _VP, C.c_size_t, C.c_uint64, _VP, _VP]),
+    "lcr_posenet_forward": (C.c_int, [_VP, _VP, _VP, C.c_size_t, C.c_int, _VP, _VP, _VP]),
+    "lcr_posenet_gradients": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, _VP, _VP]),
+    "lcr_posenet_train_step": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_size_t, C.c_uint64, C.POINTER(AdamwParams),
+                                         _VP]),
+    "lcr_posenet_propose": (C.c_int, [_VP, _VP, _VP, _VP, C.c_size_t, C.c_uint64, _VP]),
     "lcr_ply_read": (C.c_int, [C.c_char_p, C.POINTER(_VP), C.POINTER(C.c_size_t)]),
     "lcr_ply_write": (C.c_int, [C.c_char_p, _VP, C.c_size_t, C.c_int]),
     "lcr_ply_last_error": (C.c_char_p, []),

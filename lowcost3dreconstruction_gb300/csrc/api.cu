@@ -6,6 +6,7 @@
 #include <new>
 
 #include "lcr_internal.cuh"
+#include "posenet.cuh"
 
 namespace {
 
@@ -521,6 +522,192 @@ lcr_status lcr_centroid_align(lcr_ctx* ctx, const lcr_cloud* src, const lcr_clou
   *out = transform_run(ctx, src, m);
   if (transform) std::memcpy(transform, m, sizeof(m));
   sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ pose proposal
+namespace {
+
+std::vector<posenet::CloudRef> cloud_refs(const lcr_cloud* const* a, const lcr_cloud* const* b, size_t n) {
+  std::vector<posenet::CloudRef> r;
+  r.reserve(b ? 2 * n : n);
+  for (size_t i = 0; i < n; ++i) {
+    if (!a[i]) LCR_THROW(LCR_ERR_INVALID_ARG, "null cloud %zu", i);
+    r.push_back({a[i]->xyz, static_cast<long long>(a[i]->n)});
+  }
+  if (b)
+    for (size_t i = 0; i < n; ++i) {
+      if (!b[i]) LCR_THROW(LCR_ERR_INVALID_ARG, "null target cloud %zu", i);
+      r.push_back({b[i]->xyz, static_cast<long long>(b[i]->n)});
+    }
+  return r;
+}
+
+void h2d(lcr_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  if (bytes) CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+}
+
+void d2h(lcr_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  if (dst && bytes) CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+}
+
+constexpr size_t kMaxPairs = 1u << 16;
+
+}  // namespace
+
+extern "C" {
+
+lcr_status lcr_posenet_create(lcr_ctx* ctx, uint64_t seed, lcr_posenet** net) {
+  API_BEGIN(ctx)
+  REQUIRE(net, "null argument");
+  *net = nullptr;
+  auto* n = new lcr_posenet();
+  try {
+    posenet::create(ctx, n, seed);
+    sync(ctx);
+  } catch (...) {
+    if (n->block) dev_free(ctx, n->block);
+    delete n;
+    throw;
+  }
+  *net = n;
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_posenet_free(lcr_ctx* ctx, lcr_posenet* net) {
+  API_BEGIN(ctx)
+  if (net) {
+    posenet::destroy(ctx, net);
+    sync(ctx);
+    delete net;
+  }
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_posenet_get_params(lcr_ctx* ctx, const lcr_posenet* net, float* params) {
+  API_BEGIN(ctx)
+  REQUIRE(net && params, "null argument");
+  d2h(ctx, params, net->w, posenet::kParams * sizeof(float));
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_posenet_set_params(lcr_ctx* ctx, lcr_posenet* net, const float* params) {
+  API_BEGIN(ctx)
+  REQUIRE(net && params, "null argument");
+  h2d(ctx, net->w, params, posenet::kParams * sizeof(float));
+  posenet::pack(ctx, net);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_posenet_sample(lcr_ctx* ctx, const lcr_cloud* const* clouds, size_t n, uint64_t seed, float* pts,
+                              double* centroids) {
+  API_BEGIN(ctx)
+  REQUIRE(n == 0 || clouds, "null argument");
+  REQUIRE(n <= 2 * kMaxPairs, "too many clouds (%zu)", n);
+  if (n) {
+    const auto refs = cloud_refs(clouds, nullptr, n);
+    char* d = static_cast<char*>(dev_alloc(ctx, n * (sizeof(posenet::CloudRef) + posenet::kPts * 16 + 24)));
+    auto* dr = reinterpret_cast<posenet::CloudRef*>(d);
+    auto* dp = reinterpret_cast<float4*>(d + n * sizeof(posenet::CloudRef));
+    auto* dc = reinterpret_cast<double*>(d + n * (sizeof(posenet::CloudRef) + posenet::kPts * 16));
+    h2d(ctx, dr, refs.data(), n * sizeof(posenet::CloudRef));
+    posenet::sample(ctx, dr, static_cast<int>(n), seed, dp, dc);
+    d2h(ctx, pts, dp, n * posenet::kPts * 16);
+    d2h(ctx, centroids, dc, n * 24);
+    sync(ctx);
+    dev_free(ctx, d);
+  }
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_posenet_forward(lcr_ctx* ctx, lcr_posenet* net, const float* pts, size_t npairs, int train,
+                               float* features, int32_t* argmax, float* out) {
+  API_BEGIN(ctx)
+  REQUIRE(net && (npairs == 0 || pts), "null argument");
+  REQUIRE(npairs <= kMaxPairs, "too many pairs (%zu)", npairs);
+  if (npairs) {
+    const auto b = posenet::batch(ctx, net, static_cast<int>(npairs), train != 0);
+    h2d(ctx, b.pts, pts, 2 * npairs * posenet::kPts * 16);
+    posenet::encode(ctx, net, b, train != 0);
+    posenet::head_forward(ctx, net, b);
+    d2h(ctx, features, b.feat, 2 * npairs * posenet::kF3 * 4);
+    if (train) d2h(ctx, argmax, b.argmax, 2 * npairs * posenet::kF3 * 4);
+    d2h(ctx, out, b.y, npairs * posenet::kOut * 4);
+    posenet::check_error(ctx, net);
+  }
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_posenet_gradients(lcr_ctx* ctx, lcr_posenet* net, const float* pts, const float* labels, size_t npairs,
+                                 float* loss, float* grads) {
+  API_BEGIN(ctx)
+  REQUIRE(net && pts && labels && npairs > 0, "null argument or empty batch");
+  REQUIRE(npairs <= kMaxPairs, "too many pairs (%zu)", npairs);
+  const auto b = posenet::batch(ctx, net, static_cast<int>(npairs), true);
+  h2d(ctx, b.pts, pts, 2 * npairs * posenet::kPts * 16);
+  h2d(ctx, b.labels, labels, npairs * posenet::kOut * 4);
+  posenet::encode(ctx, net, b, true);
+  posenet::head_forward(ctx, net, b);
+  posenet::loss_backward(ctx, net, b);
+  d2h(ctx, loss, b.loss, 4);
+  d2h(ctx, grads, net->grad, posenet::kParams * 4);
+  posenet::check_error(ctx, net);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_posenet_train_step(lcr_ctx* ctx, lcr_posenet* net, const lcr_cloud* const* src,
+                                  const lcr_cloud* const* tgt, const float* transforms, size_t npairs, uint64_t seed,
+                                  const lcr_adamw_params* opt, float* loss) {
+  API_BEGIN(ctx)
+  REQUIRE(net && src && tgt && transforms && opt && npairs > 0, "null argument or empty batch");
+  REQUIRE(npairs <= kMaxPairs, "too many pairs (%zu)", npairs);
+  REQUIRE(opt->lr >= 0.f && opt->beta1 >= 0.f && opt->beta1 < 1.f && opt->beta2 >= 0.f && opt->beta2 < 1.f &&
+              opt->eps > 0.f && opt->weight_decay >= 0.f,
+          "bad AdamW parameters");
+  const auto refs = cloud_refs(src, tgt, npairs);
+  const auto b = posenet::batch(ctx, net, static_cast<int>(npairs), true);
+  h2d(ctx, b.refs, refs.data(), refs.size() * sizeof(posenet::CloudRef));
+  h2d(ctx, b.guess, transforms, npairs * 16 * 4);
+  posenet::sample(ctx, b.refs, static_cast<int>(2 * npairs), seed, b.pts, b.cen);
+  posenet::labels_from_poses(ctx, b, b.guess);
+  posenet::encode(ctx, net, b, true);
+  posenet::head_forward(ctx, net, b);
+  posenet::loss_backward(ctx, net, b);
+  posenet::adamw(ctx, net, opt);
+  d2h(ctx, loss, b.loss, 4);
+  posenet::check_error(ctx, net);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_posenet_propose(lcr_ctx* ctx, lcr_posenet* net, const lcr_cloud* const* src,
+                               const lcr_cloud* const* tgt, size_t npairs, uint64_t seed, float* guesses) {
+  API_BEGIN(ctx)
+  REQUIRE(net && (npairs == 0 || (src && tgt && guesses)), "null argument");
+  REQUIRE(npairs <= kMaxPairs, "too many pairs (%zu)", npairs);
+  if (npairs) {
+    const auto refs = cloud_refs(src, tgt, npairs);
+    const auto b = posenet::batch(ctx, net, static_cast<int>(npairs), false);
+    h2d(ctx, b.refs, refs.data(), refs.size() * sizeof(posenet::CloudRef));
+    posenet::sample(ctx, b.refs, static_cast<int>(2 * npairs), seed, b.pts, b.cen);
+    posenet::encode(ctx, net, b, false);
+    posenet::head_forward(ctx, net, b);
+    posenet::poses(ctx, b);
+    d2h(ctx, guesses, b.guess, npairs * 16 * 4);
+    posenet::check_error(ctx, net);
+  }
   API_END(ctx)
   return LCR_OK;
 }

@@ -238,6 +238,30 @@ LCR_API lcr_status lcr_correspondences(lcr_ctx* ctx, const lcr_cloud* src, const
 LCR_API lcr_status lcr_knn(lcr_ctx* ctx, const lcr_cloud* ref, const lcr_cloud* query, int k, float max_dist_sq,
                            int32_t* idx, float* dist);
 
+/* ------------------------------------------------ synthetic capture pairs */
+/* Seeded capture pairs generated on the GPU (training and evaluation data of
+ * the pose proposal): a superquadric object (semi-axes 0.05-0.2 m, exponents
+ * 0.3-1.5) with a block and two balls attached, 1 m in front of the camera;
+ * `points` visible surface samples per view (back-facing and covered points
+ * dropped) with normals, depth noise sigma = 1.5 mm (z/1 m)^2 when noise is
+ * set.  The target view moves the object about its centre by a yaw uniform
+ * in +-yaw_deg, a tilt uniform in +-tilt_deg and a translation uniform in
+ * +-translation (m) per axis; transforms [npairs][16] receives the exact
+ * source-to-target transform (row-major).  npairs <= 65535. */
+typedef struct lcr_synth_params {
+  float yaw_deg, tilt_deg, translation;
+  int noise;
+} lcr_synth_params;
+LCR_API lcr_status lcr_synthetic_pairs(lcr_ctx* ctx, uint64_t seed, size_t npairs, int points,
+                                       const lcr_synth_params* p, lcr_cloud** src, lcr_cloud** tgt,
+                                       float* transforms);
+
+/* Alignment error of n clouds: out[i] = RMS over the finite points p of
+ * clouds[i] of |Ta_i p - Tb_i p| (FP64; Ta, Tb [n][16] row-major), the RMSE
+ * by which a pair counts as aligned (estimate vs ground truth). */
+LCR_API lcr_status lcr_rmse_batch(lcr_ctx* ctx, const lcr_cloud* const* clouds, size_t n, const double* Ta,
+                                  const double* Tb, double* out);
+
 /* ------------------------------------------------- learned pose proposal */
 /* A shared-MLP point encoder (3 -> 64 -> 128 -> 1024 with ReLU, max over
  * LCR_POSENET_POINTS points sampled from each cloud, centred on its centroid

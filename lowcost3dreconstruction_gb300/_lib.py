@@ -81,6 +81,10 @@ class AdamwParams(C.Structure):
                 ("weight_decay", C.c_float)]
 
 
+class SynthParams(C.Structure):
+    _fields_ = [("yaw_deg", C.c_float), ("tilt_deg", C.c_float), ("translation", C.c_float), ("noise", C.c_int)]
+
+
 _VP = C.c_void_p
 _SIGS = {
     "lcr_ctx_create": (C.c_int, [C.POINTER(_VP), C.c_int]),
@@ -119,6 +123,9 @@ _SIGS = {
     "lcr_centroid": (C.c_int, [_VP, _VP, _VP]),
     "lcr_centroid_align": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_double, C.c_double, C.c_double,
                                      C.POINTER(_VP), _VP]),
+    "lcr_synthetic_pairs": (C.c_int, [_VP, C.c_uint64, C.c_size_t, C.c_int, C.POINTER(SynthParams), _VP, _VP,
+                                      _VP]),
+    "lcr_rmse_batch": (C.c_int, [_VP, _VP, C.c_size_t, _VP, _VP, _VP]),
     "lcr_posenet_create": (C.c_int, [_VP, C.c_uint64, C.POINTER(_VP)]),
     "lcr_posenet_free": (C.c_int, [_VP, _VP]),
     "lcr_posenet_get_params": (C.c_int, [_VP, _VP, _VP]),

@@ -291,3 +291,25 @@ class Context:
         self._check(self.lib.lcr_centroid_align(self.h, src.handle, tgt.handle, roll, pitch, yaw, elevation,
                                                 C.byref(out), L.ptr(m)))
         return Cloud(self, out), m.reshape(4, 4)
+
+    # ------------------------------------------------- synthetic capture pairs
+    def synthetic_pairs(self, seed: int, npairs: int, points: int, yaw_deg: float = 180.0, tilt_deg: float = 20.0,
+                        translation: float = 0.1, noise: bool = True) -> tuple[list[Cloud], list[Cloud], np.ndarray]:
+        """lcr_synthetic_pairs: (sources, targets, exact source-to-target transforms [n][4][4])."""
+        hs = (C.c_void_p * max(npairs, 1))()
+        ht = (C.c_void_p * max(npairs, 1))()
+        T = np.zeros((max(npairs, 1), 16), dtype=np.float32)
+        p = L.SynthParams(yaw_deg, tilt_deg, translation, 1 if noise else 0)
+        self._check(self.lib.lcr_synthetic_pairs(self.h, seed, npairs, points, C.byref(p), hs, ht, L.ptr(T)))
+        return ([Cloud(self, C.c_void_p(hs[i])) for i in range(npairs)],
+                [Cloud(self, C.c_void_p(ht[i])) for i in range(npairs)], T[:npairs].reshape(npairs, 4, 4))
+
+    def rmse_batch(self, clouds: list[Cloud], Ta: np.ndarray, Tb: np.ndarray) -> np.ndarray:
+        """lcr_rmse_batch: RMS over each cloud's points of |Ta p - Tb p|."""
+        n = len(clouds)
+        a = np.ascontiguousarray(Ta, dtype=np.float64).reshape(n * 16)
+        b = np.ascontiguousarray(Tb, dtype=np.float64).reshape(n * 16)
+        out = np.zeros(max(n, 1), dtype=np.float64)
+        hs = (C.c_void_p * max(n, 1))(*[c.handle for c in clouds])
+        self._check(self.lib.lcr_rmse_batch(self.h, hs, n, L.ptr(a), L.ptr(b), L.ptr(out)))
+        return out[:n]

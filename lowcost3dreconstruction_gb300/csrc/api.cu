@@ -560,6 +560,39 @@ constexpr size_t kMaxPairs = 1u << 16;
 
 extern "C" {
 
+lcr_status lcr_synthetic_pairs(lcr_ctx* ctx, uint64_t seed, size_t npairs, int points, const lcr_synth_params* p,
+                               lcr_cloud** src, lcr_cloud** tgt, float* transforms) {
+  API_BEGIN(ctx)
+  REQUIRE(p && (npairs == 0 || (src && tgt && transforms)), "null argument");
+  REQUIRE(npairs <= 65535, "too many pairs (%zu)", npairs);
+  REQUIRE(points >= 1 && points <= (1 << 24), "points must be in [1, 2^24]");
+  REQUIRE(p->yaw_deg >= 0.f && p->tilt_deg >= 0.f && p->translation >= 0.f, "ranges must be non-negative");
+  for (size_t i = 0; i < npairs; ++i) src[i] = tgt[i] = nullptr;
+  try {
+    synth_pairs(ctx, seed, static_cast<int>(npairs), points, p, src, tgt, transforms);
+  } catch (...) {
+    for (size_t i = 0; i < npairs; ++i) {
+      cloud_release(ctx, src[i]);
+      cloud_release(ctx, tgt[i]);
+      src[i] = tgt[i] = nullptr;
+    }
+    throw;
+  }
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_rmse_batch(lcr_ctx* ctx, const lcr_cloud* const* clouds, size_t n, const double* Ta, const double* Tb,
+                          double* out) {
+  API_BEGIN(ctx)
+  REQUIRE(n == 0 || (clouds && Ta && Tb && out), "null argument");
+  REQUIRE(n <= (1u << 20), "too many clouds (%zu)", n);
+  for (size_t i = 0; i < n; ++i) REQUIRE(clouds[i], "null cloud %zu", i);
+  rmse_batch(ctx, clouds, static_cast<int>(n), Ta, Tb, out);
+  API_END(ctx)
+  return LCR_OK;
+}
+
 lcr_status lcr_posenet_create(lcr_ctx* ctx, uint64_t seed, lcr_posenet** net) {
   API_BEGIN(ctx)
   REQUIRE(net, "null argument");

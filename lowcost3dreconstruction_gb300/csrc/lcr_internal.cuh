@@ -225,6 +225,11 @@ int compact_flags(lcr_ctx* ctx, const uint8_t* flags, int n, uint32_t* out_idx);
 void compact_flags_async(lcr_ctx* ctx, const uint8_t* flags, int n, uint32_t* out_idx, uint32_t* count_dev = nullptr);
 // Gathers cloud rows: out[j] = in[idx[j]].
 void gather_cloud(lcr_ctx* ctx, const lcr_cloud* in, const uint32_t* idx, int n, lcr_cloud* out);
+// RMS over each cloud's finite points of |Ta p - Tb p| (synth.cu); host Ta, Tb [n][16], out [n].
+void rmse_batch(lcr_ctx* ctx, const lcr_cloud* const* clouds, int n, const double* Ta, const double* Tb, double* out);
+// Seeded synthetic capture pairs (synth.cu); allocates src[i], tgt[i].
+void synth_pairs(lcr_ctx* ctx, uint64_t seed, int npairs, int npts, const lcr_synth_params* prm, lcr_cloud** src,
+                 lcr_cloud** tgt, float* transforms);
 // Device-side bounding box of the finite points of an xyz array: out[0] = lo, out[1] = hi.
 void bbox(lcr_ctx* ctx, const float4* xyz, int n, float4* out2);
 

@@ -192,3 +192,49 @@ def test_training_lowers_the_loss(ctx):
     losses = [n.train_step(src, tgt, T, seed=s, opt=adamw(lr=1e-3)) for s in range(30)]
     assert all(np.isfinite(losses))
     assert np.mean(losses[-5:]) < 0.5 * np.mean(losses[:3])
+
+
+# ---------------------------------------------------- synthetic pairs, RMSE
+@pytest.mark.gpu
+def test_synthetic_pairs_are_seeded_rigid_and_visible(ctx):
+    from lowcost3dreconstruction_gb300.core import xyz_of, normals_of
+    s1, t1, T1 = ctx.synthetic_pairs(42, 3, 2000)
+    s2, t2, T2 = ctx.synthetic_pairs(42, 3, 2000)
+    np.testing.assert_array_equal(T1, T2)
+    for a, b in zip(s1 + t1, s2 + t2):
+        np.testing.assert_array_equal(a.download()["x"], b.download()["x"])
+    for b in range(3):
+        R = T1[b, :3, :3].astype(np.float64)
+        np.testing.assert_allclose(R @ R.T, np.eye(3), atol=1e-5)
+        assert np.linalg.det(R) > 0.999
+        assert np.degrees(np.arccos(np.clip(R[1, 1], -1, 1))) <= 20.0 + 1e-3   # tilt bound
+        assert np.all(np.abs(T1[b, :3, 3]) < 2.0)
+        for c in (s1[b], t1[b]):
+            p = c.download()
+            xyz, nrm = xyz_of(p), normals_of(p)
+            assert np.isfinite(xyz).all() and len(p) == 2000
+            assert np.all(np.sum(nrm * xyz, axis=1) < 0)                     # every point faces the camera
+            assert np.all(np.abs(np.linalg.norm(xyz, axis=1) - 1.0) < 0.6)   # about 1 m away
+    # noise-free: the exact transform maps the source onto the target's surface
+    s, t, T = ctx.synthetic_pairs(7, 2, 4000, yaw_deg=30, noise=False)
+    for b in range(2):
+        reg = ctx.transform(s[b], T[b])
+        _, d = ctx.knn(t[b], reg, 1)
+        assert np.median(np.sqrt(d[:, 0])) < 0.01
+
+
+@pytest.mark.gpu
+def test_rmse_batch_matches_numpy(ctx):
+    from lowcost3dreconstruction_gb300.core import points_from_xyz
+    rng = np.random.default_rng(8)
+    xyz = [rng.normal(size=(n, 3)) for n in (1000, 37)]
+    clouds = [ctx.upload(points_from_xyz(x)) for x in xyz]
+    Ta = np.tile(np.eye(4), (2, 1, 1))
+    Tb = Ta.copy()
+    Tb[:, :3, 3] = [[0.001, 0, 0], [0, 0.002, 0.002]]
+    Tb[1, :3, :3] = [[0, -1, 0], [1, 0, 0], [0, 0, 1]]
+    got = ctx.rmse_batch(clouds, Ta, Tb)
+    for i, x in enumerate(xyz):
+        x32 = x.astype(np.float32).astype(np.float64)
+        d = x32 @ (Ta[i, :3, :3] - Tb[i, :3, :3]).T + (Ta[i, :3, 3] - Tb[i, :3, 3])
+        np.testing.assert_allclose(got[i], np.sqrt(np.mean(np.sum(d * d, axis=1))), rtol=1e-12)

@@ -98,8 +98,8 @@ def peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return {"hbm_gbs": d["hbm_gbs"], "src": "measured"}
-    return {"hbm_gbs": 6800.0, "src": "fallback"}
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d.get("bf16_tflops", 1900.0), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "src": "fallback"}
 
 
 # ---------------------------------------------------------------- GPU arm
@@ -355,6 +355,127 @@ def turntable_arm(args) -> dict:
                        "l2": "flushed between steps (256 MB write)"}}
 
 
+# ------------------------------------------- learned proposal vs plain ICP
+def proposal_arm(args) -> dict:
+    """Config 3 evaluation: held-out device-generated pairs (superquadric objects
+    with a block and two balls, yaw uniform in +-180 deg, tilt +-20 deg,
+    translation +-10 cm, 20k visible points per view with Kinect depth noise),
+    aligned two ways per step over all pairs: plain GPU ICP from centroid
+    alignment, and the trained proposal followed by ICP with plain ICP as the
+    fallback; both refine with batched point-to-plane ICP (a first stage, then
+    1 cm).  value = aligned pairs/s of proposal+ICP; the plain arm is reported
+    beside it."""
+    import torch
+
+    from lowcost3dreconstruction_gb300 import _lib as L
+    from lowcost3dreconstruction_gb300 import train_posenet as TP
+    from lowcost3dreconstruction_gb300.core import Context
+    from lowcost3dreconstruction_gb300.posenet import PoseNet, WEIGHTS
+    torch.cuda.set_device(0)
+    ctx = Context(0)
+    net = PoseNet(ctx)
+    net.load(WEIGHTS)
+    large = args.workload == "large512"
+    if large:
+        # config 4: 512 pairs, points per view log-uniform in 5k-500k, one generator call per pair
+        npairs = 512
+        rng = np.random.default_rng(4)
+        sizes = np.exp(rng.uniform(np.log(5_000), np.log(500_000), npairs)).astype(int)
+        srcs, tgts, Ts = [], [], []
+        for i, n in enumerate(sizes):
+            s1, t1, T1 = ctx.synthetic_pairs(444_000_000 + i, 1, int(n), yaw_deg=180.0)
+            srcs += s1
+            tgts += t1
+            Ts.append(T1[0])
+        T = np.stack(Ts)
+    else:
+        npairs = args.pairs
+        sizes = np.full(npairs, TP.EVAL_POINTS)
+        srcs, tgts, T = ctx.synthetic_pairs(987_654_321, npairs, TP.EVAL_POINTS, yaw_deg=180.0)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
+
+    def plain():
+        return TP.refine(ctx, srcs, tgts, TP.centroid_guesses(net, srcs, tgts))
+
+    def proposal():
+        res = TP.refine(ctx, srcs, tgts, net.propose(srcs, tgts), TP.proposal_params())
+        weak = [i for i, r in enumerate(res) if not TP.settled(r)]
+        if weak:
+            ws, wt = [srcs[i] for i in weak], [tgts[i] for i in weak]
+            fb = TP.refine(ctx, ws, wt, TP.centroid_guesses(net, ws, wt))
+            for j, i in enumerate(weak):
+                if TP.settled(fb[j]):
+                    res[i] = fb[j]
+        return res, len(weak)
+
+    for _ in range(args.warmup):
+        plain()
+        proposal()
+    steps = max(1, min(args.steps, 5))
+    out = {}
+    clocks = Clocks(0)
+    clocks.start()
+    for arm in ("plain", "proposal"):
+        total, ok, fbs = 0.0, 0, 0
+        l0 = ctx.launches()
+        if arm == "proposal":
+            ctx.kernel_timing(True)
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ea.record(stream)
+            if arm == "plain":
+                res = plain()
+            else:
+                res, nfb = proposal()
+                fbs += nfb
+            eb.record(stream)
+            eb.synchronize()
+            total += ea.elapsed_time(eb)
+            good, _ = TP.aligned(ctx, srcs, res, T)
+            ok += int(good.sum())
+        launches = ctx.launches() - l0
+        enc = ctx.kernel_time(L.KT_ENCODE) if arm == "proposal" else (0.0, 0)
+        ctx.kernel_timing(False)
+        out[arm] = dict(pairs_per_s=ok / (total / 1000.0), ms=total / steps, aligned=ok / steps,
+                        fallbacks=fbs / steps, launches=launches // steps, enc=enc)
+    clk = clocks.stop()
+    pr = peaks()
+    enc_ms, enc_n = out["proposal"]["enc"]
+    flops = 2 * npairs * 1024 * (2 * (64 * 128 + 128 * 1024))
+    points = int(2 * sizes.sum())
+    achieved = flops / (enc_ms / enc_n / 1000.0) / 1e12 if enc_n else None
+    bf16_peak = pr.get("bf16_tflops", 1900.0)
+    P = out["proposal"]
+    ctx.close()
+    return {"metric": METRIC, "value": round(P["pairs_per_s"], 3), "unit": "pairs/s", "n_gpus": 1, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": round(P["ms"], 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 (proposal network) + f32/f64 (ICP)", "data": "synthetic",
+            "config": {"workload": f"{npairs} held-out device-generated pairs (superquadric + block + 2 balls, yaw "
+                                   "+-180 deg, tilt +-20 deg, translation +-10 cm, "
+                                   + ("points per view log-uniform in 5k-500k" if large else
+                                      f"{TP.EVAL_POINTS} visible points per view")
+                                   + ", Kinect depth noise); proposal + point-to-plane ICP (2 cm then 1 cm) with "
+                                   "plain ICP from centroid alignment as the fallback, all pairs batched per step",
+                       "pairs": npairs, "points": points,
+                       "points_per_s": round(points / (P["ms"] / 1000.0), 1),
+                       "aligned_per_step": P["aligned"], "fallbacks_per_step": P["fallbacks"],
+                       "plain_gpu_icp": {"pairs_per_s": round(out["plain"]["pairs_per_s"], 3),
+                                         "ms_per_step": round(out["plain"]["ms"], 3),
+                                         "aligned_per_step": out["plain"]["aligned"],
+                                         "icp": "point-to-plane, 5 cm then 1 cm, from centroid alignment"},
+                       "proposal_over_plain": round(P["pairs_per_s"] / max(out["plain"]["pairs_per_s"], 1e-9), 3),
+                       "l2": "inputs (2.9 GB) larger than L2; 256 MB flush between steps"},
+            "roofline": {"kernel": "k_encode (fused shared-MLP encoder + max-pool, tcgen05)", "bound": "tensor",
+                         "achieved": round(achieved, 1) if achieved else None, "peak": bf16_peak,
+                         "unit": "TFLOP/s", "frac": round(achieved / bf16_peak, 4) if achieved else None,
+                         "peak_src": pr["src"], "algorithmic_flops_per_launch": flops,
+                         "avg_launch_ms": round(enc_ms / enc_n, 5) if enc_n else None, "traffic": None},
+            "e2e": None, "gpu_launches": P["launches"], "clocks": clk}
+
+
 # ------------------------------------------------------------ CPU (oracle)
 def cpu_pipeline(pr, threads: int):
     from lowcost3dreconstruction_gb300 import synthetic as S
@@ -419,8 +540,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="config1", choices=["config1", "turntable36"],
-                    help="config1: the headline pair pipeline; turntable36: batched ICP over a turntable cycle")
+    ap.add_argument("--workload", default="config1", choices=["config1", "turntable36", "proposal", "large512"],
+                    help="config1: the headline pair pipeline; turntable36: batched ICP over a turntable cycle; "
+                         "proposal: learned pose proposal + ICP vs plain ICP on held-out pairs; large512: the same "
+                         "on 512 pairs of 5k-500k points per view")
+    ap.add_argument("--pairs", type=int, default=2000, help="pairs of the proposal workload")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -432,6 +556,9 @@ def main():
     elif args.workload == "turntable36":
         build.build_lib()
         out = turntable_arm(args) if rank == 0 else None
+    elif args.workload in ("proposal", "large512"):
+        build.build_lib()
+        out = proposal_arm(args) if rank == 0 else None
     else:
         build.build_lib()
         build.build_oracle()

@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+from pathlib import Path
 
 import numpy as np
 
@@ -17,6 +18,8 @@ from . import _lib as L
 from .core import Cloud, Context
 
 PARAMS = L.POSENET_PARAMS
+# Trained parameters shipped with the package (train_posenet.py made them; fp32, LAYOUT order).
+WEIGHTS = Path(__file__).resolve().parent / "weights" / "posenet.npy"
 POINTS = L.POSENET_POINTS
 # (name, shape) of each tensor in the flat parameter vector, in order
 LAYOUT = [("W1", (64, 3)), ("b1", (64,)), ("W2", (128, 64)), ("b2", (128,)), ("W3", (1024, 128)), ("b3", (1024,)),

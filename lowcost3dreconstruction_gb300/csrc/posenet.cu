@@ -152,227 +152,279 @@ __global__ void __launch_bounds__(256) k_sample(const CloudRef* __restrict__ clo
 
 // ---------------------------------------------------------------- encoder
 // Shared-memory map of k_encode (offsets from a 1024-byte-aligned base).
-constexpr uint32_t sW2 = 0;                    // W2 image, 128 x 64 bf16              16 KB
-constexpr uint32_t sA1 = sW2 + 16384;          // layer-1 output, 2 x (128 x 64)       32 KB
-constexpr uint32_t sB3 = sA1 + 32768;          // layer-2 output, 256 points x 128     64 KB
-constexpr uint32_t sW3 = sB3 + 65536;          // W3 tile double buffer, 2 x 32 KB     64 KB
-constexpr uint32_t sRun = sW3 + 2 * kW3Tile;   // running max per channel (f32)         4 KB
-constexpr uint32_t sArg = sRun + 4 * kF3;      // its point (int)                        4 KB
-constexpr uint32_t sW1 = sArg + 4 * kF3;       // (w0, w1, w2, b1) per layer-1 unit      1 KB
-constexpr uint32_t sB2 = sW1 + 16 * kF1;       // b2                                   512 B
-constexpr uint32_t sBar = sB2 + 4 * kF2;       // 4 mbarriers, TMEM slot, flag
-constexpr uint32_t kEncSmem = sBar + 64 + 1024;  // + alignment slack
-constexpr int kChunk = 256;                    // points per layer-3 MMA (N)
+constexpr uint32_t sW2 = 0;                    // W2 image, 128 x 64 bf16                      16 KB
+constexpr uint32_t sA1 = sW2 + 16384;          // layer-1 output, 2 x (128 points x 64)        32 KB
+constexpr uint32_t sB3 = sA1 + 32768;          // layer-2 output, 2 atoms x (256 points x 64)  64 KB
+constexpr int kW3Ring = 3;                     // W3 tile images in flight
+constexpr uint32_t sW3 = sB3 + 65536;          // W3 tile ring, 3 x 32 KB                      96 KB
+constexpr uint32_t sRun = sW3 + kW3Ring * kW3Tile;  // running max per channel (f32)          4 KB
+constexpr uint32_t sArg = sRun + 4 * kF3;      // its point (int)                               4 KB
+constexpr uint32_t sW1 = sArg + 4 * kF3;       // (w0, w1, w2, b1) per layer-1 unit             1 KB
+constexpr uint32_t sB2 = sW1 + 16 * kF1;       // b2                                          512 B
+constexpr uint32_t sBar = sB2 + 4 * kF2;       // mbarriers (16 x 8 B), TMEM slot, flag
+constexpr uint32_t kEncSmem = sBar + 160 + 1024;  // + alignment slack
+static_assert(kEncSmem <= 227 * 1024, "encoder shared memory");
+constexpr int kChunk = 256;                    // points per chunk (layer-2 M = 2 x 128)
+constexpr int kGroupN = 128;                   // points per layer-3 MMA (N)
+constexpr int kEpiThreads = 128;               // warps 0-3: layer 1, epilogues
+constexpr int kEncThreads = kEpiThreads + 32;  // warp 4: bulk copies and MMA issue
+// TMEM columns: layer-3 accumulators [0, 128) and [128, 256), layer 2 [256, 512).
+constexpr uint32_t kD2Col = 256;
 
-// One CTA (4 warps) encodes whole clouds, one after the other: per chunk of
-// 256 points, layer 1 on the CUDA cores (thread t: points t and t+128), layer
-// 2 as two 128x128x64 MMAs, its epilogue (bias, ReLU, bf16) written straight
-// into the swizzled B operand of layer 3, then for each 128-channel tile of W3
-// (bulk-copied into a double buffer one tile ahead) a 128x256x128 MMA whose
-// epilogue folds the 256 points into the running max of the thread's channel.
-// kTrain also records the arg-max point and stores the layer-2 activations for
-// the backward pass.  TMEM: columns [0, 256) layer 3, [256, 512) layer 2.
+// Barrier slots (uint64_t index from sBar).
+enum : int {
+  kBarW2 = 0,
+  kBarW3Full = 1,    // [3]  tile image landed (bulk-copy bytes)
+  kBarW3Empty = 4,   // [3]  MMAs reading the tile finished (MMA commit)
+  kBarA1 = 7,        //      layer-1 operand written (128 arrivals)
+  kBarD2 = 8,        //      layer-2 accumulator ready (MMA commit)
+  kBarB3 = 9,        //      layer-3 operand written (128 arrivals)
+  kBarD3Full = 10,   // [2]  layer-3 accumulator ready (MMA commit)
+  kBarD3Empty = 12,  // [2]  layer-3 accumulator drained (128 arrivals)
+  kBarDrain = 14,    //      every MMA issued so far completed (final commit)
+  kBarCount = 15
+};
+
+// One CTA per SM encodes whole clouds one after the other, warp-specialised.
+// Warps 0-3 (one thread per TMEM lane) compute layer 1 (3 -> 64) on the CUDA
+// cores into the swizzled A operand of layer 2, move layer 2's accumulator
+// (bias, ReLU, bf16) into the swizzled B operand of layer 3, and drain the
+// layer-3 accumulators into the running max of their channel.  Warp 4 (one
+// elected lane) keeps a ring of three W3 tile images filled by bulk copies and
+// issues every MMA: layer 2 as two 128x128x64, layer 3 as sixteen
+// 128(channels)x128(points)x128 per 256-point chunk into two TMEM buffers, so
+// that the epilogue of one overlaps the MMA of the next.  Handoffs are
+// mbarriers (MMA commits, bulk-copy byte counts, thread arrivals); every wait
+// is bounded and a timeout drains what this CTA issued before its TMEM is
+// freed.  kTrain also records the arg-max point per channel and stores the
+// layer-2 activations for the backward pass.
 template <bool kTrain>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(kEncThreads, 1)
     k_encode(const float4* __restrict__ pts, int nclouds, int npairs, const float* __restrict__ w,
              const uint8_t* __restrict__ w2img, const uint8_t* __restrict__ w3img, float* __restrict__ feat,
              bf16* __restrict__ featb, int* __restrict__ argmax, bf16* __restrict__ h2g, int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
   const int tid = threadIdx.x, warp = tid >> 5;
-  uint64_t* bar_w3 = reinterpret_cast<uint64_t*>(sm + sBar);  // [2]
-  uint64_t* bar_mma = bar_w3 + 2;
-  uint64_t* bar_w2 = bar_w3 + 3;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + sBar + 32);
-  volatile int* sflag = reinterpret_cast<volatile int*>(sm + sBar + 36);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + sBar);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + sBar + 8 * 16);
+  volatile int* sflag = reinterpret_cast<volatile int*>(sm + sBar + 8 * 16 + 4);
   float* run = reinterpret_cast<float*>(sm + sRun);
   int* arg = reinterpret_cast<int*>(sm + sArg);
   float4* w1s = reinterpret_cast<float4*>(sm + sW1);
   float* b2s = reinterpret_cast<float*>(sm + sB2);
 
   const int ncl = (nclouds - static_cast<int>(blockIdx.x) + static_cast<int>(gridDim.x) - 1) / gridDim.x;
-  const int ntiles = ncl * (kPts / kChunk) * (kF3 / 128);
+  const int nchunks = ncl * (kPts / kChunk);
+  const int ntiles = nchunks * (kF3 / 128);
   if (tid == 0) {
-    tc::mbar_init(&bar_w3[0], 1);
-    tc::mbar_init(&bar_w3[1], 1);
-    tc::mbar_init(bar_mma, 1);
-    tc::mbar_init(bar_w2, 1);
+    tc::mbar_init(&bar[kBarW2], 1);
+    for (int i = 0; i < kW3Ring; ++i) {
+      tc::mbar_init(&bar[kBarW3Full + i], 1);
+      tc::mbar_init(&bar[kBarW3Empty + i], 1);
+    }
+    tc::mbar_init(&bar[kBarA1], kEpiThreads);
+    tc::mbar_init(&bar[kBarD2], 1);
+    tc::mbar_init(&bar[kBarB3], kEpiThreads);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&bar[kBarD3Full + i], 1);
+      tc::mbar_init(&bar[kBarD3Empty + i], kEpiThreads);
+    }
+    tc::mbar_init(&bar[kBarDrain], 1);
     *sflag = 0;
     tc::mbar_fence_init();
   }
-  for (int i = tid; i < kF1; i += 128)
+  for (int i = tid; i < kF1; i += kEncThreads)
     w1s[i] = make_float4(bf16r(w[oW1 + 3 * i]), bf16r(w[oW1 + 3 * i + 1]), bf16r(w[oW1 + 3 * i + 2]), w[oB1 + i]);
-  for (int i = tid; i < kF2; i += 128) b2s[i] = w[oB2 + i];
-  if (warp == 0) tc::tmem_alloc<512>(tslot);
+  for (int i = tid; i < kF2; i += kEncThreads) b2s[i] = w[oB2 + i];
+  if (warp == 4) tc::tmem_alloc<512>(tslot);
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
-  if (tid == 0) {
-    tc::mbar_expect_tx(bar_w2, 16384);
-    tc::bulk_g2s(sm + sW2, w2img, 16384, bar_w2);
-    for (int g = 0; g < 2 && g < ntiles; ++g) {
-      tc::mbar_expect_tx(&bar_w3[g], kW3Tile);
-      tc::bulk_g2s(sm + sW3 + g * kW3Tile, w3img + (g & 7) * kW3Tile, kW3Tile, &bar_w3[g]);
-    }
-  }
-  if (!tc::mbar_wait(bar_w2, 0)) *sflag = 1;
-  __syncthreads();  // every thread reads the same flag below
-  uint32_t mph = 0;
-  int g = 0;  // W3 tiles consumed by this CTA
-  bool mma_stuck = false;
-  auto wait_mma = [&]() {
-    if (tc::mbar_wait(bar_mma, mph)) {
-      mph ^= 1;
-    } else {
-      mma_stuck = true;
-      *sflag = 1;
-    }
-  };
-  for (int ci = 0; ci < ncl && !*sflag; ++ci) {
-    const int cloud = static_cast<int>(blockIdx.x) + ci * static_cast<int>(gridDim.x);
-    for (int j = 0; j < kF3 / 128; ++j) {
-      run[tid + 128 * j] = -INFINITY;
-      arg[tid + 128 * j] = 0;
-    }
-    for (int pc = 0; pc < kPts / kChunk; ++pc) {
-      // ---- layer 1: 3 -> 64, CUDA cores, into the swizzled A operand of layer 2
-      for (int half = 0; half < 2; ++half) {
-        const float4 p = pts[static_cast<size_t>(cloud) * kPts + pc * kChunk + half * 128 + tid];
-        unsigned char* A = sm + sA1 + half * 16384 + tid * 128;
-#pragma unroll 1
-        for (int c8 = 0; c8 < 8; ++c8) {
-          uint32_t pk[4];
-#pragma unroll
-          for (int j2 = 0; j2 < 4; ++j2) {
-            float h[2];
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-              const float4 wv = w1s[c8 * 8 + j2 * 2 + e];
-              float a = wv.w;
-              a = fmaf(wv.x, p.x, a);
-              a = fmaf(wv.y, p.y, a);
-              a = fmaf(wv.z, p.z, a);
-              h[e] = fmaxf(a, 0.f);
-            }
-            pk[j2] = pack_bf16x2(h[0], h[1]);
-          }
-          *reinterpret_cast<uint4*>(A + ((c8 ^ (tid & 7)) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-        }
+
+  if (warp == 4) {
+    // ================================================ bulk copies + MMA issue
+    if ((tid & 31) == 0) {
+      bool ok = true;
+      int loaded = 0;      // tile images requested so far
+      int tiles_used = 0;  // tile images whose MMAs were issued
+      tc::mbar_expect_tx(&bar[kBarW2], 16384);
+      tc::bulk_g2s(sm + sW2, w2img, 16384, &bar[kBarW2]);
+      for (; loaded < kW3Ring && loaded < ntiles; ++loaded) {
+        tc::mbar_expect_tx(&bar[kBarW3Full + loaded], kW3Tile);
+        tc::bulk_g2s(sm + sW3 + loaded * kW3Tile, w3img + (loaded & 7) * kW3Tile, kW3Tile, &bar[kBarW3Full + loaded]);
       }
-      tc::fence_async_smem();
-      tc::tc_fence_before();
-      __syncthreads();
-      // ---- layer 2: 64 -> 128, two 128x128x64 MMAs (A = points, B = W2)
-      if (tid == 0) {
+      ok = tc::mbar_wait(&bar[kBarW2], 0);
+      const uint32_t id2 = tc::idesc_bf16_f32(128, 128), id3 = tc::idesc_bf16_f32(128, kGroupN);
+      const uint32_t w2a = tc::smem_u32(sm + sW2), a1a = tc::smem_u32(sm + sA1), b3a = tc::smem_u32(sm + sB3);
+      for (int C = 0; C < nchunks && ok && !*sflag; ++C) {
+        // layer 2: D2[point][feature] for the two 128-point halves of the chunk
+        if (!(ok = tc::mbar_wait(&bar[kBarA1], C & 1))) break;
         tc::tc_fence_after();
-        const uint32_t id2 = tc::idesc_bf16_f32(128, 128);
-        const uint32_t b0 = tc::smem_u32(sm + sW2);
-        for (int half = 0; half < 2; ++half) {
-          const uint32_t a0 = tc::smem_u32(sm + sA1 + half * 16384);
+        for (int half = 0; half < 2; ++half)
           for (int s = 0; s < kF1 / 16; ++s)
-            tc::mma_bf16(tmem + 256 + half * 128, tc::sdesc_sw128(a0 + s * 32), tc::sdesc_sw128(b0 + s * 32), id2,
-                         s > 0);
+            tc::mma_bf16(tmem + kD2Col + half * 128, tc::sdesc_sw128(a1a + half * 16384 + s * 32),
+                         tc::sdesc_sw128(w2a + s * 32), id2, s > 0);
+        tc::mma_commit(&bar[kBarD2]);
+        // layer 3: per W3 tile, two 128-point groups into alternating accumulators
+        if (!(ok = tc::mbar_wait(&bar[kBarB3], C & 1))) break;
+        tc::tc_fence_after();
+        for (int ct = 0; ct < kF3 / 128 && ok; ++ct) {
+          const int t = C * (kF3 / 128) + ct, rb = t % kW3Ring;
+          if (!(ok = tc::mbar_wait(&bar[kBarW3Full + rb], (t / kW3Ring) & 1))) break;
+          const uint32_t wa = tc::smem_u32(sm + sW3 + rb * kW3Tile);
+          for (int nh = 0; nh < 2; ++nh) {
+            const int G = 2 * t + nh, db = G & 1;
+            if (G >= 2 && !(ok = tc::mbar_wait(&bar[kBarD3Empty + db], ((G - 2) >> 1) & 1))) break;
+            tc::tc_fence_after();
+            for (int s = 0; s < kF2 / 16; ++s)
+              tc::mma_bf16(tmem + db * kGroupN, tc::sdesc_sw128(wa + (s >> 2) * 16384 + (s & 3) * 32),
+                           tc::sdesc_sw128(b3a + (s >> 2) * (kChunk * 128) + nh * (kGroupN * 128) + (s & 3) * 32),
+                           id3, s > 0);
+            tc::mma_commit(&bar[kBarD3Full + db]);
+          }
+          if (!ok) break;
+          tc::mma_commit(&bar[kBarW3Empty + rb]);
+          tiles_used = t + 1;
+          // refill the slot of the previous tile (its MMAs are done or nearly) two tiles ahead
+          if (t >= 1 && loaded < ntiles) {
+            const int pt = t - 1, pb = pt % kW3Ring;
+            if (!(ok = tc::mbar_wait(&bar[kBarW3Empty + pb], (pt / kW3Ring) & 1))) break;
+            tc::mbar_expect_tx(&bar[kBarW3Full + pb], kW3Tile);
+            tc::bulk_g2s(sm + sW3 + pb * kW3Tile, w3img + (loaded & 7) * kW3Tile, kW3Tile, &bar[kBarW3Full + pb]);
+            ++loaded;
+          }
         }
-        tc::mma_commit(bar_mma);
       }
-      wait_mma();
-      tc::tc_fence_after();
-      // ---- layer-2 epilogue: bias, ReLU, bf16, into the swizzled B operand of layer 3
-      for (int half = 0; half < 2; ++half) {
-        const int R = half * 128 + tid;  // point within the chunk
-        for (int q = 0; q < kF2 / 32; ++q) {
-          float v[32];
-          tc::tmem_ld32(tmem + lane_base + 256 + half * 128 + q * 32, v);
-#pragma unroll
-          for (int c4 = 0; c4 < 4; ++c4) {
+      if (!ok) *sflag = 1;
+      // drain before the CTA's shared memory and TMEM go away: tile images requested but
+      // never consumed (only after a failure), then one commit behind every MMA issued
+      for (int t = tiles_used; t < loaded; ++t)
+        tc::mbar_wait(&bar[kBarW3Full + t % kW3Ring], (t / kW3Ring) & 1);
+      tc::mma_commit(&bar[kBarDrain]);
+      if (!tc::mbar_wait(&bar[kBarDrain], 0)) *sflag = 1;
+    }
+  } else {
+    // ======================================================== warps 0-3
+    const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+    int C = 0;
+    bool ok = true;
+    for (int ci = 0; ci < ncl && ok; ++ci) {
+      const int cloud = static_cast<int>(blockIdx.x) + ci * static_cast<int>(gridDim.x);
+      for (int j = 0; j < kF3 / 128; ++j) {
+        run[tid + 128 * j] = -INFINITY;
+        arg[tid + 128 * j] = 0;
+      }
+      for (int pc = 0; pc < kPts / kChunk && ok; ++pc, ++C) {
+        // ---- layer 1 (3 -> 64) into the A operand (free: chunk C-1's layer 2 completed)
+        for (int half = 0; half < 2; ++half) {
+          const float4 p = pts[static_cast<size_t>(cloud) * kPts + pc * kChunk + half * 128 + tid];
+          unsigned char* A = sm + sA1 + half * 16384 + tid * 128;
+#pragma unroll 1
+          for (int c8 = 0; c8 < 8; ++c8) {
             uint32_t pk[4];
 #pragma unroll
             for (int j2 = 0; j2 < 4; ++j2) {
-              const int i0 = c4 * 8 + j2 * 2;
-              pk[j2] = pack_bf16x2(fmaxf(v[i0] + b2s[q * 32 + i0], 0.f), fmaxf(v[i0 + 1] + b2s[q * 32 + i0 + 1], 0.f));
-            }
-            const int f0 = q * 32 + c4 * 8;
-            const uint4 val = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-            *reinterpret_cast<uint4*>(sm + sB3 + (f0 >> 6) * (kChunk * 128) + R * 128 +
-                                      ((((f0 & 63) >> 3) ^ (R & 7)) << 4)) = val;
-            if (kTrain)
-              *reinterpret_cast<uint4*>(h2g + (static_cast<size_t>(cloud) * kPts + pc * kChunk + R) * kF2 + f0) = val;
-          }
-        }
-      }
-      tc::fence_async_smem();
-      tc::tc_fence_before();
-      __syncthreads();
-      if (*sflag) break;
-      // ---- layer 3: 128 -> 1024 per 128-channel tile, max over the chunk's points
-      for (int ct = 0; ct < kF3 / 128; ++ct, ++g) {
-        const int buf = g & 1;
-        if (tid == 0) {
-          if (!tc::mbar_wait(&bar_w3[buf], (g >> 1) & 1)) *sflag = 1;
-          tc::tc_fence_after();
-          const uint32_t id3 = tc::idesc_bf16_f32(128, kChunk);
-          const uint32_t a0 = tc::smem_u32(sm + sW3 + buf * kW3Tile), b0 = tc::smem_u32(sm + sB3);
-          for (int s = 0; s < kF2 / 16; ++s)
-            tc::mma_bf16(tmem, tc::sdesc_sw128(a0 + (s >> 2) * 16384 + (s & 3) * 32),
-                         tc::sdesc_sw128(b0 + (s >> 2) * (kChunk * 128) + (s & 3) * 32), id3, s > 0);
-          tc::mma_commit(bar_mma);
-        }
-        wait_mma();
-        tc::tc_fence_after();
-        if (tid == 0 && g + 2 < ntiles && !*sflag) {  // the tile's MMAs are done: refill its buffer
-          tc::mbar_expect_tx(&bar_w3[buf], kW3Tile);
-          tc::bulk_g2s(sm + sW3 + buf * kW3Tile, w3img + ((g + 2) & 7) * kW3Tile, kW3Tile, &bar_w3[buf]);
-        }
-        const int ch = ct * 128 + tid;
-        float best = run[ch];
-        int barg = arg[ch];
-        for (int q = 0; q < kChunk / 32; ++q) {
-          float v[32];
-          tc::tmem_ld32(tmem + lane_base + q * 32, v);
+              float h[2];
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            if (kTrain) {
-              if (v[i] > best) {
-                best = v[i];
-                barg = pc * kChunk + q * 32 + i;
+              for (int e = 0; e < 2; ++e) {
+                const float4 wv = w1s[c8 * 8 + j2 * 2 + e];
+                float a = wv.w;
+                a = fmaf(wv.x, p.x, a);
+                a = fmaf(wv.y, p.y, a);
+                a = fmaf(wv.z, p.z, a);
+                h[e] = fmaxf(a, 0.f);
               }
-            } else {
-              best = fmaxf(best, v[i]);
+              pk[j2] = pack_bf16x2(h[0], h[1]);
+            }
+            *reinterpret_cast<uint4*>(A + ((c8 ^ (tid & 7)) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+          }
+        }
+        tc::fence_async_smem();
+        tc::tc_fence_before();
+        tc::mbar_arrive(&bar[kBarA1]);
+        // ---- layer-2 epilogue into the B operand of layer 3 (free: chunk C-1's layer 3 completed)
+        if (!(ok = tc::mbar_wait(&bar[kBarD2], C & 1))) break;
+        tc::tc_fence_after();
+        for (int half = 0; half < 2; ++half) {
+          const int R = half * 128 + tid;  // point within the chunk
+          for (int q = 0; q < kF2 / 32; ++q) {
+            float v[32];
+            tc::tmem_ld32(tmem + lane_base + kD2Col + half * 128 + q * 32, v);
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) {
+              uint32_t pk[4];
+#pragma unroll
+              for (int j2 = 0; j2 < 4; ++j2) {
+                const int i0 = c4 * 8 + j2 * 2;
+                pk[j2] = pack_bf16x2(fmaxf(v[i0] + b2s[q * 32 + i0], 0.f),
+                                     fmaxf(v[i0 + 1] + b2s[q * 32 + i0 + 1], 0.f));
+              }
+              const int f0 = q * 32 + c4 * 8;
+              const uint4 val = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+              *reinterpret_cast<uint4*>(sm + sB3 + (f0 >> 6) * (kChunk * 128) + R * 128 +
+                                        ((((f0 & 63) >> 3) ^ (R & 7)) << 4)) = val;
+              if (kTrain)
+                *reinterpret_cast<uint4*>(h2g + (static_cast<size_t>(cloud) * kPts + pc * kChunk + R) * kF2 + f0) =
+                    val;
             }
           }
         }
-        run[ch] = best;
-        arg[ch] = barg;
+        tc::fence_async_smem();
         tc::tc_fence_before();
-        __syncthreads();
-        if (*sflag) break;
+        tc::mbar_arrive(&bar[kBarB3]);
+        // ---- layer-3 epilogues: the max over each group's 128 points
+        for (int ct = 0; ct < kF3 / 128 && ok; ++ct) {
+          const int ch = ct * 128 + tid;
+          float best = run[ch];
+          int barg = arg[ch];
+          for (int nh = 0; nh < 2; ++nh) {
+            const int G = 2 * (C * (kF3 / 128) + ct) + nh, db = G & 1;
+            if (!(ok = tc::mbar_wait(&bar[kBarD3Full + db], (G >> 1) & 1))) break;
+            tc::tc_fence_after();
+            for (int q = 0; q < kGroupN / 32; ++q) {
+              float v[32];
+              tc::tmem_ld32(tmem + lane_base + db * kGroupN + q * 32, v);
+#pragma unroll
+              for (int i = 0; i < 32; ++i) {
+                if (kTrain) {
+                  if (v[i] > best) {
+                    best = v[i];
+                    barg = pc * kChunk + nh * kGroupN + q * 32 + i;
+                  }
+                } else {
+                  best = fmaxf(best, v[i]);
+                }
+              }
+            }
+            tc::tc_fence_before();
+            tc::mbar_arrive(&bar[kBarD3Empty + db]);
+          }
+          run[ch] = best;
+          arg[ch] = barg;
+        }
+        if (*sflag) ok = false;
       }
-      if (*sflag) break;
+      if (!ok) break;
+      // ---- pooled feature: ReLU(max + b3); bias after the max (fp32 rounding is monotone)
+      const int row = cloud < npairs ? cloud : cloud - npairs;
+      const int col0 = cloud < npairs ? 0 : kF3;
+      for (int j = 0; j < kF3 / 128; ++j) {
+        const int c = tid + 128 * j;
+        const float m = fmaxf(run[c] + w[oB3 + c], 0.f);
+        feat[static_cast<size_t>(cloud) * kF3 + c] = m;
+        featb[static_cast<size_t>(row) * kIn + col0 + c] = __float2bfloat16_rn(m);
+        if (kTrain) argmax[static_cast<size_t>(cloud) * kF3 + c] = arg[c];
+      }
     }
-    if (*sflag) break;
-    // ---- pooled feature: ReLU(max + b3); bias after the max (fp32 rounding is monotone)
-    const int row = cloud < npairs ? cloud : cloud - npairs;
-    const int col0 = cloud < npairs ? 0 : kF3;
-    for (int j = 0; j < kF3 / 128; ++j) {
-      const int c = tid + 128 * j;
-      const float m = fmaxf(run[c] + w[oB3 + c], 0.f);
-      feat[static_cast<size_t>(cloud) * kF3 + c] = m;
-      featb[static_cast<size_t>(row) * kIn + col0 + c] = __float2bfloat16_rn(m);
-      if (kTrain) argmax[static_cast<size_t>(cloud) * kF3 + c] = arg[c];
-    }
+    if (!ok) *sflag = 1;
   }
-  // ---- teardown: after a timed-out wait, let the work this CTA issued drain
-  // (bounded) before its TMEM is released
-  if (*sflag && tid == 0) {
-    if (mma_stuck) tc::mbar_wait(bar_mma, mph);
-    for (int t = g; t < g + 3 && t < ntiles; ++t) tc::mbar_wait(&bar_w3[t & 1], (t >> 1) & 1);
-    atomicExch(err, 1);
-  }
+  // ---- teardown
   tc::tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (*sflag && tid == 0) atomicExch(err, 1);
+  if (warp == 4) {
     tc::tc_fence_after();
     tc::tmem_free<512>(tmem);
   }
@@ -486,10 +538,10 @@ void encode(lcr_ctx* ctx, lcr_posenet* net, const Batch& b, bool train) {
   const int grid = nclouds < ctx->sms ? nclouds : ctx->sms;
   KernelTimer kt(ctx, LCR_KT_ENCODE);
   if (train)
-    LCR_LAUNCH(ctx, k_encode<true>, grid, 128, kEncSmem, b.pts, nclouds, b.B, net->w, net->pw.w2img, net->pw.w3img,
+    LCR_LAUNCH(ctx, k_encode<true>, grid, kEncThreads, kEncSmem, b.pts, nclouds, b.B, net->w, net->pw.w2img, net->pw.w3img,
                b.feat, b.featb, b.argmax, b.h2g, net->err);
   else
-    LCR_LAUNCH(ctx, k_encode<false>, grid, 128, kEncSmem, b.pts, nclouds, b.B, net->w, net->pw.w2img,
+    LCR_LAUNCH(ctx, k_encode<false>, grid, kEncThreads, kEncSmem, b.pts, nclouds, b.B, net->w, net->pw.w2img,
                net->pw.w3img, b.feat, b.featb, b.argmax, b.h2g, net->err);
 }
 

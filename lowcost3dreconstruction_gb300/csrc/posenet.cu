@@ -307,115 +307,131 @@ __global__ void __launch_bounds__(kEncThreads, 1)
     }
   } else {
     // ======================================================== warps 0-3
+    // Chunk C (global over this CTA's clouds) is cloud C / 4, points 256 (C % 4) ...
+    // Layer 1 of chunk C+1 is computed right after chunk C's layer-3 operand is
+    // handed over, so the MMA warp can queue layer 2 of C+1 behind layer 3 of C.
     const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
-    int C = 0;
-    bool ok = true;
-    for (int ci = 0; ci < ncl && ok; ++ci) {
-      const int cloud = static_cast<int>(blockIdx.x) + ci * static_cast<int>(gridDim.x);
-      for (int j = 0; j < kF3 / 128; ++j) {
-        run[tid + 128 * j] = -INFINITY;
-        arg[tid + 128 * j] = 0;
-      }
-      for (int pc = 0; pc < kPts / kChunk && ok; ++pc, ++C) {
-        // ---- layer 1 (3 -> 64) into the A operand (free: chunk C-1's layer 2 completed)
-        for (int half = 0; half < 2; ++half) {
-          const float4 p = pts[static_cast<size_t>(cloud) * kPts + pc * kChunk + half * 128 + tid];
-          unsigned char* A = sm + sA1 + half * 16384 + tid * 128;
+    constexpr int kChunksPerCloud = kPts / kChunk;
+    auto cloud_of = [&](int C) { return static_cast<int>(blockIdx.x) + (C / kChunksPerCloud) * static_cast<int>(gridDim.x); };
+    // layer 1 (3 -> 64) of chunk C into the A operand of layer 2
+    auto layer1 = [&](int C) {
+      const size_t base = static_cast<size_t>(cloud_of(C)) * kPts + (C % kChunksPerCloud) * kChunk;
+      for (int half = 0; half < 2; ++half) {
+        const float4 p = pts[base + half * 128 + tid];
+        unsigned char* A = sm + sA1 + half * 16384 + tid * 128;
 #pragma unroll 1
-          for (int c8 = 0; c8 < 8; ++c8) {
+        for (int c8 = 0; c8 < 8; ++c8) {
+          uint32_t pk[4];
+#pragma unroll
+          for (int j2 = 0; j2 < 4; ++j2) {
+            float h[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+              const float4 wv = w1s[c8 * 8 + j2 * 2 + e];
+              float a = wv.w;
+              a = fmaf(wv.x, p.x, a);
+              a = fmaf(wv.y, p.y, a);
+              a = fmaf(wv.z, p.z, a);
+              h[e] = fmaxf(a, 0.f);
+            }
+            pk[j2] = pack_bf16x2(h[0], h[1]);
+          }
+          *reinterpret_cast<uint4*>(A + ((c8 ^ (tid & 7)) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        }
+      }
+      tc::fence_async_smem();
+      tc::tc_fence_before();
+      tc::mbar_arrive(&bar[kBarA1]);
+    };
+    bool ok = true;
+    for (int j = 0; j < kF3 / 128; ++j) {
+      run[tid + 128 * j] = -INFINITY;
+      arg[tid + 128 * j] = 0;
+    }
+    if (nchunks > 0) layer1(0);
+    for (int C = 0; C < nchunks && ok; ++C) {
+      const int cloud = cloud_of(C), pc = C % kChunksPerCloud;
+      // ---- layer-2 epilogue into the B operand of layer 3 (free: chunk C-1's layer 3 completed)
+      if (!(ok = tc::mbar_wait(&bar[kBarD2], C & 1))) break;
+      tc::tc_fence_after();
+      for (int half = 0; half < 2; ++half) {
+        const int R = half * 128 + tid;  // point within the chunk
+        float v[kF2];
+        tc::tmem_ld128(tmem + lane_base + kD2Col + half * 128, v);
+#pragma unroll
+        for (int q = 0; q < kF2 / 32; ++q) {
+#pragma unroll
+          for (int c4 = 0; c4 < 4; ++c4) {
             uint32_t pk[4];
 #pragma unroll
             for (int j2 = 0; j2 < 4; ++j2) {
-              float h[2];
-#pragma unroll
-              for (int e = 0; e < 2; ++e) {
-                const float4 wv = w1s[c8 * 8 + j2 * 2 + e];
-                float a = wv.w;
-                a = fmaf(wv.x, p.x, a);
-                a = fmaf(wv.y, p.y, a);
-                a = fmaf(wv.z, p.z, a);
-                h[e] = fmaxf(a, 0.f);
-              }
-              pk[j2] = pack_bf16x2(h[0], h[1]);
+              const int i0 = q * 32 + c4 * 8 + j2 * 2;
+              pk[j2] = pack_bf16x2(fmaxf(v[i0] + b2s[i0], 0.f), fmaxf(v[i0 + 1] + b2s[i0 + 1], 0.f));
             }
-            *reinterpret_cast<uint4*>(A + ((c8 ^ (tid & 7)) << 4)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            const int f0 = q * 32 + c4 * 8;
+            const uint4 val = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            *reinterpret_cast<uint4*>(sm + sB3 + (f0 >> 6) * (kChunk * 128) + R * 128 +
+                                      ((((f0 & 63) >> 3) ^ (R & 7)) << 4)) = val;
+            if (kTrain)
+              *reinterpret_cast<uint4*>(h2g + (static_cast<size_t>(cloud) * kPts + pc * kChunk + R) * kF2 + f0) = val;
           }
         }
-        tc::fence_async_smem();
-        tc::tc_fence_before();
-        tc::mbar_arrive(&bar[kBarA1]);
-        // ---- layer-2 epilogue into the B operand of layer 3 (free: chunk C-1's layer 3 completed)
-        if (!(ok = tc::mbar_wait(&bar[kBarD2], C & 1))) break;
-        tc::tc_fence_after();
-        for (int half = 0; half < 2; ++half) {
-          const int R = half * 128 + tid;  // point within the chunk
-          for (int q = 0; q < kF2 / 32; ++q) {
-            float v[32];
-            tc::tmem_ld32(tmem + lane_base + kD2Col + half * 128 + q * 32, v);
-#pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4) {
-              uint32_t pk[4];
-#pragma unroll
-              for (int j2 = 0; j2 < 4; ++j2) {
-                const int i0 = c4 * 8 + j2 * 2;
-                pk[j2] = pack_bf16x2(fmaxf(v[i0] + b2s[q * 32 + i0], 0.f),
-                                     fmaxf(v[i0 + 1] + b2s[q * 32 + i0 + 1], 0.f));
-              }
-              const int f0 = q * 32 + c4 * 8;
-              const uint4 val = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-              *reinterpret_cast<uint4*>(sm + sB3 + (f0 >> 6) * (kChunk * 128) + R * 128 +
-                                        ((((f0 & 63) >> 3) ^ (R & 7)) << 4)) = val;
-              if (kTrain)
-                *reinterpret_cast<uint4*>(h2g + (static_cast<size_t>(cloud) * kPts + pc * kChunk + R) * kF2 + f0) =
-                    val;
-            }
-          }
-        }
-        tc::fence_async_smem();
-        tc::tc_fence_before();
-        tc::mbar_arrive(&bar[kBarB3]);
-        // ---- layer-3 epilogues: the max over each group's 128 points
-        for (int ct = 0; ct < kF3 / 128 && ok; ++ct) {
-          const int ch = ct * 128 + tid;
-          float best = run[ch];
-          int barg = arg[ch];
-          for (int nh = 0; nh < 2; ++nh) {
-            const int G = 2 * (C * (kF3 / 128) + ct) + nh, db = G & 1;
-            if (!(ok = tc::mbar_wait(&bar[kBarD3Full + db], (G >> 1) & 1))) break;
-            tc::tc_fence_after();
-            for (int q = 0; q < kGroupN / 32; ++q) {
-              float v[32];
-              tc::tmem_ld32(tmem + lane_base + db * kGroupN + q * 32, v);
-#pragma unroll
-              for (int i = 0; i < 32; ++i) {
-                if (kTrain) {
-                  if (v[i] > best) {
-                    best = v[i];
-                    barg = pc * kChunk + nh * kGroupN + q * 32 + i;
-                  }
-                } else {
-                  best = fmaxf(best, v[i]);
-                }
-              }
-            }
-            tc::tc_fence_before();
-            tc::mbar_arrive(&bar[kBarD3Empty + db]);
-          }
-          run[ch] = best;
-          arg[ch] = barg;
-        }
-        if (*sflag) ok = false;
       }
+      tc::fence_async_smem();
+      tc::tc_fence_before();
+      tc::mbar_arrive(&bar[kBarB3]);
+      // ---- layer 1 of the next chunk (A operand free: this chunk's layer 2 completed)
+      if (C + 1 < nchunks) layer1(C + 1);
+      // ---- layer-3 epilogues: the max over each group's 128 points
+      for (int ct = 0; ct < kF3 / 128 && ok; ++ct) {
+        const int ch = ct * 128 + tid;
+        float best = run[ch];
+        int barg = arg[ch];
+        for (int nh = 0; nh < 2; ++nh) {
+          const int G = 2 * (C * (kF3 / 128) + ct) + nh, db = G & 1;
+          if (!(ok = tc::mbar_wait(&bar[kBarD3Full + db], (G >> 1) & 1))) break;
+          tc::tc_fence_after();
+          float v[kGroupN];
+          tc::tmem_ld128(tmem + lane_base + db * kGroupN, v);
+          tc::tc_fence_before();
+          tc::mbar_arrive(&bar[kBarD3Empty + db]);  // the values are in registers: release the buffer
+          if (kTrain) {
+#pragma unroll
+            for (int i = 0; i < kGroupN; ++i)
+              if (v[i] > best) {
+                best = v[i];
+                barg = pc * kChunk + nh * kGroupN + i;
+              }
+          } else {
+            float m0 = v[0], m1 = v[1], m2 = v[2], m3 = v[3];  // four independent chains
+#pragma unroll
+            for (int i = 4; i < kGroupN; i += 4) {
+              m0 = fmaxf(m0, v[i]);
+              m1 = fmaxf(m1, v[i + 1]);
+              m2 = fmaxf(m2, v[i + 2]);
+              m3 = fmaxf(m3, v[i + 3]);
+            }
+            best = fmaxf(best, fmaxf(fmaxf(m0, m1), fmaxf(m2, m3)));
+          }
+        }
+        run[ch] = best;
+        arg[ch] = barg;
+      }
+      if (*sflag) ok = false;
       if (!ok) break;
-      // ---- pooled feature: ReLU(max + b3); bias after the max (fp32 rounding is monotone)
-      const int row = cloud < npairs ? cloud : cloud - npairs;
-      const int col0 = cloud < npairs ? 0 : kF3;
-      for (int j = 0; j < kF3 / 128; ++j) {
-        const int c = tid + 128 * j;
-        const float m = fmaxf(run[c] + w[oB3 + c], 0.f);
-        feat[static_cast<size_t>(cloud) * kF3 + c] = m;
-        featb[static_cast<size_t>(row) * kIn + col0 + c] = __float2bfloat16_rn(m);
-        if (kTrain) argmax[static_cast<size_t>(cloud) * kF3 + c] = arg[c];
+      if (pc == kChunksPerCloud - 1) {
+        // ---- pooled feature: ReLU(max + b3); bias after the max (fp32 rounding is monotone)
+        const int row = cloud < npairs ? cloud : cloud - npairs;
+        const int col0 = cloud < npairs ? 0 : kF3;
+        for (int j = 0; j < kF3 / 128; ++j) {
+          const int c = tid + 128 * j;
+          const float m = fmaxf(run[c] + w[oB3 + c], 0.f);
+          feat[static_cast<size_t>(cloud) * kF3 + c] = m;
+          featb[static_cast<size_t>(row) * kIn + col0 + c] = __float2bfloat16_rn(m);
+          if (kTrain) argmax[static_cast<size_t>(cloud) * kF3 + c] = arg[c];
+          run[c] = -INFINITY;
+          arg[c] = 0;
+        }
       }
     }
     if (!ok) *sflag = 1;

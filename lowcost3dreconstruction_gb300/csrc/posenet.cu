@@ -165,11 +165,12 @@ constexpr uint32_t sBar = sB2 + 4 * kF2;       // mbarriers (16 x 8 B), TMEM slo
 constexpr uint32_t kEncSmem = sBar + 160 + 1024;  // + alignment slack
 static_assert(kEncSmem <= 227 * 1024, "encoder shared memory");
 constexpr int kChunk = 256;                    // points per chunk (layer-2 M = 2 x 128)
-constexpr int kGroupN = 128;                   // points per layer-3 MMA (N)
+constexpr int kGroupN = 256;                   // points per layer-3 MMA (N): the whole chunk
 constexpr int kEpiThreads = 128;               // warps 0-3: layer 1, epilogues
 constexpr int kEncThreads = kEpiThreads + 32;  // warp 4: bulk copies and MMA issue
-// TMEM columns: layer-3 accumulators [0, 128) and [128, 256), layer 2 [256, 512).
-constexpr uint32_t kD2Col = 256;
+// TMEM columns: layer-3 accumulators [0, 256) and [256, 512); layer 2's
+// accumulator (two 128-point halves x 128 features) aliases the first one.
+constexpr uint32_t kD2Col = 0;
 
 // Barrier slots (uint64_t index from sBar).
 enum : int {
@@ -191,9 +192,12 @@ enum : int {
 // (bias, ReLU, bf16) into the swizzled B operand of layer 3, and drain the
 // layer-3 accumulators into the running max of their channel.  Warp 4 (one
 // elected lane) keeps a ring of three W3 tile images filled by bulk copies and
-// issues every MMA: layer 2 as two 128x128x64, layer 3 as sixteen
-// 128(channels)x128(points)x128 per 256-point chunk into two TMEM buffers, so
-// that the epilogue of one overlaps the MMA of the next.  Handoffs are
+// issues every MMA: layer 2 as two 128x128x64, layer 3 as eight
+// 128(channels)x256(points)x128 per 256-point chunk into two TMEM buffers, so
+// that the epilogue of one overlaps the MMA of the next (N = 256 halves the
+// shared-memory operand bytes per flop against N = 128).  Layer 2 writes the
+// first layer-3 buffer: it is issued after that buffer's last drain, and
+// layer 3 of the chunk starts only after layer 2 was read (the B3 handoff).  Handoffs are
 // mbarriers (MMA commits, bulk-copy byte counts, thread arrivals); every wait
 // is bounded and a timeout drains what this CTA issued before its TMEM is
 // freed.  kTrain also records the arg-max point per channel and stores the
@@ -259,32 +263,30 @@ __global__ void __launch_bounds__(kEncThreads, 1)
       const uint32_t id2 = tc::idesc_bf16_f32(128, 128), id3 = tc::idesc_bf16_f32(128, kGroupN);
       const uint32_t w2a = tc::smem_u32(sm + sW2), a1a = tc::smem_u32(sm + sA1), b3a = tc::smem_u32(sm + sB3);
       for (int C = 0; C < nchunks && ok && !*sflag; ++C) {
-        // layer 2: D2[point][feature] for the two 128-point halves of the chunk
+        // layer 2: D2[point][feature] for the two 128-point halves of the chunk,
+        // into layer-3 buffer 0 once its last group (8C - 2) was drained
         if (!(ok = tc::mbar_wait(&bar[kBarA1], C & 1))) break;
+        if (C > 0 && !(ok = tc::mbar_wait(&bar[kBarD3Empty], ((8 * C - 2) >> 1) & 1))) break;
         tc::tc_fence_after();
         for (int half = 0; half < 2; ++half)
           for (int s = 0; s < kF1 / 16; ++s)
             tc::mma_bf16(tmem + kD2Col + half * 128, tc::sdesc_sw128(a1a + half * 16384 + s * 32),
                          tc::sdesc_sw128(w2a + s * 32), id2, s > 0);
         tc::mma_commit(&bar[kBarD2]);
-        // layer 3: per W3 tile, two 128-point groups into alternating accumulators
+        // layer 3: one 256-point group per W3 tile, into alternating accumulators
         if (!(ok = tc::mbar_wait(&bar[kBarB3], C & 1))) break;
         tc::tc_fence_after();
         for (int ct = 0; ct < kF3 / 128 && ok; ++ct) {
           const int t = C * (kF3 / 128) + ct, rb = t % kW3Ring;
           if (!(ok = tc::mbar_wait(&bar[kBarW3Full + rb], (t / kW3Ring) & 1))) break;
           const uint32_t wa = tc::smem_u32(sm + sW3 + rb * kW3Tile);
-          for (int nh = 0; nh < 2; ++nh) {
-            const int G = 2 * t + nh, db = G & 1;
-            if (G >= 2 && !(ok = tc::mbar_wait(&bar[kBarD3Empty + db], ((G - 2) >> 1) & 1))) break;
-            tc::tc_fence_after();
-            for (int s = 0; s < kF2 / 16; ++s)
-              tc::mma_bf16(tmem + db * kGroupN, tc::sdesc_sw128(wa + (s >> 2) * 16384 + (s & 3) * 32),
-                           tc::sdesc_sw128(b3a + (s >> 2) * (kChunk * 128) + nh * (kGroupN * 128) + (s & 3) * 32),
-                           id3, s > 0);
-            tc::mma_commit(&bar[kBarD3Full + db]);
-          }
-          if (!ok) break;
+          const int G = t, db = G & 1;
+          if (G >= 2 && !(ok = tc::mbar_wait(&bar[kBarD3Empty + db], ((G - 2) >> 1) & 1))) break;
+          tc::tc_fence_after();
+          for (int s = 0; s < kF2 / 16; ++s)
+            tc::mma_bf16(tmem + db * kGroupN, tc::sdesc_sw128(wa + (s >> 2) * 16384 + (s & 3) * 32),
+                         tc::sdesc_sw128(b3a + (s >> 2) * (kChunk * 128) + (s & 3) * 32), id3, s > 0);
+          tc::mma_commit(&bar[kBarD3Full + db]);
           tc::mma_commit(&bar[kBarW3Empty + rb]);
           tiles_used = t + 1;
           // refill the slot of the previous tile (its MMAs are done or nearly) two tiles ahead
@@ -382,30 +384,32 @@ __global__ void __launch_bounds__(kEncThreads, 1)
       tc::mbar_arrive(&bar[kBarB3]);
       // ---- layer 1 of the next chunk (A operand free: this chunk's layer 2 completed)
       if (C + 1 < nchunks) layer1(C + 1);
-      // ---- layer-3 epilogues: the max over each group's 128 points
+      // ---- layer-3 epilogues: the max over the chunk's 256 points, 128 columns at a time
       for (int ct = 0; ct < kF3 / 128 && ok; ++ct) {
         const int ch = ct * 128 + tid;
         float best = run[ch];
         int barg = arg[ch];
+        const int G = C * (kF3 / 128) + ct, db = G & 1;
+        if (!(ok = tc::mbar_wait(&bar[kBarD3Full + db], (G >> 1) & 1))) break;
+        tc::tc_fence_after();
         for (int nh = 0; nh < 2; ++nh) {
-          const int G = 2 * (C * (kF3 / 128) + ct) + nh, db = G & 1;
-          if (!(ok = tc::mbar_wait(&bar[kBarD3Full + db], (G >> 1) & 1))) break;
-          tc::tc_fence_after();
-          float v[kGroupN];
-          tc::tmem_ld128(tmem + lane_base + db * kGroupN, v);
-          tc::tc_fence_before();
-          tc::mbar_arrive(&bar[kBarD3Empty + db]);  // the values are in registers: release the buffer
+          float v[128];
+          tc::tmem_ld128(tmem + lane_base + db * kGroupN + nh * 128, v);
+          if (nh == 1) {
+            tc::tc_fence_before();
+            tc::mbar_arrive(&bar[kBarD3Empty + db]);  // the values are in registers: release the buffer
+          }
           if (kTrain) {
 #pragma unroll
-            for (int i = 0; i < kGroupN; ++i)
+            for (int i = 0; i < 128; ++i)
               if (v[i] > best) {
                 best = v[i];
-                barg = pc * kChunk + nh * kGroupN + i;
+                barg = pc * kChunk + nh * 128 + i;
               }
           } else {
             float m0 = v[0], m1 = v[1], m2 = v[2], m3 = v[3];  // four independent chains
 #pragma unroll
-            for (int i = 4; i < kGroupN; i += 4) {
+            for (int i = 4; i < 128; i += 4) {
               m0 = fmaxf(m0, v[i]);
               m1 = fmaxf(m1, v[i + 1]);
               m2 = fmaxf(m2, v[i + 2]);

@@ -170,6 +170,11 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
 
     # moments of the source cloud for the RMSE check (outside the timed region)
     src0, tgt0, res0 = step(True)
+    # launch shapes for this cloud size and device (untimed; both contexts use them)
+    v0 = ctx.voxel_grid(ctx.backproject_device(d_frames[0].data_ptr(), params), 0.001)
+    tune = ctx.autotune(v0, tgt0)
+    ctxs[1].tune_set(tune["sor_warps"], tune["normals_warps"], tune["icp_blocks_per_sm"])
+    del v0
     xs = xyz_of(src0.download()).astype(np.float64)
     m1, m2, nsrc = xs.mean(0), (xs.T @ xs) / len(xs), len(xs)
     ntgt = len(tgt0)
@@ -254,7 +259,9 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
                    "parallelism": f"replicas x{world}; per pair the two captures run concurrently on two streams",
                    "stage_ms_per_step": {k: round(v / args.steps, 4) for k, v in stage_ms.items() if k != "icp_iters"},
                    "stage_ms_note": "summed over both captures, which overlap in time",
-                   "icp_iterations_per_step": stage_ms.get("icp_iters", 0) / args.steps},
+                   "icp_iterations_per_step": stage_ms.get("icp_iters", 0) / args.steps,
+                   "launch_shapes": {k: tune[k] for k in ("sor_warps", "normals_warps", "icp_blocks_per_sm")},
+                   "autotune_ms": {k: tune[k] for k in ("sor_ms", "normals_ms", "icp_ms")}},
         "roofline": {"kernel": "k_sor_dist (SOR k-NN pass, k=51)", "bound": "hbm",
                      "achieved": round(achieved, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / pk["hbm_gbs"], 5), "peak_src": pk["src"],

@@ -238,6 +238,33 @@ LCR_API lcr_status lcr_correspondences(lcr_ctx* ctx, const lcr_cloud* src, const
 LCR_API lcr_status lcr_knn(lcr_ctx* ctx, const lcr_cloud* ref, const lcr_cloud* query, int k, float max_dist_sq,
                            int32_t* idx, float* dist);
 
+/* ------------------------------------------------------------ autotuning */
+/* Launch shapes of the search kernels.  Every result is independent of them;
+ * only the speed changes. */
+typedef struct lcr_tune {
+  int sor_warps;          /* warps per block of the SOR k-NN kernel, 1-8 (default 5) */
+  int normals_warps;      /* warps per block of the NormalEstimation k-NN kernels, 1-8 (default 5) */
+  int icp_blocks_per_sm;  /* persistent blocks per SM of the batched ICP kernels, 1-8 (default 4) */
+} lcr_tune;
+LCR_API lcr_status lcr_tune_get(lcr_ctx* ctx, lcr_tune* t);
+LCR_API lcr_status lcr_tune_set(lcr_ctx* ctx, const lcr_tune* t);
+
+typedef struct lcr_tune_report {
+  lcr_tune chosen;
+  int from_cache;          /* 1: read from the cache file, nothing timed */
+  double sor_ms[8];        /* SOR k-NN kernel time per candidate (index warps - 1; 0 = not a candidate) */
+  double normals_ms[8];    /* NormalEstimation k-NN kernel time per candidate */
+  double icp_ms[8];        /* one point-to-point ICP of src onto tgt per candidate blocks per SM */
+} lcr_tune_report;
+/* Times the candidate shapes on a representative pair (clouds of the size the
+ * context will process: SOR k=50 and normals k=30 on src, ICP of src onto
+ * tgt), applies the fastest, and when cache_path is not NULL appends the
+ * choice there (one JSON object per line, keyed by the device name, its SM
+ * count and floor(log2 n_src)); a later call with the same key reads the file
+ * instead of timing.  src needs more than 50 points. */
+LCR_API lcr_status lcr_autotune(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const char* cache_path,
+                                lcr_tune_report* report);
+
 /* ------------------------------------------------ synthetic capture pairs */
 /* Seeded capture pairs generated on the GPU (training and evaluation data of
  * the pose proposal): a superquadric object (semi-axes 0.05-0.2 m, exponents

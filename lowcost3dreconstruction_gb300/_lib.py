@@ -85,6 +85,15 @@ class SynthParams(C.Structure):
     _fields_ = [("yaw_deg", C.c_float), ("tilt_deg", C.c_float), ("translation", C.c_float), ("noise", C.c_int)]
 
 
+class Tune(C.Structure):
+    _fields_ = [("sor_warps", C.c_int), ("normals_warps", C.c_int), ("icp_blocks_per_sm", C.c_int)]
+
+
+class TuneReport(C.Structure):
+    _fields_ = [("chosen", Tune), ("from_cache", C.c_int), ("sor_ms", C.c_double * 8),
+                ("normals_ms", C.c_double * 8), ("icp_ms", C.c_double * 8)]
+
+
 _VP = C.c_void_p
 _SIGS = {
     "lcr_ctx_create": (C.c_int, [C.POINTER(_VP), C.c_int]),
@@ -123,6 +132,9 @@ _SIGS = {
     "lcr_centroid": (C.c_int, [_VP, _VP, _VP]),
     "lcr_centroid_align": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_double, C.c_double, C.c_double,
                                      C.POINTER(_VP), _VP]),
+    "lcr_tune_get": (C.c_int, [_VP, C.POINTER(Tune)]),
+    "lcr_tune_set": (C.c_int, [_VP, C.POINTER(Tune)]),
+    "lcr_autotune": (C.c_int, [_VP, _VP, _VP, C.c_char_p, C.POINTER(TuneReport)]),
     "lcr_synthetic_pairs": (C.c_int, [_VP, C.c_uint64, C.c_size_t, C.c_int, C.POINTER(SynthParams), _VP, _VP,
                                       _VP]),
     "lcr_rmse_batch": (C.c_int, [_VP, _VP, C.c_size_t, _VP, _VP, _VP]),

@@ -313,3 +313,23 @@ class Context:
         hs = (C.c_void_p * max(n, 1))(*[c.handle for c in clouds])
         self._check(self.lib.lcr_rmse_batch(self.h, hs, n, L.ptr(a), L.ptr(b), L.ptr(out)))
         return out[:n]
+
+    # ------------------------------------------------------------- autotuning
+    def tune_get(self) -> dict:
+        t = L.Tune()
+        self._check(self.lib.lcr_tune_get(self.h, C.byref(t)))
+        return {"sor_warps": t.sor_warps, "normals_warps": t.normals_warps, "icp_blocks_per_sm": t.icp_blocks_per_sm}
+
+    def tune_set(self, sor_warps: int, normals_warps: int, icp_blocks_per_sm: int) -> None:
+        t = L.Tune(sor_warps, normals_warps, icp_blocks_per_sm)
+        self._check(self.lib.lcr_tune_set(self.h, C.byref(t)))
+
+    def autotune(self, src: Cloud, tgt: Cloud, cache_path: str | None = None) -> dict:
+        """lcr_autotune: times the candidate launch shapes on (src, tgt) and applies the fastest."""
+        r = L.TuneReport()
+        self._check(self.lib.lcr_autotune(self.h, src.handle, tgt.handle,
+                                          cache_path.encode() if cache_path else None, C.byref(r)))
+        ms = lambda a: {i + 1: round(a[i], 4) for i in range(8) if a[i] > 0}
+        return {"sor_warps": r.chosen.sor_warps, "normals_warps": r.chosen.normals_warps,
+                "icp_blocks_per_sm": r.chosen.icp_blocks_per_sm, "from_cache": bool(r.from_cache),
+                "sor_ms": ms(r.sor_ms), "normals_ms": ms(r.normals_ms), "icp_ms": ms(r.icp_ms)}

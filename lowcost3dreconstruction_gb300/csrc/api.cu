@@ -560,6 +560,34 @@ constexpr size_t kMaxPairs = 1u << 16;
 
 extern "C" {
 
+lcr_status lcr_tune_get(lcr_ctx* ctx, lcr_tune* t) {
+  API_BEGIN(ctx)
+  REQUIRE(t, "null argument");
+  *t = tune_current(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_tune_set(lcr_ctx* ctx, const lcr_tune* t) {
+  API_BEGIN(ctx)
+  REQUIRE(t, "null argument");
+  sync(ctx);
+  tune_apply(ctx, *t);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_autotune(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const char* cache_path,
+                        lcr_tune_report* report) {
+  API_BEGIN(ctx)
+  REQUIRE(src && tgt && report, "null argument");
+  REQUIRE(src->n > 64 && tgt->n > 0, "autotuning needs a source of more than 64 points and a target");
+  autotune_run(ctx, src, tgt, cache_path, report);
+  sync(ctx);
+  API_END(ctx)
+  return LCR_OK;
+}
+
 lcr_status lcr_synthetic_pairs(lcr_ctx* ctx, uint64_t seed, size_t npairs, int points, const lcr_synth_params* p,
                                lcr_cloud** src, lcr_cloud** tgt, float* transforms) {
   API_BEGIN(ctx)

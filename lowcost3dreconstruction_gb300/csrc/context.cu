@@ -261,3 +261,20 @@ void centroid_run(lcr_ctx* ctx, const lcr_cloud* in, double* c4) {
   sync(ctx);
   for (int i = 0; i < 4; ++i) c4[i] = h[i];
 }
+
+double kernel_time_take(lcr_ctx* ctx, int which) {
+  sync(ctx);
+  auto& t = ctx->kt[which];
+  double ms = t.ms;
+  for (auto& e : t.pending) {
+    float v = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&v, e.first, e.second));
+    ms += v;
+    ctx->event_pool.push_back(e.first);
+    ctx->event_pool.push_back(e.second);
+  }
+  t.pending.clear();
+  t.ms = 0.0;
+  t.launches = 0;
+  return ms;
+}

@@ -590,9 +590,9 @@ __global__ void k_rank_of(const uint32_t* __restrict__ kept, int nkeep, uint32_t
   if (j < nkeep) rank[kept[j]] = static_cast<uint32_t>(j);
 }
 
-// Warps per block of the unordered k-NN kernels (11 KB of shared memory per
-// warp: 5 warps x 4 blocks = 20 resident warps per SM).
-constexpr int kSetWarps = 5;
+// Warps per block of the unordered k-NN kernels come from ctx->tune (11 KB of
+// shared memory per warp; the default 5 warps x 4 blocks = 20 resident warps
+// per SM).  Every per-query result is independent of the block shape.
 
 // Queue of tiles the unordered form hands to the sorted form: [0] = count,
 // [1..] = tile ids.  Its grid: one block per SM, warps striding the queue.
@@ -622,7 +622,8 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
   const int nw = K <= 64 ? 4 : 2;
   const size_t smem = list_smem(nw, K);
   if (smem > 227 * 1024) LCR_THROW(LCR_ERR_INVALID_ARG, "mean_k=%d too large", mean_k);
-  const size_t smem_set = kSetWarps * kset_warp_bytes();
+  const int set_warps = ctx->tune.sor_warps;
+  const size_t smem_set = set_warps * kset_warp_bytes();
   float* dist = static_cast<float*>(dev_alloc(ctx, sizeof(float) * n));
   uint8_t* flags = static_cast<uint8_t*>(dev_alloc(ctx, 3 * static_cast<size_t>(n)));
   uint8_t* valid = flags, *keep = flags + n, *drop = flags + 2 * static_cast<size_t>(n);
@@ -657,7 +658,7 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
                                 static_cast<int>(smem)));
   {
     KernelTimer kt(ctx, LCR_KT_SOR_KNN);
-    LCR_LAUNCH(ctx, k_sor_dist, (ix.nleaf + kSetWarps - 1) / kSetWarps, kSetWarps * 32, smem_set, ix, mean_k, dist,
+    LCR_LAUNCH(ctx, k_sor_dist, (ix.nleaf + set_warps - 1) / set_warps, set_warps * 32, smem_set, ix, mean_k, dist,
                valid, nvalid, rq.tiles(), rq.count(), too_few, lists);
   }
   LCR_LAUNCH(ctx, k_sor_dist_sorted, ctx->sms, nw * 32, smem, ix, mean_k, dist, valid, nvalid, rq.tiles(), rq.count(),
@@ -744,7 +745,8 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
   CUDA_TRY(cudaMemcpyAsync(out->rgb, in->rgb, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
   // non-finite points keep NaN normals (they are not searched)
   CUDA_TRY(cudaMemsetAsync(out->nrm, 0xff, sizeof(float4) * n, ctx->stream));
-  const size_t smem_set = kSetWarps * kset_warp_bytes();
+  const int set_warps = ctx->tune.ne_warps;
+  const size_t smem_set = set_warps * kset_warp_bytes();
   const int flip = (flags & LCR_NORMALS_FLIP_ALL) ? 1 : 0;
   const NbrHint* h = in->nbr;
   if (h && k <= h->K && h->K <= kListMaxK) {
@@ -763,7 +765,7 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
     CUDA_TRY(cudaFuncSetAttribute(k_normals_queued, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(smem_set)));
     LCR_LAUNCH(ctx, k_index_pos, (ix.nleaf * 32 + 255) / 256, 256, 0, ix, pos);
-    LCR_LAUNCH(ctx, k_normals_queued, ctx->sms * 2, kSetWarps * 32, smem_set, ix, k, in->xyz, vp[0], vp[1], vp[2],
+    LCR_LAUNCH(ctx, k_normals_queued, ctx->sms * 2, set_warps * 32, smem_set, ix, k, in->xyz, vp[0], vp[1], vp[2],
                flip, out->nrm, queue, nq, h->keys, h->K, h->kept, pos);
     dev_free(ctx, tmp);
     // the lists (8 B x (k+1) per point) are released once consumed: a second
@@ -777,7 +779,7 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
   CUDA_TRY(cudaFuncSetAttribute(k_normals, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_set)));
   {
     KernelTimer kt(ctx, LCR_KT_NORMALS_KNN);
-    LCR_LAUNCH(ctx, k_normals, (ix.nleaf + kSetWarps - 1) / kSetWarps, kSetWarps * 32, smem_set, ix, k, in->xyz,
+    LCR_LAUNCH(ctx, k_normals, (ix.nleaf + set_warps - 1) / set_warps, set_warps * 32, smem_set, ix, k, in->xyz,
                vp[0], vp[1], vp[2], flip, out->nrm);
   }
   out->index = share_index(in->index);  // same points in the same order

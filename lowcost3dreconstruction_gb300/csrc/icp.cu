@@ -877,7 +877,7 @@ __global__ void __launch_bounds__(kIcpThreads) k_centroid_final(const BatchDesc*
   }
 }
 
-int icp_grid(lcr_ctx* ctx) { return ctx->sms * 4; }
+int icp_grid(lcr_ctx* ctx) { return ctx->sms * ctx->tune.icp_bps; }
 int reduce_grid(lcr_ctx* ctx) { return ctx->sms * 2; }
 
 // Persistent per-context block: the descriptor, then the counters.
@@ -1149,4 +1149,13 @@ void icp_batch_run(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* c
 void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr_icp_params* p, const float* guess,
              lcr_icp_result* res) {
   icp_batch_run(ctx, &src, &tgt, 1, p, guess, res);
+}
+
+void icp_graphs_reset(lcr_ctx* ctx) {
+  for (auto& per_method : ctx->icp_exec)
+    for (cudaGraphExec_t& e : per_method)
+      if (e) {
+        cudaGraphExecDestroy(e);
+        e = nullptr;
+      }
 }

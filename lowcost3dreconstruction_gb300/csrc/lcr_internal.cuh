@@ -118,6 +118,12 @@ struct lcr_ctx {
     uint64_t launches = 0;
   } kt[LCR_KT_COUNT];
   std::vector<cudaEvent_t> event_pool;
+  // launch shapes (lcr_tune_set / lcr_autotune); the defaults are the hand-tuned ones
+  struct Tune {
+    int sor_warps = 5;      // warps per block of k_sor_dist
+    int ne_warps = 5;       // warps per block of k_normals, k_normals_queued
+    int icp_bps = 4;        // persistent blocks per SM of the batched ICP search kernels
+  } tune;
 };
 
 // Brackets one launch with events when timing is on (see lcr_kernel_timing).
@@ -250,6 +256,15 @@ lcr_cloud* voxel_run(lcr_ctx* ctx, const lcr_cloud* in, float lx, float ly, floa
 void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_cloud** inliers,
              lcr_cloud** outliers, lcr_sor_stats* stats, float* host_dist);
 lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[3], int flags);
+// Launch-shape tuning (tune.cu).
+void tune_apply(lcr_ctx* ctx, const lcr_tune& t);
+lcr_tune tune_current(const lcr_ctx* ctx);
+void autotune_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const char* cache_path,
+                  lcr_tune_report* rep);
+// Drops the captured ICP loops (their launch shapes changed).
+void icp_graphs_reset(lcr_ctx* ctx);
+// Takes the accumulated event time of a timed kernel (ms) and clears it.
+double kernel_time_take(lcr_ctx* ctx, int which);
 void icp_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr_icp_params* p, const float* guess,
              lcr_icp_result* res);
 void icp_batch_run(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* const* tgt, int npairs,

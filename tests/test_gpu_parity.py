@@ -485,3 +485,34 @@ def test_empty_cloud_errors(ctx):
         ctx.icp(e, e, ctx.icp_params())
     assert ex.value.status == L.EMPTY
     assert len(ctx.voxel_grid(e, 0.01).download()) == 0
+
+
+# ------------------------------------------------------------- autotuning
+@pytest.mark.gpu
+def test_launch_shapes_do_not_change_results(ctx, cfg0, tmp_path):
+    """SOR distances, normals and ICP are bit-identical under every launch
+    shape the autotuner can pick; the tuning cache round-trips."""
+    from lowcost3dreconstruction_gb300.core import normals_of
+    v, t = ctx.upload(cfg0["vsrc"]), ctx.upload(cfg0["vtgt"])
+    prm = ctx.icp_params(max_correspondence_distance=0.05, max_iterations=30, transformation_epsilon=1e-8)
+    base = ctx.tune_get()
+    outs = []
+    for shape in ((2, 2, 2), (8, 8, 8), (3, 6, 1), (5, 5, 4)):
+        ctx.tune_set(*shape)
+        d, _ = ctx.sor_distances(v, 50)
+        n = normals_of(ctx.normals(v, 30).download())
+        r = ctx.icp_batch([v], [t], prm)[0]
+        outs.append((d.view(np.uint32), n.view(np.uint32), r.transform64, r.iterations))
+    for o in outs[1:]:
+        np.testing.assert_array_equal(o[0], outs[0][0])
+        np.testing.assert_array_equal(o[1], outs[0][1])
+        np.testing.assert_array_equal(o[2], outs[0][2])
+        assert o[3] == outs[0][3]
+    cache = tmp_path / "tune.jsonl"
+    first = ctx.autotune(v, t, str(cache))
+    assert not first["from_cache"] and set(first["sor_ms"]) == {2, 3, 4, 5, 6, 8}
+    again = ctx.autotune(v, t, str(cache))
+    assert again["from_cache"]
+    assert [again[k] for k in ("sor_warps", "normals_warps", "icp_blocks_per_sm")] == \
+        [first[k] for k in ("sor_warps", "normals_warps", "icp_blocks_per_sm")]
+    ctx.tune_set(base["sor_warps"], base["normals_warps"], base["icp_blocks_per_sm"])

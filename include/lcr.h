@@ -353,6 +353,9 @@ LCR_API lcr_status lcr_crop_redundant(lcr_ctx* ctx, const lcr_cloud* src, const 
                                       uint8_t* removed);
 
 /* ---------------------------------------------------- transforms, centroid */
+/* pcl::removeNaNFromPointCloud (rotate_align/rotate_align.cpp:201): the points
+ * with finite x, y, z, in their order. */
+LCR_API lcr_status lcr_remove_nan(lcr_ctx* ctx, const lcr_cloud* in, lcr_cloud** out);
 /* pcl::transformPointCloudWithNormals with a row-major 4x4 (pcl_tools/transform.cpp:90,
  * scale.cpp:70 with diag(s,s,s,1), and inside every ICP iteration). */
 LCR_API lcr_status lcr_transform(lcr_ctx* ctx, const lcr_cloud* in, const float m[16], lcr_cloud** out);

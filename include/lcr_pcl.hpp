@@ -234,6 +234,14 @@ inline void compute3DCentroid(const PointCloud& cloud, std::array<float, 4>& c,
   ctx.check(lcr_centroid(ctx.get(), d.get(), c.data()));
 }
 
+inline void removeNaNFromPointCloud(const PointCloud& in, PointCloud& out,
+                                   const Context& ctx = Context::thread_default()) {
+  DeviceCloud d(ctx, in);
+  lcr_cloud* o = nullptr;
+  ctx.check(lcr_remove_nan(ctx.get(), d.get(), &o));
+  DeviceCloud(ctx, o).download(out);
+}
+
 inline void transformPointCloudWithNormals(const PointCloud& in, PointCloud& out, const Matrix4f& T,
                                            const Context& ctx = Context::thread_default()) {
   DeviceCloud d(ctx, in);

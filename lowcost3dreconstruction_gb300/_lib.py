@@ -128,6 +128,7 @@ _SIGS = {
     "lcr_accumulate": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_int, C.c_double, C.c_int, C.POINTER(_VP),
                                  C.POINTER(_VP)]),
     "lcr_crop_redundant": (C.c_int, [_VP, _VP, _VP, C.c_double, _VP]),
+    "lcr_remove_nan": (C.c_int, [_VP, _VP, C.POINTER(_VP)]),
     "lcr_transform": (C.c_int, [_VP, _VP, _VP, C.POINTER(_VP)]),
     "lcr_centroid": (C.c_int, [_VP, _VP, _VP]),
     "lcr_centroid_align": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_double, C.c_double, C.c_double,

@@ -276,6 +276,10 @@ class Context:
         return Cloud(self, out), Cloud(self, rem)
 
     # ------------------------------------------------- transforms, centroid
+    def remove_nan(self, cloud: Cloud) -> Cloud:
+        """pcl::removeNaNFromPointCloud."""
+        return self._cloud(self.lib.lcr_remove_nan, cloud.handle)
+
     def transform(self, cloud: Cloud, m: np.ndarray) -> Cloud:
         m = np.ascontiguousarray(m, dtype=np.float32).reshape(16)
         return self._cloud(self.lib.lcr_transform, cloud.handle, L.ptr(m))

@@ -35,6 +35,14 @@ namespace {
     if (!(cond)) LCR_THROW(LCR_ERR_INVALID_ARG, __VA_ARGS__); \
   } while (0)
 
+__global__ void k_finite_flags(const float4* __restrict__ xyz, size_t n, uint8_t* __restrict__ out) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float4 p = xyz[i];
+    out[i] = finite3(p.x, p.y, p.z) ? 1 : 0;
+  }
+}
+
 __global__ void k_invert(const uint8_t* __restrict__ in, size_t n, uint8_t* __restrict__ out) {
   const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < n) out[i] = in[i] ? 0 : 1;
@@ -559,6 +567,28 @@ constexpr size_t kMaxPairs = 1u << 16;
 }  // namespace
 
 extern "C" {
+
+lcr_status lcr_remove_nan(lcr_ctx* ctx, const lcr_cloud* in, lcr_cloud** out) {
+  API_BEGIN(ctx)
+  REQUIRE(in && out, "null argument");
+  *out = nullptr;
+  const size_t n = in->n;
+  uint8_t* keep = static_cast<uint8_t*>(dev_alloc(ctx, n + 16));
+  uint32_t* idx = static_cast<uint32_t*>(dev_alloc(ctx, 4 * n + 16));
+  int nk = 0;
+  if (n) {
+    LCR_LAUNCH(ctx, k_finite_flags, static_cast<unsigned>((n + 255) / 256), 256, 0, in->xyz, n, keep);
+    nk = compact_flags(ctx, keep, static_cast<int>(n), idx);
+  }
+  lcr_cloud* o = cloud_alloc(ctx, nk);
+  gather_cloud(ctx, in, idx, nk, o);
+  dev_free(ctx, keep);
+  dev_free(ctx, idx);
+  sync(ctx);
+  *out = o;
+  API_END(ctx)
+  return LCR_OK;
+}
 
 lcr_status lcr_tune_get(lcr_ctx* ctx, lcr_tune* t) {
   API_BEGIN(ctx)

@@ -102,3 +102,58 @@ def test_tools_chain_matches_oracle(tmp_path, cfg0):
     reg = L.read_ply(tmp_path / "reg.ply")
     want = O.transform(cfg0["vsrc"], ref["transform"].astype(np.float32))
     np.testing.assert_allclose(reg["x"], want["x"], atol=2e-5)
+
+
+# ------------------------------------------------------------ rotate_align
+def test_rotate_align_help_and_gui():
+    r = run("rotate_align", "-h")
+    assert r.returncode == 0
+    for f in ("--gui", "--accumulated_file", "--capture_name", "--capture_step", "--num_captures", "--distance_x",
+              "--distance_y", "--distance_z"):
+        assert f in r.stdout, f
+    r = run("rotate_align", "-g")
+    assert r.returncode == 255 and "not available" in r.stderr
+
+
+def test_rotate_align_missing_captures(tmp_path):
+    """Unreadable views are reported and stay empty; the tool still writes every output."""
+    r = run("rotate_align", "-n", "cap", "-s", "10", "-c", "2", cwd=tmp_path)
+    assert r.returncode == 0
+    assert "cap0.ply is not a valid file." in r.stdout and "cap10.ply is not a valid file." in r.stdout
+    from lowcost3dreconstruction_gb300 import _lib as L
+    for a in (0, 10):
+        assert len(L.read_ply(tmp_path / f"cap{a}_rotated.ply")) == 0
+
+
+@pytest.mark.gpu
+def test_rotate_align_matches_oracle(tmp_path):
+    from lowcost3dreconstruction_gb300 import _lib as L
+    from oracle import oracle as O
+    rng = np.random.default_rng(3)
+    views = []
+    for i in range(3):
+        p = random_cloud(500 + 100 * i, 10 + i)
+        p["x"][::50] = np.nan
+        L.write_ply(tmp_path / f"v{20 * i}.ply", p)
+        views.append(p)
+    r = run("rotate_align", "-n", "v", "-s", "20", "-c", "3", "-a", "all.ply", "-x", "1.5", "-y", "-2", "-z", "30",
+            cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.count("LOADED ALRIGHT!") == 3
+    acc = []
+    for i, p in enumerate(views):
+        fin = p[np.isfinite(p["x"]) & np.isfinite(p["y"]) & np.isfinite(p["z"])]
+        T = np.eye(4, dtype=np.float32)
+        T[:3, 3] = [1.5, -2.0, 30.0]
+        a = np.float32(-((20 * i + i * 1.17) * 0.017453293))
+        c, s = np.float32(np.cos(a)), np.float32(np.sin(a))
+        R = np.eye(4, dtype=np.float32)
+        R[0, 0], R[2, 2], R[0, 2], R[2, 0] = c, c, s, -s
+        want = O.transform(O.transform(fin, T), R)
+        got = L.read_ply(tmp_path / f"v{20 * i}_rotated.ply")
+        assert len(got) == len(want)
+        for f in ("x", "y", "z", "normal_x", "normal_y", "normal_z"):
+            np.testing.assert_allclose(got[f], want[f], rtol=1e-6, atol=1e-5, err_msg=f)
+        acc.append(got)
+    allp = L.read_ply(tmp_path / "all.ply")
+    np.testing.assert_array_equal(allp["x"], np.concatenate([a["x"] for a in acc]))

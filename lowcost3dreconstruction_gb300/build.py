@@ -33,7 +33,7 @@ CU_SOURCES = ["api.cu", "context.cu", "sort.cu", "index.cu", "knn.cu", "icp.cu",
               "filters.cu", "posenet.cu", "posenet_train.cu", "synth.cu", "tune.cu"]
 HOST_SOURCES = ["ply.cpp"]
 TOOLS = ["fine_registration", "cloud_downsampling", "outlier_removal", "normal_estimation", "accumulate_clouds",
-         "transform", "scale", "centroid_align", "depth_to_cloud", "rotate_align"]
+         "transform", "scale", "centroid_align", "depth_to_cloud", "rotate_align", "pose_proposal"]
 
 
 def _nvcc() -> str:

@@ -157,3 +157,39 @@ def test_rotate_align_matches_oracle(tmp_path):
         acc.append(got)
     allp = L.read_ply(tmp_path / "all.ply")
     np.testing.assert_array_equal(allp["x"], np.concatenate([a["x"] for a in acc]))
+
+
+# ------------------------------------------------------------ pose_proposal
+def test_pose_proposal_usage():
+    r = run("pose_proposal", "-h")
+    assert r.returncode == 0
+    for f in ("--input", "--matrix", "--registered", "--units", "--refine", "--weights"):
+        assert f in r.stdout, f
+    r = run("pose_proposal", "-i", "only_one.ply")
+    assert r.returncode == 255 and "Correct mode of use" in (r.stdout + r.stderr)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("units", [1.0, 0.1])
+def test_pose_proposal_drops_into_the_coarse_stage(tmp_path, ctx, units):
+    """Super4PCS's place in alignment.sh: matrix file with two header lines
+    (deleted by the script), then `transform -t` moves Q onto P."""
+    from lowcost3dreconstruction_gb300 import _lib as L
+    from lowcost3dreconstruction_gb300 import train_posenet as TP
+    src, tgt, T = ctx.synthetic_pairs(424_242, 1, 20000, yaw_deg=60.0)
+    q, p = src[0].download(), tgt[0].download()
+    for c in (q, p):
+        for f in ("x", "y", "z"):
+            c[f] /= np.float32(units)
+    L.write_ply(tmp_path / "P.ply", p)
+    L.write_ply(tmp_path / "Q.ply", q)
+    r = run("pose_proposal", "-i", tmp_path / "P.ply", tmp_path / "Q.ply", "-m", tmp_path / "m.txt", "-r",
+            tmp_path / "reg.ply", "-t", "15", "-o", "0.6", "-d", "0.03", "-n", "700", "-u", str(units))
+    assert r.returncode == 0, r.stderr
+    lines = (tmp_path / "m.txt").read_text().splitlines()
+    M = np.array([[float(v) for v in ln.split()] for ln in lines[2:6]])
+    assert TP.rotation_error_deg(M[None], T)[0] < 2.0
+    np.testing.assert_allclose(M[:3, 3] * units, T[0, :3, 3], atol=0.01)
+    (tmp_path / "t.txt").write_text("\n".join(lines[2:]) + "\n")   # sed -i '1,2d'
+    assert run("transform", "-i", tmp_path / "Q.ply", "-o", tmp_path / "q2.ply", "-t", tmp_path / "t.txt").returncode == 0
+    np.testing.assert_allclose(L.read_ply(tmp_path / "q2.ply")["x"], L.read_ply(tmp_path / "reg.ply")["x"], atol=1e-4)

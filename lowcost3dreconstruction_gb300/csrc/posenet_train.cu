@@ -1,7 +1,8 @@
 // Pose proposal: pair head (forward and backward), loss, encoder backward,
 // AdamW, and the conversions between the network's output and 4x4 poses.
 //
-// All of it runs on the CUDA cores with one thread per output and a fixed
+// The head's forward layers are tcgen05 GEMMs (k_gemm_tc).  The backward
+// pass runs on the CUDA cores with one thread per output and a fixed
 // summation order, so gradients are bit-reproducible run to run.  The
 // encoder's max-pool makes its backward sparse: a pooled channel's gradient
 // flows only into the point that won the max, so dW3 is a gather over the
@@ -12,6 +13,7 @@
 #include <cmath>
 
 #include "posenet.cuh"
+#include "tc.cuh"
 
 using bf16 = __nv_bfloat16;
 
@@ -97,6 +99,123 @@ void gemm(lcr_ctx* ctx, int M, int N, int K, const TA* A, long long sam, long lo
   if (M == 0 || N == 0) return;
   const dim3 grid((N + 63) / 64, (M + 63) / 64);
   LCR_LAUNCH(ctx, (k_gemm<TA, TB>), grid, 256, 0, M, N, K, A, sam, sak, B, sbn, sbk, e);
+}
+
+// ------------------------------------------------------ tensor-core GEMM
+// C[m][n] = act(sum_k A[m][k] B[n][k] + bias[n]) with A [M][K] and B [N][K]
+// bf16 row-major (both K-major), fp32 accumulation in TMEM: the head's
+// forward layers.  One CTA (4 warps) per 128-row tile of A and NT-column tile
+// of B.  K runs in 64-wide steps through two shared-memory stages: the threads
+// copy one step's tiles into the 128-byte swizzled layout while the tensor
+// core multiplies the previous step's (one elected thread issues four
+// 128 x NT x 16 MMAs per step).  Thread t then reads TMEM lane t (row m0 + t)
+// for the epilogue.  Rows past M and columns past N are zero-filled on load
+// and skipped on store.  K must be a multiple of 64.  Every wait is bounded;
+// a timeout drains the MMAs issued and raises *err.
+template <int NT>
+__global__ void __launch_bounds__(128) k_gemm_tc(int M, int N, int K, const bf16* __restrict__ A,
+                                                 const bf16* __restrict__ Bm, Epi e, int* __restrict__ err) {
+  constexpr int kATile = 128 * 128;  // 128 rows x 64 bf16
+  constexpr int kBTile = NT * 128;
+  constexpr int kStage = kATile + kBTile;
+  constexpr int kCols = NT < 32 ? 32 : NT;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* sm = smem_raw + ((1024u - (tc::smem_u32(smem_raw) & 1023u)) & 1023u);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * kStage);  // [0..1] stage MMAs done, [2] drain
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 3);
+  volatile int* flag = reinterpret_cast<volatile int*>(tslot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int m0 = blockIdx.y * 128, n0 = blockIdx.x * NT;
+  if (tid == 0) {
+    for (int i = 0; i < 3; ++i) tc::mbar_init(&bar[i], 1);
+    *flag = 0;
+    tc::mbar_fence_init();
+  }
+  if (warp == 0) tc::tmem_alloc<kCols>(tslot);
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tslot;
+  auto load = [&](int ks, int st) {
+    unsigned char* a = sm + st * kStage;
+    unsigned char* b = a + kATile;
+    const int k0 = ks * 64;
+    for (int i = tid; i < 128 * 8; i += 128) {
+      const int r = i >> 3, c = i & 7;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (m0 + r < M) v = *reinterpret_cast<const uint4*>(A + static_cast<size_t>(m0 + r) * K + k0 + c * 8);
+      *reinterpret_cast<uint4*>(a + r * 128 + ((c ^ (r & 7)) << 4)) = v;
+    }
+    for (int i = tid; i < NT * 8; i += 128) {
+      const int r = i >> 3, c = i & 7;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (n0 + r < N) v = *reinterpret_cast<const uint4*>(Bm + static_cast<size_t>(n0 + r) * K + k0 + c * 8);
+      *reinterpret_cast<uint4*>(b + r * 128 + ((c ^ (r & 7)) << 4)) = v;
+    }
+    tc::fence_async_smem();
+  };
+  const uint32_t idesc = tc::idesc_bf16_f32(128, NT);
+  const int nk = K / 64;
+  uint32_t ph[2] = {0u, 0u};
+  load(0, 0);
+  for (int ks = 0; ks < nk; ++ks) {
+    const int st = ks & 1;
+    __syncthreads();  // the stage is written by every thread
+    if (*flag) break;
+    if (tid == 0) {
+      tc::tc_fence_after();
+      const uint32_t a = tc::smem_u32(sm + st * kStage), b = a + kATile;
+      for (int s = 0; s < 4; ++s)
+        tc::mma_bf16(tmem, tc::sdesc_sw128(a + s * 32), tc::sdesc_sw128(b + s * 32), idesc, ks > 0 || s > 0);
+      tc::mma_commit(&bar[st]);
+    }
+    if (ks + 1 < nk) {
+      // the other stage was read by step ks-1's MMAs
+      if (ks >= 1) {
+        if (!tc::mbar_wait(&bar[st ^ 1], ph[st ^ 1])) *flag = 1;
+        ph[st ^ 1] ^= 1;
+      }
+      load(ks + 1, st ^ 1);
+    }
+  }
+  __syncthreads();
+  if (tid == 0) tc::mma_commit(&bar[2]);  // behind every MMA issued
+  if (!tc::mbar_wait(&bar[2], 0)) *flag = 1;
+  tc::tc_fence_after();
+  const uint32_t lane_base = static_cast<uint32_t>(warp * 32) << 16;
+  const int m = m0 + tid;
+  for (int c0 = 0; c0 < NT; c0 += 32) {
+    float v[32];
+    tc::tmem_ld32(tmem + lane_base + c0, v);
+    if (m >= M || *flag) continue;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int n = n0 + c0 + j;
+      if (c0 + j >= NT || n >= N) break;
+      float x = v[j];
+      if (e.bias) x += e.bias[n];
+      if (e.relu) x = fmaxf(x, 0.f);
+      if (e.out) e.out[m * e.ldo + n] = x;
+      if (e.outb) e.outb[m * e.ldo + n] = __float2bfloat16_rn(x);
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc::tc_fence_after();
+    tc::tmem_free<kCols>(tmem);
+  }
+  if (*flag && tid == 0) atomicExch(err, 1);
+}
+
+template <int NT>
+void gemm_tc(lcr_ctx* ctx, int M, int N, int K, const bf16* A, const bf16* B, const Epi& e, int* err) {
+  if (M == 0 || N == 0) return;
+  if (K % 64 != 0) LCR_THROW(LCR_ERR_INVALID_ARG, "tensor-core GEMM needs K a multiple of 64 (K=%d)", K);
+  const int smem = 2 * (128 * 128 + NT * 128) + 64 + 1024;
+  CUDA_TRY(cudaFuncSetAttribute(k_gemm_tc<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  const dim3 grid((N + NT - 1) / NT, (M + 127) / 128);
+  LCR_LAUNCH(ctx, k_gemm_tc<NT>, grid, 128, smem, M, N, K, A, B, e, err);
 }
 
 // out[c] = sum over rows of src[r][c], rows in order.
@@ -412,18 +531,18 @@ void head_forward(lcr_ctx* ctx, lcr_posenet* net, const Batch& b) {
   e1.relu = true;
   e1.outb = b.a1;
   e1.ldo = kH1;
-  gemm(ctx, B, kH1, kIn, b.featb, kIn, 1, net->pw.h1b, kIn, 1, e1);
+  gemm_tc<256>(ctx, B, kH1, kIn, b.featb, net->pw.h1b, e1, net->err);
   Epi e2;
   e2.bias = net->w + oC2;
   e2.relu = true;
   e2.outb = b.a2;
   e2.ldo = kH2;
-  gemm(ctx, B, kH2, kH1, b.a1, kH1, 1, net->pw.h2b, kH1, 1, e2);
+  gemm_tc<256>(ctx, B, kH2, kH1, b.a1, net->pw.h2b, e2, net->err);
   Epi e3;
   e3.bias = net->w + oC3;
   e3.out = b.y;
   e3.ldo = kOut;
-  gemm(ctx, B, kOut, kH2, b.a2, kH2, 1, net->pw.h3b, kH2, 1, e3);
+  gemm_tc<16>(ctx, B, kOut, kH2, b.a2, net->pw.h3b, e3, net->err);
 }
 
 void loss_backward(lcr_ctx* ctx, lcr_posenet* net, const Batch& b) {

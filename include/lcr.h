@@ -238,6 +238,35 @@ LCR_API lcr_status lcr_correspondences(lcr_ctx* ctx, const lcr_cloud* src, const
 LCR_API lcr_status lcr_knn(lcr_ctx* ctx, const lcr_cloud* ref, const lcr_cloud* query, int k, float max_dist_sq,
                            int32_t* idx, float* dist);
 
+/* ------------------------------------------------------ SfM-side filters */
+/* pcl::CropBox (pcl_tools/crop_cloud.cpp:81-97): inside = the finite points
+ * with min <= p <= max on every axis, outside = the other finite points, each
+ * in input order (either may be NULL). */
+LCR_API lcr_status lcr_crop_box(lcr_ctx* ctx, const lcr_cloud* in, const float min[3], const float max[3],
+                                lcr_cloud** inside, lcr_cloud** outside);
+/* pcl::EuclideanClusterExtraction (pcl_tools/cluster_extraction.cpp:90-130):
+ * connected components of the graph joining finite points whose squared FP32
+ * distance is below float(tolerance^2) (FLANN's radius search), kept when
+ * min_size <= size <= max_size, ordered by size (descending; equal sizes: the
+ * cluster with the smaller first index first).  labels (host, n, may be NULL)
+ * receives each point's cluster rank or -1; clustered the kept clusters'
+ * points, cluster after cluster, ascending index within each; rest every
+ * other point in input order (either may be NULL). */
+LCR_API lcr_status lcr_euclidean_clusters(lcr_ctx* ctx, const lcr_cloud* in, double tolerance, size_t min_size,
+                                          size_t max_size, int32_t* labels, size_t* nclusters, lcr_cloud** clustered,
+                                          lcr_cloud** rest);
+/* pcl::SACSegmentation with SACMODEL_PLANE, SAC_RANSAC and optimized
+ * coefficients (pcl_tools/planar_segmentation.cpp:80-110): `hypotheses`
+ * planes through three finite points drawn by a hash of seed, all scored at
+ * once (inliers: |n.p + d| < threshold); the best (most inliers, then the
+ * lowest hypothesis) is refitted by least squares on its inliers (FP64) and
+ * the inliers are selected again.  coefficients (a b c d) of the refitted
+ * plane; ninliers 0 when no plane was found.  plane: the inliers, rest: every
+ * other point, in input order (either may be NULL). */
+LCR_API lcr_status lcr_plane_segment(lcr_ctx* ctx, const lcr_cloud* in, double threshold, int hypotheses,
+                                     uint64_t seed, float coefficients[4], size_t* ninliers, lcr_cloud** plane,
+                                     lcr_cloud** rest);
+
 /* ------------------------------------------------------------ autotuning */
 /* Launch shapes of the search kernels.  Every result is independent of them;
  * only the speed changes. */

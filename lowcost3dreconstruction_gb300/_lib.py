@@ -133,6 +133,11 @@ _SIGS = {
     "lcr_centroid": (C.c_int, [_VP, _VP, _VP]),
     "lcr_centroid_align": (C.c_int, [_VP, _VP, _VP, C.c_double, C.c_double, C.c_double, C.c_double,
                                      C.POINTER(_VP), _VP]),
+    "lcr_crop_box": (C.c_int, [_VP, _VP, _VP, _VP, C.POINTER(_VP), C.POINTER(_VP)]),
+    "lcr_euclidean_clusters": (C.c_int, [_VP, _VP, C.c_double, C.c_size_t, C.c_size_t, _VP, C.POINTER(C.c_size_t),
+                                         C.POINTER(_VP), C.POINTER(_VP)]),
+    "lcr_plane_segment": (C.c_int, [_VP, _VP, C.c_double, C.c_int, C.c_uint64, _VP, C.POINTER(C.c_size_t),
+                                    C.POINTER(_VP), C.POINTER(_VP)]),
     "lcr_tune_get": (C.c_int, [_VP, C.POINTER(Tune)]),
     "lcr_tune_set": (C.c_int, [_VP, C.POINTER(Tune)]),
     "lcr_autotune": (C.c_int, [_VP, _VP, _VP, C.c_char_p, C.POINTER(TuneReport)]),

@@ -337,3 +337,32 @@ class Context:
         return {"sor_warps": r.chosen.sor_warps, "normals_warps": r.chosen.normals_warps,
                 "icp_blocks_per_sm": r.chosen.icp_blocks_per_sm, "from_cache": bool(r.from_cache),
                 "sor_ms": ms(r.sor_ms), "normals_ms": ms(r.normals_ms), "icp_ms": ms(r.icp_ms)}
+
+    # ------------------------------------------------------- SfM-side filters
+    def crop_box(self, cloud: Cloud, lo, hi) -> tuple[Cloud, Cloud]:
+        """lcr_crop_box: (inside, outside) of the box [lo, hi]."""
+        a = np.ascontiguousarray(lo, dtype=np.float32).reshape(3)
+        b = np.ascontiguousarray(hi, dtype=np.float32).reshape(3)
+        i, o = C.c_void_p(), C.c_void_p()
+        self._check(self.lib.lcr_crop_box(self.h, cloud.handle, L.ptr(a), L.ptr(b), C.byref(i), C.byref(o)))
+        return Cloud(self, i), Cloud(self, o)
+
+    def euclidean_clusters(self, cloud: Cloud, tolerance: float, min_size: int = 1, max_size: int | None = None):
+        """lcr_euclidean_clusters: (labels, nclusters, clustered, rest)."""
+        n = len(cloud)
+        labels = np.zeros(max(n, 1), dtype=np.int32)
+        k = C.c_size_t()
+        a, b = C.c_void_p(), C.c_void_p()
+        self._check(self.lib.lcr_euclidean_clusters(self.h, cloud.handle, tolerance, min_size,
+                                                    n if max_size is None else max_size, L.ptr(labels), C.byref(k),
+                                                    C.byref(a), C.byref(b)))
+        return labels[:n], k.value, Cloud(self, a), Cloud(self, b)
+
+    def plane_segment(self, cloud: Cloud, threshold: float, hypotheses: int = 1024, seed: int = 0):
+        """lcr_plane_segment: (coefficients, ninliers, plane, rest)."""
+        coef = np.zeros(4, dtype=np.float32)
+        m = C.c_size_t()
+        a, b = C.c_void_p(), C.c_void_p()
+        self._check(self.lib.lcr_plane_segment(self.h, cloud.handle, threshold, hypotheses, seed, L.ptr(coef),
+                                               C.byref(m), C.byref(a), C.byref(b)))
+        return coef, m.value, Cloud(self, a), Cloud(self, b)

@@ -590,6 +590,45 @@ lcr_status lcr_remove_nan(lcr_ctx* ctx, const lcr_cloud* in, lcr_cloud** out) {
   return LCR_OK;
 }
 
+lcr_status lcr_crop_box(lcr_ctx* ctx, const lcr_cloud* in, const float min[3], const float max[3],
+                        lcr_cloud** inside, lcr_cloud** outside) {
+  API_BEGIN(ctx)
+  REQUIRE(in && min && max, "null argument");
+  if (inside) *inside = nullptr;
+  if (outside) *outside = nullptr;
+  crop_box_run(ctx, in, min, max, inside, outside);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_euclidean_clusters(lcr_ctx* ctx, const lcr_cloud* in, double tolerance, size_t min_size,
+                                  size_t max_size, int32_t* labels, size_t* nclusters, lcr_cloud** clustered,
+                                  lcr_cloud** rest) {
+  API_BEGIN(ctx)
+  REQUIRE(in && nclusters, "null argument");
+  REQUIRE(tolerance > 0 && std::isfinite(tolerance), "tolerance must be positive");
+  REQUIRE(in->n < (1u << 31), "cloud too large");
+  if (clustered) *clustered = nullptr;
+  if (rest) *rest = nullptr;
+  euclidean_clusters_run(ctx, in, tolerance, min_size, max_size, labels, nclusters, clustered, rest);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_plane_segment(lcr_ctx* ctx, const lcr_cloud* in, double threshold, int hypotheses, uint64_t seed,
+                             float coefficients[4], size_t* ninliers, lcr_cloud** plane, lcr_cloud** rest) {
+  API_BEGIN(ctx)
+  REQUIRE(in && coefficients && ninliers, "null argument");
+  REQUIRE(threshold > 0 && std::isfinite(threshold), "threshold must be positive");
+  REQUIRE(hypotheses >= 1 && hypotheses <= (1 << 20), "hypotheses must be in [1, 2^20]");
+  REQUIRE(in->n < (1u << 31), "cloud too large");
+  if (plane) *plane = nullptr;
+  if (rest) *rest = nullptr;
+  plane_segment_run(ctx, in, threshold, hypotheses, seed, coefficients, ninliers, plane, rest);
+  API_END(ctx)
+  return LCR_OK;
+}
+
 lcr_status lcr_tune_get(lcr_ctx* ctx, lcr_tune* t) {
   API_BEGIN(ctx)
   REQUIRE(t, "null argument");

@@ -256,6 +256,13 @@ lcr_cloud* voxel_run(lcr_ctx* ctx, const lcr_cloud* in, float lx, float ly, floa
 void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_cloud** inliers,
              lcr_cloud** outliers, lcr_sor_stats* stats, float* host_dist);
 lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[3], int flags);
+// SfM-side filters (sfm.cu).
+void crop_box_run(lcr_ctx* ctx, const lcr_cloud* in, const float lo[3], const float hi[3], lcr_cloud** inside,
+                  lcr_cloud** outside);
+void euclidean_clusters_run(lcr_ctx* ctx, const lcr_cloud* in, double tolerance, size_t min_size, size_t max_size,
+                            int32_t* host_labels, size_t* nclusters, lcr_cloud** clustered, lcr_cloud** rest);
+void plane_segment_run(lcr_ctx* ctx, const lcr_cloud* in, double threshold, int hypotheses, uint64_t seed,
+                       float coefficients[4], size_t* ninliers, lcr_cloud** plane, lcr_cloud** rest);
 // Launch-shape tuning (tune.cu).
 void tune_apply(lcr_ctx* ctx, const lcr_tune& t);
 lcr_tune tune_current(const lcr_ctx* ctx);

@@ -27,6 +27,9 @@ TOOLS = {
     "centroid_align": ["--input", "--target", "--output", "--roll", "--pitch", "--yaw", "--elevation"],
     "transform": ["--input", "--output", "--transform"],
     "scale": ["--input", "--output", "--scale"],
+    "crop_cloud": ["--input", "--output", "--radius", "--negative"],
+    "cluster_extraction": ["--input", "--output", "--outliers_file", "--cluster_percentage", "--tolerance"],
+    "planar_segmentation": ["--input", "--output", "--threshold", "--negative"],
 }
 
 

@@ -483,6 +483,85 @@ def proposal_arm(args) -> dict:
             "e2e": None, "gpu_launches": P["launches"], "clocks": clk}
 
 
+# ------------------------------------------------------ SfM-side filters
+def sfm_arm(args) -> dict:
+    """The filters of sfm.sh:82-85 on a 1M-point synthetic dense model (a noisy
+    2 x 2 m floor of 900k points, three blobs, scattered points): Euclidean
+    clusters (tolerance 2 cm, clusters >= 10% of the points), the RANSAC plane
+    of the clustered points (1 cm, 1024 hypotheses) and a CropBox; CUDA events
+    per filter.  The CPU oracle runs the same filters on a 100k-point sample."""
+    import torch
+
+    from lowcost3dreconstruction_gb300.core import Context, points_from_xyz
+    from oracle import sfm as OS
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(11)
+    n_floor = 900_000
+    floor = np.c_[rng.uniform(-1, 1, (n_floor, 2)), rng.normal(0, 0.003, n_floor)]
+    blobs = [rng.normal(c, 0.04, (m, 3)) for c, m in (((0.3, 0.2, 0.4), 50_000), ((-0.4, -0.1, 0.5), 35_000),
+                                                          ((0.0, 0.6, 0.3), 14_000))]
+    xyz = np.concatenate([floor] + blobs + [rng.uniform(-1, 1, (1000, 3))]).astype(np.float32)
+    xyz = xyz[rng.permutation(len(xyz))]
+    n = len(xyz)
+    ctx = Context(0)
+    cloud = ctx.upload(points_from_xyz(xyz))
+    stream = torch.cuda.ExternalStream(ctx.stream, device=0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda:0")
+    c0 = ctx.centroid(cloud)
+
+    def step():
+        labels, k, kept, rest = ctx.euclidean_clusters(cloud, 0.02, int(n * 0.1), n)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e1.record(stream)
+        coef, m, plane, off = ctx.plane_segment(kept, 0.01, 1024, 0)
+        e2 = torch.cuda.Event(enable_timing=True)
+        e2.record(stream)
+        inside, outside = ctx.crop_box(cloud, c0[:3] - 0.5, c0[:3] + 0.5)
+        return k, len(kept), m, len(inside), e1, e2
+
+    for _ in range(args.warmup):
+        step()
+    ms = {"clusters": 0.0, "plane": 0.0, "crop": 0.0}
+    l0 = ctx.launches
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        k, nk, m, ni, e1, e2 = step()
+        e3 = torch.cuda.Event(enable_timing=True)
+        e3.record(stream)
+        e3.synchronize()
+        ms["clusters"] += e0.elapsed_time(e1)
+        ms["plane"] += e1.elapsed_time(e2)
+        ms["crop"] += e2.elapsed_time(e3)
+    total = sum(ms.values()) / args.steps
+    launches = (ctx.launches - l0) // args.steps
+    # CPU oracle on a bounded sample
+    sample = xyz[:100_000]
+    t0 = time.perf_counter()
+    OS.euclidean_clusters(sample, 0.02, 10_000, len(sample))
+    t1 = time.perf_counter()
+    OS.plane_segment(sample, 0.01, 64, 0)
+    t2 = time.perf_counter()
+    ctx.close()
+    cpu_pps = len(sample) / ((t1 - t0) + (t2 - t1) * 1024 / 64)
+    return {"metric": "points/s through the SfM filters (Euclidean clusters + RANSAC plane + CropBox)",
+            "value": round(n / (total / 1000.0), 1), "unit": "points/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP64 plane refit)", "data": "synthetic",
+            "config": {"workload": "1M-point dense model: clusters (2 cm, >= 10%), plane of the clustered points "
+                                   "(1 cm, 1024 hypotheses), CropBox (0.5 m around the centroid)",
+                       "points": n, "clusters": int(k), "clustered_points": int(nk), "plane_inliers": int(m),
+                       "cropped_points": int(ni),
+                       "ms_per_filter": {key: round(v / args.steps, 3) for key, v in ms.items()},
+                       "l2": "256 MB flush between steps"},
+            "roofline": None, "e2e": None, "gpu_launches": launches,
+            "cpu_baseline": {"value": round(cpu_pps, 1), "unit": "points/s", "cores": 1, "kind": "port",
+                             "sample": "the oracle (scipy cKDTree + connected components, numpy RANSAC scaled from "
+                                       "64 to 1024 hypotheses) on the first 100k points"}}
+
+
 # ------------------------------------------------------------ CPU (oracle)
 def cpu_pipeline(pr, threads: int):
     from lowcost3dreconstruction_gb300 import synthetic as S
@@ -547,10 +626,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="config1", choices=["config1", "turntable36", "proposal", "large512"],
+    ap.add_argument("--workload", default="config1",
+                    choices=["config1", "turntable36", "proposal", "large512", "sfm"],
                     help="config1: the headline pair pipeline; turntable36: batched ICP over a turntable cycle; "
                          "proposal: learned pose proposal + ICP vs plain ICP on held-out pairs; large512: the same "
-                         "on 512 pairs of 5k-500k points per view")
+                         "on 512 pairs of 5k-500k points per view; sfm: the SfM-side filters on a 1M-point model")
     ap.add_argument("--pairs", type=int, default=2000, help="pairs of the proposal workload")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
@@ -563,6 +643,9 @@ def main():
     elif args.workload == "turntable36":
         build.build_lib()
         out = turntable_arm(args) if rank == 0 else None
+    elif args.workload == "sfm":
+        build.build_lib()
+        out = sfm_arm(args) if rank == 0 else None
     elif args.workload in ("proposal", "large512"):
         build.build_lib()
         out = proposal_arm(args) if rank == 0 else None

@@ -8,14 +8,22 @@
 // parsed and skipped.  Writes binary_little_endian with PCL's field order for
 // PointXYZRGBNormal (x y z, rgb as red/green/blue, normal_x/y/z, curvature), as
 // pcl::io::savePLYFileBinary does for the reference tools.
-#include <cerrno>
+//
+// The file is read in one piece; vertex records decode through the property
+// list straight from the buffer, text scalars with std::from_chars (correctly
+// rounded, as strtof/strtod), and large clouds split over host threads: text
+// files one instance per line in parallel (any other layout falls back to the
+// token stream).  The text writer prints the shortest form that reads back to
+// the same float (std::to_chars).
+#include <algorithm>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <fstream>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../../include/lcr.h"
@@ -84,10 +92,10 @@ inline void swap_bytes(unsigned char* p, size_t n) {
 }
 
 // Value of a binary scalar, as double, plus its raw 32-bit pattern (for packed rgb).
-bool read_bin(std::istream& in, T t, bool big, double& v, uint32_t& raw) {
+inline void decode_bin(const unsigned char* src, T t, bool big, double& v, uint32_t& raw) {
   unsigned char b[8];
   const size_t n = type_size(t);
-  if (!in.read(reinterpret_cast<char*>(b), static_cast<std::streamsize>(n))) return false;
+  std::memcpy(b, src, n);
   if (big) swap_bytes(b, n);
   raw = 0;
   switch (t) {
@@ -99,30 +107,46 @@ bool read_bin(std::istream& in, T t, bool big, double& v, uint32_t& raw) {
     case T::U32: { uint32_t x; std::memcpy(&x, b, 4); v = x; raw = x; break; }
     case T::F32: { float x; std::memcpy(&x, b, 4); v = x; std::memcpy(&raw, b, 4); break; }
     case T::F64: { double x; std::memcpy(&x, b, 8); v = x; float f = static_cast<float>(x); std::memcpy(&raw, &f, 4); break; }
-    default: return false;
+    default: v = 0; break;
   }
+}
+
+inline bool is_space(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\v' || c == '\f'; }
+
+// Next whitespace-separated token of [p, end).
+inline bool next_token(const char*& p, const char* end, const char*& ts, const char*& te) {
+  while (p < end && is_space(*p)) ++p;
+  if (p >= end) return false;
+  ts = p;
+  while (p < end && !is_space(*p)) ++p;
+  te = p;
   return true;
 }
 
-bool read_ascii(std::istream& in, T t, double& v, uint32_t& raw) {
-  std::string tok;
-  if (!(in >> tok)) return false;
-  errno = 0;
-  char* end = nullptr;
+// One text scalar, correctly rounded as strtof/strtod would (from_chars).
+inline bool parse_token(const char* s, const char* e, T t, double& v, uint32_t& raw) {
+  if (s < e && *s == '+') ++s;
   if (t == T::F32) {
-    const float f = std::strtof(tok.c_str(), &end);  // one rounding, as PCL's text parse to float
+    float f = 0.f;
+    const auto r = std::from_chars(s, e, f);
+    if (r.ec != std::errc() || r.ptr != e) return false;
     v = f;
     std::memcpy(&raw, &f, 4);
   } else if (t == T::F64) {
-    v = std::strtod(tok.c_str(), &end);
-    const float f = static_cast<float>(v);
+    double d = 0.0;
+    const auto r = std::from_chars(s, e, d);
+    if (r.ec != std::errc() || r.ptr != e) return false;
+    v = d;
+    const float f = static_cast<float>(d);
     std::memcpy(&raw, &f, 4);
   } else {
-    const long long x = std::strtoll(tok.c_str(), &end, 10);
+    long long x = 0;
+    const auto r = std::from_chars(s, e, x);
+    if (r.ec != std::errc() || r.ptr != e) return false;
     v = static_cast<double>(x);
     raw = static_cast<uint32_t>(x);
   }
-  return end && *end == '\0';
+  return true;
 }
 
 void assign(lcr_point& p, Field f, T t, double v, uint32_t raw) {
@@ -156,6 +180,37 @@ lcr_status fail(lcr_status s, const std::string& msg) {
   return s;
 }
 
+// Work split over host threads for large element counts (each part a
+// contiguous range; f(begin, end, part) returns false on malformed data).
+template <class F>
+bool parallel_ranges(size_t n, F&& f) {
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const size_t parts = n >= 65536 ? hw : 1;
+  if (parts == 1) return f(size_t{0}, n, size_t{0});
+  std::vector<std::thread> th;
+  std::vector<char> ok(parts, 1);
+  for (size_t k = 0; k < parts; ++k)
+    th.emplace_back([&, k] { ok[k] = f(n * k / parts, n * (k + 1) / parts, k) ? 1 : 0; });
+  for (auto& t : th) t.join();
+  for (char c : ok)
+    if (!c) return false;
+  return true;
+}
+
+bool read_file(const char* path, std::vector<char>& buf) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return false;
+  bool ok = std::fseek(f, 0, SEEK_END) == 0;
+  const long sz = ok ? std::ftell(f) : -1;
+  ok = ok && sz >= 0 && std::fseek(f, 0, SEEK_SET) == 0;
+  if (ok) {
+    buf.resize(static_cast<size_t>(sz));
+    ok = sz == 0 || std::fread(buf.data(), 1, buf.size(), f) == buf.size();
+  }
+  std::fclose(f);
+  return ok;
+}
+
 }  // namespace
 
 extern "C" {
@@ -168,14 +223,26 @@ LCR_API lcr_status lcr_ply_read(const char* path, lcr_point** out, size_t* n_out
   if (!path || !out || !n_out) return fail(LCR_ERR_INVALID_ARG, "null argument");
   *out = nullptr;
   *n_out = 0;
-  std::ifstream in(path, std::ios::binary);
-  if (!in) return fail(LCR_ERR_IO, std::string("cannot open ") + path);
+  std::vector<char> file;
+  if (!read_file(path, file)) return fail(LCR_ERR_IO, std::string("cannot open ") + path);
+  const char* p = file.data();
+  const char* const end = p + file.size();
+  // ---- header, line by line
+  auto next_line = [&](std::string& line) {
+    if (p >= end) return false;
+    const char* nl = static_cast<const char*>(std::memchr(p, '\n', static_cast<size_t>(end - p)));
+    const char* le = nl ? nl : end;
+    line.assign(p, le);
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    p = nl ? nl + 1 : end;
+    return true;
+  };
   std::string line;
-  if (!std::getline(in, line) || line.rfind("ply", 0) != 0) return fail(LCR_ERR_IO, "not a PLY file");
+  if (!next_line(line) || line.rfind("ply", 0) != 0) return fail(LCR_ERR_IO, "not a PLY file");
   int format = -1;  // 0 ascii, 1 binary le, 2 binary be
   std::vector<Element> els;
-  while (std::getline(in, line)) {
-    if (!line.empty() && line.back() == '\r') line.pop_back();
+  bool ended = false;
+  while (next_line(line)) {
     std::istringstream ls(line);
     std::string kw;
     ls >> kw;
@@ -190,28 +257,30 @@ LCR_API lcr_status lcr_ply_read(const char* path, lcr_point** out, size_t* n_out
       els.push_back(e);
     } else if (kw == "property") {
       if (els.empty()) return fail(LCR_ERR_IO, "property before element");
-      Prop p;
+      Prop pr;
       std::string t;
       ls >> t;
       if (t == "list") {
         std::string ct, it;
-        ls >> ct >> it >> p.name;
-        p.list = true;
-        p.count_type = parse_type(ct);
-        p.type = parse_type(it);
-        if (p.count_type == T::BAD || p.type == T::BAD) return fail(LCR_ERR_IO, "bad list property");
+        ls >> ct >> it >> pr.name;
+        pr.list = true;
+        pr.count_type = parse_type(ct);
+        pr.type = parse_type(it);
+        if (pr.count_type == T::BAD || pr.type == T::BAD) return fail(LCR_ERR_IO, "bad list property");
       } else {
-        ls >> p.name;
-        p.type = parse_type(t);
-        if (p.type == T::BAD) return fail(LCR_ERR_IO, "bad property type " + t);
+        ls >> pr.name;
+        pr.type = parse_type(t);
+        if (pr.type == T::BAD) return fail(LCR_ERR_IO, "bad property type " + t);
       }
-      if (els.back().name == "vertex" && !p.list) p.field = vertex_field(p.name);
-      els.back().props.push_back(p);
+      if (els.back().name == "vertex" && !pr.list) pr.field = vertex_field(pr.name);
+      els.back().props.push_back(pr);
     } else if (kw == "end_header") {
+      ended = true;
       break;
     }
   }
   if (format < 0) return fail(LCR_ERR_IO, "missing format line");
+  if (!ended) return fail(LCR_ERR_IO, "missing end_header");
   size_t nv = 0;
   for (const Element& e : els)
     if (e.name == "vertex") nv = e.count;
@@ -219,30 +288,125 @@ LCR_API lcr_status lcr_ply_read(const char* path, lcr_point** out, size_t* n_out
   lcr_point* pts = static_cast<lcr_point*>(std::calloc(nv ? nv : 1, sizeof(lcr_point)));
   if (!pts) return fail(LCR_ERR_OOM, "allocation failed");
   const bool big = format == 2;
+  auto bad = [&](const std::string& msg) {
+    std::free(pts);
+    return fail(LCR_ERR_IO, msg);
+  };
   for (const Element& e : els) {
     const bool isv = e.name == "vertex";
+    bool has_list = false;
+    for (const Prop& pr : e.props) has_list |= pr.list;
+    if (format != 0) {
+      // ------------------------------------------------------------ binary
+      if (!has_list) {
+        size_t rec = 0;
+        for (const Prop& pr : e.props) rec += type_size(pr.type);
+        if (static_cast<size_t>(end - p) / (rec ? rec : 1) < e.count)
+          return bad("truncated or malformed " + e.name + " data");
+        if (isv) {
+          const unsigned char* base = reinterpret_cast<const unsigned char*>(p);
+          parallel_ranges(e.count, [&](size_t b, size_t en, size_t) {
+            for (size_t i = b; i < en; ++i) {
+              const unsigned char* r = base + i * rec;
+              size_t off = 0;
+              for (const Prop& pr : e.props) {
+                double v;
+                uint32_t raw;
+                decode_bin(r + off, pr.type, big, v, raw);
+                assign(pts[i], pr.field, pr.type, v, raw);
+                off += type_size(pr.type);
+              }
+            }
+            return true;
+          });
+        }
+        p += rec * e.count;
+      } else {
+        for (size_t i = 0; i < e.count; ++i) {
+          lcr_point dummy;
+          lcr_point& pt = isv ? pts[i] : dummy;
+          for (const Prop& pr : e.props) {
+            double v;
+            uint32_t raw;
+            if (pr.list) {
+              const size_t cs = type_size(pr.count_type);
+              if (static_cast<size_t>(end - p) < cs) return bad("truncated list");
+              decode_bin(reinterpret_cast<const unsigned char*>(p), pr.count_type, big, v, raw);
+              p += cs;
+              if (v < 0) return bad("truncated list");
+              const size_t bytes = static_cast<size_t>(v) * type_size(pr.type);
+              if (static_cast<size_t>(end - p) < bytes) return bad("truncated list data");
+              p += bytes;
+              continue;
+            }
+            const size_t sz = type_size(pr.type);
+            if (static_cast<size_t>(end - p) < sz) return bad("truncated or malformed " + e.name + " data");
+            decode_bin(reinterpret_cast<const unsigned char*>(p), pr.type, big, v, raw);
+            p += sz;
+            if (isv) assign(pt, pr.field, pr.type, v, raw);
+          }
+        }
+      }
+      continue;
+    }
+    // -------------------------------------------------------------- ascii
+    // Fast form: one instance per line (what every writer produces), lines
+    // parsed in parallel; any other layout takes the token stream below.
+    bool done = false;
+    if (isv && !has_list && e.count > 0) {
+      std::vector<const char*> starts(e.count + 1);
+      const char* q = p;
+      size_t i = 0;
+      for (; i < e.count && q < end; ++i) {
+        starts[i] = q;
+        const char* nl = static_cast<const char*>(std::memchr(q, '\n', static_cast<size_t>(end - q)));
+        q = nl ? nl + 1 : end;
+      }
+      if (i == e.count) {
+        starts[e.count] = q;
+        const bool ok = parallel_ranges(e.count, [&](size_t b, size_t en, size_t) {
+          for (size_t k = b; k < en; ++k) {
+            const char* s = starts[k];
+            const char* le = starts[k + 1];
+            for (const Prop& pr : e.props) {
+              const char *ts, *te;
+              double v;
+              uint32_t raw;
+              if (!next_token(s, le, ts, te) || !parse_token(ts, te, pr.type, v, raw)) return false;
+              assign(pts[k], pr.field, pr.type, v, raw);
+            }
+            const char *ts, *te;
+            if (next_token(s, le, ts, te)) return false;  // extra tokens: not one instance per line
+          }
+          return true;
+        });
+        if (ok) {
+          p = q;
+          done = true;
+        } else {
+          std::memset(pts, 0, sizeof(lcr_point) * nv);
+        }
+      }
+    }
+    if (done) continue;
     for (size_t i = 0; i < e.count; ++i) {
       lcr_point dummy;
-      lcr_point& p = isv ? pts[i] : dummy;
+      lcr_point& pt = isv ? pts[i] : dummy;
       for (const Prop& pr : e.props) {
+        const char *ts, *te;
         double v;
         uint32_t raw;
         if (pr.list) {
-          bool ok = format == 0 ? read_ascii(in, pr.count_type, v, raw) : read_bin(in, pr.count_type, big, v, raw);
-          if (!ok || v < 0) { std::free(pts); return fail(LCR_ERR_IO, "truncated list"); }
+          if (!next_token(p, end, ts, te) || !parse_token(ts, te, pr.count_type, v, raw) || v < 0)
+            return bad("truncated list");
           const size_t cnt = static_cast<size_t>(v);
-          for (size_t k = 0; k < cnt; ++k) {
-            ok = format == 0 ? read_ascii(in, pr.type, v, raw) : read_bin(in, pr.type, big, v, raw);
-            if (!ok) { std::free(pts); return fail(LCR_ERR_IO, "truncated list data"); }
-          }
+          for (size_t k = 0; k < cnt; ++k)
+            if (!next_token(p, end, ts, te) || !parse_token(ts, te, pr.type, v, raw)) return bad("truncated list data");
           continue;
         }
-        const bool ok = format == 0 ? read_ascii(in, pr.type, v, raw) : read_bin(in, pr.type, big, v, raw);
-        if (!ok) {
-          std::free(pts);
-          return fail(LCR_ERR_IO, "truncated or malformed " + e.name + " data");
-        }
-        if (isv) assign(p, pr.field, pr.type, v, raw);
+        if (!next_token(p, end, ts, te) || !parse_token(ts, te, pr.type, v, raw))
+          return bad("truncated or malformed " + e.name + " data");
+        if (isv) assign(pt, pr.field, pr.type, v, raw);
       }
     }
   }
@@ -263,28 +427,58 @@ LCR_API lcr_status lcr_ply_write(const char* path, const lcr_point* pts, size_t 
                "property float curvature\nend_header\n");
   bool ok = true;
   if (binary) {
-    std::vector<unsigned char> buf(n * 31);
+    std::vector<unsigned char> buf(n * 31);  // memory-bound: one thread
     for (size_t i = 0; i < n; ++i) {
-      unsigned char* b = &buf[i * 31];
-      const lcr_point& p = pts[i];
-      std::memcpy(b, &p.x, 4);
-      std::memcpy(b + 4, &p.y, 4);
-      std::memcpy(b + 8, &p.z, 4);
-      b[12] = p.r;
-      b[13] = p.g;
-      b[14] = p.b;
-      std::memcpy(b + 15, &p.normal_x, 4);
-      std::memcpy(b + 19, &p.normal_y, 4);
-      std::memcpy(b + 23, &p.normal_z, 4);
-      std::memcpy(b + 27, &p.curvature, 4);
+      unsigned char* o = &buf[i * 31];
+      const lcr_point& q = pts[i];
+      std::memcpy(o, &q.x, 4);
+      std::memcpy(o + 4, &q.y, 4);
+      std::memcpy(o + 8, &q.z, 4);
+      o[12] = q.r;
+      o[13] = q.g;
+      o[14] = q.b;
+      std::memcpy(o + 15, &q.normal_x, 4);
+      std::memcpy(o + 19, &q.normal_y, 4);
+      std::memcpy(o + 23, &q.normal_z, 4);
+      std::memcpy(o + 27, &q.curvature, 4);
     }
     ok = std::fwrite(buf.data(), 1, buf.size(), f) == buf.size();
   } else {
-    for (size_t i = 0; i < n && ok; ++i) {
-      const lcr_point& p = pts[i];
-      ok = std::fprintf(f, "%.9g %.9g %.9g %d %d %d %.9g %.9g %.9g %.9g\n", p.x, p.y, p.z, p.r, p.g, p.b, p.normal_x,
-                        p.normal_y, p.normal_z, p.curvature) > 0;
-    }
+    // shortest text that reads back to the same float (to_chars), formatted in parallel
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const size_t parts = n >= 65536 ? hw : 1;
+    std::vector<std::string> chunk(parts);
+    parallel_ranges(n, [&](size_t b, size_t en, size_t k) {
+      std::string& s = chunk[parts == 1 ? 0 : k];
+      s.reserve((en - b) * 96);
+      char tmp[64];
+      auto put_f = [&](float v, char sep) {
+        const auto r = std::to_chars(tmp, tmp + sizeof tmp, v);
+        s.append(tmp, r.ptr);
+        s.push_back(sep);
+      };
+      auto put_u = [&](unsigned v, char sep) {
+        const auto r = std::to_chars(tmp, tmp + sizeof tmp, v);
+        s.append(tmp, r.ptr);
+        s.push_back(sep);
+      };
+      for (size_t i = b; i < en; ++i) {
+        const lcr_point& q = pts[i];
+        put_f(q.x, ' ');
+        put_f(q.y, ' ');
+        put_f(q.z, ' ');
+        put_u(q.r, ' ');
+        put_u(q.g, ' ');
+        put_u(q.b, ' ');
+        put_f(q.normal_x, ' ');
+        put_f(q.normal_y, ' ');
+        put_f(q.normal_z, ' ');
+        put_f(q.curvature, '\n');
+      }
+      return true;
+    });
+    for (const std::string& s : chunk)
+      if (ok && !s.empty()) ok = std::fwrite(s.data(), 1, s.size(), f) == s.size();
   }
   ok = (std::fclose(f) == 0) && ok;
   return ok ? LCR_OK : fail(LCR_ERR_IO, std::string("write failed: ") + path);

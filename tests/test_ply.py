@@ -81,3 +81,23 @@ def test_malformed_files_fail_cleanly(tmp_path):
         L.read_ply(tmp_path / "short.ply")
     with pytest.raises(L.LcrError):
         L.read_ply(tmp_path / "missing.ply")
+
+
+def test_large_text_round_trip_uses_the_parallel_form(tmp_path):
+    pts = random_cloud(150_000, 5)
+    pts["normal_y"][::1000] = np.nan
+    L.write_ply(tmp_path / "big.ply", pts, binary=False)
+    back = L.read_ply(tmp_path / "big.ply")
+    for f in FIELDS:
+        np.testing.assert_array_equal(back[f], pts[f], err_msg=f)
+
+
+def test_text_instances_split_over_lines(tmp_path):
+    """Any whitespace layout is valid PLY: the token-stream form reads it."""
+    text = ("ply\nformat ascii 1.0\nelement vertex 2\nproperty float x\nproperty float y\nproperty float z\n"
+            "end_header\n1.5\n2.5 3.5 -4\n+5e-1\n6\n")
+    (tmp_path / "s.ply").write_text(text)
+    p = L.read_ply(tmp_path / "s.ply")
+    np.testing.assert_array_equal(p["x"], np.float32([1.5, -4.0]))
+    np.testing.assert_array_equal(p["y"], np.float32([2.5, 0.5]))
+    np.testing.assert_array_equal(p["z"], np.float32([3.5, 6.0]))

@@ -267,6 +267,26 @@ LCR_API lcr_status lcr_plane_segment(lcr_ctx* ctx, const lcr_cloud* in, double t
                                      uint64_t seed, float coefficients[4], size_t* ninliers, lcr_cloud** plane,
                                      lcr_cloud** rest);
 
+/* ---------------------------------------------------- super-resolution */
+/* The front end of capture/super_resolution/super_resolution.cpp:236-314 for
+ * one view: frames (host, [frames][height][width] uint16 mm) are registered
+ * to frame 0 by ECC affine alignment (enhanced correlation coefficient,
+ * Gauss-Newton, after a 5x5 Gaussian smoothing, until the coefficient changes
+ * by less than ecc_epsilon or after ecc_iterations), warped onto it
+ * (bilinear, zero outside), upsampled by `factor` (nearest), fused by the
+ * zero-eliminated mean and resampled back by Lanczos-4, rounded and
+ * saturated to uint16 (depth_out [height][width]).  Optional outputs: warps
+ * [frames][6] (2x3 row-major inverse maps, frame 0 the identity), minmax the
+ * observed nonzero range, iterations [frames]. */
+typedef struct lcr_sr_params {
+  int width, height, frames;
+  int factor;          /* resample factor (the tool's default 4) */
+  int ecc_iterations;  /* 200 in the reference */
+  double ecc_epsilon;  /* 1e-12 in the reference */
+} lcr_sr_params;
+LCR_API lcr_status lcr_super_resolve(lcr_ctx* ctx, const uint16_t* frames, const lcr_sr_params* p,
+                                     uint16_t* depth_out, float* warps, float minmax[2], int32_t* iterations);
+
 /* ------------------------------------------------------------ autotuning */
 /* Launch shapes of the search kernels.  Every result is independent of them;
  * only the speed changes. */

@@ -94,6 +94,11 @@ class TuneReport(C.Structure):
                 ("normals_ms", C.c_double * 8), ("icp_ms", C.c_double * 8)]
 
 
+class SrParams(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("frames", C.c_int), ("factor", C.c_int),
+                ("ecc_iterations", C.c_int), ("ecc_epsilon", C.c_double)]
+
+
 _VP = C.c_void_p
 _SIGS = {
     "lcr_ctx_create": (C.c_int, [C.POINTER(_VP), C.c_int]),
@@ -138,6 +143,7 @@ _SIGS = {
                                          C.POINTER(_VP), C.POINTER(_VP)]),
     "lcr_plane_segment": (C.c_int, [_VP, _VP, C.c_double, C.c_int, C.c_uint64, _VP, C.POINTER(C.c_size_t),
                                     C.POINTER(_VP), C.POINTER(_VP)]),
+    "lcr_super_resolve": (C.c_int, [_VP, _VP, C.POINTER(SrParams), _VP, _VP, _VP, _VP]),
     "lcr_tune_get": (C.c_int, [_VP, C.POINTER(Tune)]),
     "lcr_tune_set": (C.c_int, [_VP, C.POINTER(Tune)]),
     "lcr_autotune": (C.c_int, [_VP, _VP, _VP, C.c_char_p, C.POINTER(TuneReport)]),

@@ -30,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 CU_SOURCES = ["api.cu", "context.cu", "sort.cu", "index.cu", "knn.cu", "icp.cu", "depth.cu", "voxel.cu",
-              "filters.cu", "posenet.cu", "posenet_train.cu", "synth.cu", "tune.cu", "sfm.cu"]
+              "filters.cu", "posenet.cu", "posenet_train.cu", "synth.cu", "tune.cu", "sfm.cu", "sr.cu"]
 HOST_SOURCES = ["ply.cpp"]
 TOOLS = ["fine_registration", "cloud_downsampling", "outlier_removal", "normal_estimation", "accumulate_clouds",
          "transform", "scale", "centroid_align", "depth_to_cloud", "rotate_align", "pose_proposal",

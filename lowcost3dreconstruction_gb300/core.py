@@ -366,3 +366,18 @@ class Context:
         self._check(self.lib.lcr_plane_segment(self.h, cloud.handle, threshold, hypotheses, seed, L.ptr(coef),
                                                C.byref(m), C.byref(a), C.byref(b)))
         return coef, m.value, Cloud(self, a), Cloud(self, b)
+
+    # ------------------------------------------------------ super-resolution
+    def super_resolve(self, frames: np.ndarray, factor: int = 4, ecc_iterations: int = 200,
+                      ecc_epsilon: float = 1e-12):
+        """lcr_super_resolve: (fused uint16 depth, warps [F][2][3], (min, max), iterations [F])."""
+        frames = np.ascontiguousarray(frames, dtype=np.uint16)
+        F, h, w = frames.shape
+        out = np.zeros((h, w), dtype=np.uint16)
+        warps = np.zeros((F, 6), dtype=np.float32)
+        mm = np.zeros(2, dtype=np.float32)
+        it = np.zeros(F, dtype=np.int32)
+        p = L.SrParams(w, h, F, factor, ecc_iterations, ecc_epsilon)
+        self._check(self.lib.lcr_super_resolve(self.h, L.ptr(frames), C.byref(p), L.ptr(out), L.ptr(warps),
+                                               L.ptr(mm), L.ptr(it)))
+        return out, warps.reshape(F, 2, 3), (float(mm[0]), float(mm[1])), it

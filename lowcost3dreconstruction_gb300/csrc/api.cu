@@ -629,6 +629,21 @@ lcr_status lcr_plane_segment(lcr_ctx* ctx, const lcr_cloud* in, double threshold
   return LCR_OK;
 }
 
+lcr_status lcr_super_resolve(lcr_ctx* ctx, const uint16_t* frames, const lcr_sr_params* p, uint16_t* depth_out,
+                             float* warps, float minmax[2], int32_t* iterations) {
+  API_BEGIN(ctx)
+  REQUIRE(p && frames && depth_out, "null argument");
+  REQUIRE(p->width >= 1 && p->height >= 1 && static_cast<long long>(p->width) * p->height <= (1LL << 26),
+          "bad image size %dx%d", p->width, p->height);
+  REQUIRE(p->frames >= 1 && p->frames <= 1024, "frames must be in [1, 1024]");
+  REQUIRE(p->factor >= 1 && p->factor <= 16, "factor must be in [1, 16]");
+  REQUIRE(p->ecc_iterations >= 0 && p->ecc_epsilon >= 0, "bad ECC limits");
+  super_resolve_run(ctx, frames, p->width, p->height, p->frames, p->factor, p->ecc_iterations, p->ecc_epsilon,
+                    depth_out, warps, minmax, iterations);
+  API_END(ctx)
+  return LCR_OK;
+}
+
 lcr_status lcr_tune_get(lcr_ctx* ctx, lcr_tune* t) {
   API_BEGIN(ctx)
   REQUIRE(t, "null argument");

@@ -263,6 +263,9 @@ void euclidean_clusters_run(lcr_ctx* ctx, const lcr_cloud* in, double tolerance,
                             int32_t* host_labels, size_t* nclusters, lcr_cloud** clustered, lcr_cloud** rest);
 void plane_segment_run(lcr_ctx* ctx, const lcr_cloud* in, double threshold, int hypotheses, uint64_t seed,
                        float coefficients[4], size_t* ninliers, lcr_cloud** plane, lcr_cloud** rest);
+// Super-resolution front end (sr.cu).
+void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F, int factor, int max_iter,
+                       double eps, uint16_t* out, float* warps_out, float minmax_out[2], int* iters_out);
 // Launch-shape tuning (tune.cu).
 void tune_apply(lcr_ctx* ctx, const lcr_tune& t);
 lcr_tune tune_current(const lcr_ctx* ctx);

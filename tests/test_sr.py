@@ -61,19 +61,30 @@ def test_oracle_ecc_recovers_a_known_motion():
 # ------------------------------------------------------------------ GPU
 @pytest.mark.gpu
 def test_super_resolve_matches_oracle(ctx):
-    frames, truth = burst(F=4, seed=1)
+    """A burst with 1% missing pixels (zeros): like the reference, which passes
+    no mask to the registration, zeros take part as intensities -- the GPU
+    and the oracle must agree, whatever the holes do to the motion."""
+    frames, _ = burst(F=4, seed=1)
     out, warps, mm, its = ctx.super_resolve(frames, factor=4, ecc_iterations=60, ecc_epsilon=1e-10)
     want, wwarps, wits = O.super_resolve(frames, 4, 60, 1e-10)
     nz = frames[frames > 0]
     assert mm == (float(nz.min()), float(nz.max()))
     np.testing.assert_array_equal(warps[0], np.float32([[1, 0, 0], [0, 1, 0]]))
     for f in range(1, 4):
-        np.testing.assert_allclose(warps[f][:, 2], truth[f][:, 2], atol=0.08)
-        np.testing.assert_allclose(warps[f][:, :2], truth[f][:, :2], atol=3e-3)
         np.testing.assert_allclose(warps[f], wwarps[f], atol=2e-3)
     diff = np.abs(out.astype(np.int64) - want.astype(np.int64))
     assert np.mean(diff <= 1) > 0.995
-    assert np.array_equal(out == 0, want == 0) or np.mean((out == 0) != (want == 0)) < 1e-3
+    assert np.mean((out == 0) != (want == 0)) < 1e-3
+
+
+@pytest.mark.gpu
+def test_ecc_recovers_known_motions(ctx):
+    frames, truth = burst(F=6, seed=3, holes=False)
+    _, warps, _, its = ctx.super_resolve(frames, factor=4, ecc_iterations=100, ecc_epsilon=1e-10)
+    assert its[0] == 0 and np.all(its[1:] >= 1)
+    for f in range(1, 6):
+        np.testing.assert_allclose(warps[f][:, 2], truth[f][:, 2], atol=0.05)
+        np.testing.assert_allclose(warps[f][:, :2], truth[f][:, :2], atol=2e-3)
 
 
 @pytest.mark.gpu

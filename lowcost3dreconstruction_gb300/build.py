@@ -84,6 +84,16 @@ def build_lib(jobs: int | None = None, verbose: bool = False) -> Path:
     return LIB
 
 
+# Tools with extra sources and libraries, built only where the library is present.
+EXTRA_TOOLS = {"super_resolution": (["png16.cpp"], ["-lz"], "zlib.h")}
+
+
+def _have_header(name: str) -> bool:
+    res = subprocess.run(["g++", "-x", "c++", "-fsyntax-only", "-"], input=f"#include <{name}>\n", text=True,
+                         capture_output=True)
+    return res.returncode == 0
+
+
 def build_tools() -> None:
     BIN.mkdir(exist_ok=True)
     common = [CSRC / "host" / "cli_common.cpp"]
@@ -91,14 +101,16 @@ def build_tools() -> None:
         return
     deps = common + list((CSRC / "host").glob("*.h")) + [ROOT / "include" / "lcr.h", ROOT / "include" / "lcr_pcl.hpp", LIB]
     cmds = []
-    for t in TOOLS:
+    for t in TOOLS + [t for t, (_, _, hdr) in EXTRA_TOOLS.items() if _have_header(hdr)]:
         src = CSRC / "host" / f"{t}.cpp"
         out = BIN / t
         if not src.exists():
             continue
-        if _stale(out, [src] + deps):
+        extra_src, extra_libs, _ = EXTRA_TOOLS.get(t, ([], [], ""))
+        extra = [CSRC / "host" / e for e in extra_src]
+        if _stale(out, [src] + extra + deps):
             cmds.append(["g++", "-O2", "-std=c++17", "-I", str(ROOT / "include"), "-I", str(CSRC / "host"), str(src),
-                         *map(str, common), "-o", str(out), "-L", str(PKG), "-llcr",
+                         *map(str, extra), *map(str, common), "-o", str(out), "-L", str(PKG), "-llcr", *extra_libs,
                          "-Wl,-rpath,$ORIGIN/.."])
     with cf.ThreadPoolExecutor(max_workers=min(len(cmds) or 1, os.cpu_count() or 4)) as ex:
         list(ex.map(_run, cmds))

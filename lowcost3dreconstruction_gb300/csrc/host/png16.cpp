@@ -1,0 +1,168 @@
+// PNG codec for grayscale depth images (see png16.h).
+#include "png16.h"
+
+#include <zlib.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+namespace png16 {
+namespace {
+
+const unsigned char kSig[8] = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};
+
+uint32_t be32(const unsigned char* p) {
+  return (static_cast<uint32_t>(p[0]) << 24) | (static_cast<uint32_t>(p[1]) << 16) | (static_cast<uint32_t>(p[2]) << 8) | p[3];
+}
+
+void put32(std::vector<unsigned char>& o, uint32_t v) {
+  o.push_back(static_cast<unsigned char>(v >> 24));
+  o.push_back(static_cast<unsigned char>(v >> 16));
+  o.push_back(static_cast<unsigned char>(v >> 8));
+  o.push_back(static_cast<unsigned char>(v));
+}
+
+void chunk(std::vector<unsigned char>& o, const char* type, const unsigned char* data, size_t n) {
+  put32(o, static_cast<uint32_t>(n));
+  const size_t at = o.size();
+  o.insert(o.end(), type, type + 4);
+  o.insert(o.end(), data, data + n);
+  put32(o, static_cast<uint32_t>(crc32(0L, o.data() + at, static_cast<uInt>(n + 4))));
+}
+
+int paeth(int a, int b, int c) {
+  const int p = a + b - c, pa = std::abs(p - a), pb = std::abs(p - b), pc = std::abs(p - c);
+  if (pa <= pb && pa <= pc) return a;
+  return pb <= pc ? b : c;
+}
+
+}  // namespace
+
+bool read(const std::string& path, std::vector<uint16_t>& pixels, int& width, int& height, std::string& err) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) {
+    err = "cannot open " + path;
+    return false;
+  }
+  std::vector<unsigned char> buf;
+  unsigned char tmp[65536];
+  size_t got;
+  while ((got = std::fread(tmp, 1, sizeof tmp, f)) > 0) buf.insert(buf.end(), tmp, tmp + got);
+  std::fclose(f);
+  if (buf.size() < 8 || std::memcmp(buf.data(), kSig, 8) != 0) {
+    err = path + " is not a PNG file";
+    return false;
+  }
+  size_t p = 8;
+  int depth = 0, ctype = -1, interlace = 0;
+  std::vector<unsigned char> idat;
+  bool have_hdr = false, ended = false;
+  while (p + 12 <= buf.size() && !ended) {
+    const uint32_t n = be32(&buf[p]);
+    if (p + 12 + static_cast<size_t>(n) > buf.size()) break;
+    const unsigned char* type = &buf[p + 4];
+    const unsigned char* data = &buf[p + 8];
+    if (static_cast<uint32_t>(crc32(0L, type, n + 4)) != be32(data + n)) {
+      err = path + ": chunk CRC mismatch";
+      return false;
+    }
+    if (!std::memcmp(type, "IHDR", 4) && n >= 13) {
+      width = static_cast<int>(be32(data));
+      height = static_cast<int>(be32(data + 4));
+      depth = data[8];
+      ctype = data[9];
+      interlace = data[12];
+      have_hdr = true;
+    } else if (!std::memcmp(type, "IDAT", 4)) {
+      idat.insert(idat.end(), data, data + n);
+    } else if (!std::memcmp(type, "IEND", 4)) {
+      ended = true;
+    }
+    p += 12 + n;
+  }
+  if (!have_hdr || !ended) {
+    err = path + ": truncated PNG";
+    return false;
+  }
+  if (ctype != 0 || (depth != 8 && depth != 16) || interlace != 0 || width <= 0 || height <= 0 ||
+      static_cast<long long>(width) * height > (1LL << 28)) {
+    err = path + ": only non-interlaced 8- or 16-bit grayscale PNG is supported";
+    return false;
+  }
+  const size_t bpp = depth / 8, stride = static_cast<size_t>(width) * bpp;
+  std::vector<unsigned char> raw((stride + 1) * height);
+  uLongf rawlen = static_cast<uLongf>(raw.size());
+  if (uncompress(raw.data(), &rawlen, idat.data(), static_cast<uLong>(idat.size())) != Z_OK || rawlen != raw.size()) {
+    err = path + ": corrupt image data";
+    return false;
+  }
+  std::vector<unsigned char> prev(stride, 0), cur(stride);
+  pixels.resize(static_cast<size_t>(width) * height);
+  for (int y = 0; y < height; ++y) {
+    const unsigned char* row = &raw[y * (stride + 1)];
+    const int filter = row[0];
+    for (size_t i = 0; i < stride; ++i) {
+      const int x = row[1 + i];
+      const int a = i >= bpp ? cur[i - bpp] : 0, b = prev[i], c = i >= bpp ? prev[i - bpp] : 0;
+      int v;
+      switch (filter) {
+        case 0: v = x; break;
+        case 1: v = x + a; break;
+        case 2: v = x + b; break;
+        case 3: v = x + ((a + b) >> 1); break;
+        case 4: v = x + paeth(a, b, c); break;
+        default:
+          err = path + ": unknown scanline filter";
+          return false;
+      }
+      cur[i] = static_cast<unsigned char>(v & 255);
+    }
+    for (int x = 0; x < width; ++x)
+      pixels[static_cast<size_t>(y) * width + x] =
+          bpp == 2 ? static_cast<uint16_t>((cur[2 * x] << 8) | cur[2 * x + 1]) : cur[x];
+    prev.swap(cur);
+  }
+  return true;
+}
+
+bool write(const std::string& path, const uint16_t* pixels, int width, int height, std::string& err) {
+  const size_t stride = static_cast<size_t>(width) * 2;
+  std::vector<unsigned char> raw((stride + 1) * height);
+  for (int y = 0; y < height; ++y) {
+    unsigned char* row = &raw[y * (stride + 1)];
+    row[0] = 0;
+    for (int x = 0; x < width; ++x) {
+      const uint16_t v = pixels[static_cast<size_t>(y) * width + x];
+      row[1 + 2 * x] = static_cast<unsigned char>(v >> 8);
+      row[2 + 2 * x] = static_cast<unsigned char>(v & 255);
+    }
+  }
+  uLongf zlen = compressBound(static_cast<uLong>(raw.size()));
+  std::vector<unsigned char> z(zlen);
+  if (compress2(z.data(), &zlen, raw.data(), static_cast<uLong>(raw.size()), 6) != Z_OK) {
+    err = "compression failed";
+    return false;
+  }
+  std::vector<unsigned char> out(kSig, kSig + 8);
+  unsigned char hdr[13];
+  const uint32_t w = static_cast<uint32_t>(width), h = static_cast<uint32_t>(height);
+  const unsigned char ih[13] = {static_cast<unsigned char>(w >> 24), static_cast<unsigned char>(w >> 16),
+                                static_cast<unsigned char>(w >> 8),  static_cast<unsigned char>(w),
+                                static_cast<unsigned char>(h >> 24), static_cast<unsigned char>(h >> 16),
+                                static_cast<unsigned char>(h >> 8),  static_cast<unsigned char>(h),
+                                16, 0, 0, 0, 0};
+  std::memcpy(hdr, ih, 13);
+  chunk(out, "IHDR", hdr, 13);
+  chunk(out, "IDAT", z.data(), zlen);
+  chunk(out, "IEND", nullptr, 0);
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) {
+    err = "cannot create " + path;
+    return false;
+  }
+  const bool ok = std::fwrite(out.data(), 1, out.size(), f) == out.size();
+  return (std::fclose(f) == 0) && ok ? true : (err = "write failed: " + path, false);
+}
+
+}  // namespace png16

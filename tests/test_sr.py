@@ -8,6 +8,11 @@ close to the truth and to the oracle's, the fused image equal to the
 oracle's within one unit of rounding."""
 from __future__ import annotations
 
+import struct
+import subprocess
+import zlib
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -97,3 +102,124 @@ def test_super_resolve_single_frame_is_a_lanczos_round_trip(ctx):
     assert its[0] == 0
     assert np.mean(np.abs(out.astype(np.int64) - want.astype(np.int64)) <= 1) > 0.999
     assert np.mean(np.abs(out.astype(np.int64) - frames[0].astype(np.int64))) < 3.0
+
+
+# ------------------------------------------------------------------ the tool
+# capture/super_resolution/super_resolution.cpp: flags and messages (:142-211),
+# <name>_burst_<view>_<i>.png in, <name>_srdepth_<view>.png and
+# <name>_srmesh_<view>.ply out.
+BIN = Path(__file__).resolve().parents[1] / "lowcost3dreconstruction_gb300" / "bin"
+
+
+def _paeth(a: int, b: int, c: int) -> int:
+    p = a + b - c
+    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+    return a if pa <= pb and pa <= pc else (b if pb <= pc else c)
+
+
+def write_png16(path, img: np.ndarray) -> None:
+    """16-bit grayscale PNG, row y filtered with filter type y % 5 so that the
+    tool's decoder meets every scanline filter."""
+    h, w = img.shape
+    be = img.astype(">u2").tobytes()
+    stride = 2 * w
+    raw = bytearray()
+    prev = bytes(stride)
+    for y in range(h):
+        row = be[y * stride:(y + 1) * stride]
+        ft = y % 5
+        out = bytearray([ft])
+        for i in range(stride):
+            a = row[i - 2] if i >= 2 else 0
+            b = prev[i]
+            c = prev[i - 2] if i >= 2 else 0
+            pred = (0, a, b, (a + b) // 2, _paeth(a, b, c))[ft]
+            out.append((row[i] - pred) & 255)
+        raw += out
+        prev = row
+
+    def chunk(t: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + t + data + struct.pack(">I", zlib.crc32(t + data) & 0xFFFFFFFF)
+    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 16, 0, 0, 0, 0))
+    png += chunk(b"IDAT", zlib.compress(bytes(raw), 6)) + chunk(b"IEND", b"")
+    Path(path).write_bytes(png)
+
+
+def read_png16(path) -> np.ndarray:
+    """The tool's output: 16-bit grayscale, filter type 0 on every row."""
+    data = Path(path).read_bytes()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, idat, w, h = 8, b"", 0, 0
+    while pos < len(data):
+        n, = struct.unpack(">I", data[pos:pos + 4])
+        t, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
+        assert struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])[0] == zlib.crc32(t + body) & 0xFFFFFFFF
+        if t == b"IHDR":
+            w, h, depth, color = struct.unpack(">IIBB", body[:10])
+            assert depth == 16 and color == 0
+        elif t == b"IDAT":
+            idat += body
+        pos += 12 + n
+    raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, 1 + 2 * w)
+    assert np.all(raw[:, 0] == 0)
+    return raw[:, 1:].copy().view(">u2").astype(np.uint16).reshape(h, w)
+
+
+def run_tool(*args, cwd):
+    return subprocess.run([str(BIN / "super_resolution"), *map(str, args)], capture_output=True, text=True,
+                          timeout=300, cwd=cwd)
+
+
+@pytest.fixture(scope="module")
+def sr_tool():
+    from lowcost3dreconstruction_gb300 import build
+    build.build_lib()
+    build.build_tools()
+    if not (BIN / "super_resolution").exists():
+        pytest.skip("super_resolution needs zlib headers")
+
+
+def test_png_writer_reader_round_trip(tmp_path):
+    img = np.random.default_rng(0).integers(0, 65536, (7, 11)).astype(np.uint16)
+    write_png16(tmp_path / "a.png", img)
+    data = (tmp_path / "a.png").read_bytes()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n" and b"IHDR" in data
+
+
+def test_tool_help_and_usage_errors(sr_tool, tmp_path):
+    r = run_tool("-h", cwd=tmp_path)
+    assert r.returncode == 0
+    for f in ("--capture_name", "--capture_step", "--num_captures", "--sr_size", "--resample_factor",
+              "--view_angle", "--top", "--bottom"):
+        assert f in r.stdout, f
+    assert "(=artefact)" in r.stdout and "(=16)" in r.stdout and "(=4)" in r.stdout
+    r = run_tool("-f", "0", cwd=tmp_path)
+    assert r.returncode == 255 and "must be bigger than zero" in r.stdout
+    r = run_tool("-a", "20", "-t", cwd=tmp_path)
+    assert r.returncode == 255 and "can not be used together" in r.stdout
+    r = run_tool("-a", "20", "-n", "missing", cwd=tmp_path)
+    assert r.returncode == 255 and "Image can not be read: missing_burst_20_0.png" in r.stdout
+
+
+@pytest.mark.gpu
+def test_tool_writes_the_fused_depth_and_cloud(sr_tool, tmp_path, ctx):
+    from lowcost3dreconstruction_gb300 import _lib as L
+    frames, _ = burst(h=48, w=64, F=4, seed=5, holes=False)
+    for i, f in enumerate(frames):
+        write_png16(tmp_path / f"obj_burst_top_{i}.png", f)
+    r = run_tool("-n", "obj", "-t", "-z", 4, "-f", 4, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    want, warps, mm, _ = ctx.super_resolve(frames, factor=4)
+    assert f"Observed Global Min: {mm[0]:.0f}" in r.stdout
+    assert f"Observed Global Max: {mm[1]:.0f}" in r.stdout
+    assert "View(top) Alignment 3-> 0 = [" in r.stdout
+    got = read_png16(tmp_path / "obj_srdepth_top.png")
+    np.testing.assert_array_equal(got, want)
+    pts = L.read_ply(tmp_path / "obj_srmesh_top.ply")
+    p = L.DepthParams(L.KINECT_V1, 64, 48, 1, 572.882768, 542.739980, 314.649173, 240.160459, mm[0], mm[1],
+                      0, 63, 0, 47, 1.0, 1, 128, 128, 128, 0)
+    cloud = ctx.backproject(want, p).download()
+    assert len(pts) == len(cloud) > 0
+    np.testing.assert_allclose(pts["x"], cloud["x"], rtol=1e-6, atol=1e-4)
+    np.testing.assert_allclose(pts["z"], cloud["z"], rtol=1e-6, atol=1e-4)
+    assert (tmp_path / "obj_srmesh_top.ply").read_bytes().startswith(b"ply\nformat ascii")

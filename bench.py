@@ -562,6 +562,75 @@ def sfm_arm(args) -> dict:
                                        "64 to 1024 hypotheses) on the first 100k points"}}
 
 
+def sr_arm(args) -> dict:
+    """The super-resolution front end of capture/super_resolution (:236-314) on
+    the reference's default capture: 18 views, each a burst of 16 Kinect v1
+    frames of 640 x 480, fused at resample factor 4.  A frame is a smooth
+    depth scene seen under a small random rigid motion (<= 0.4 deg, <= 0.8 px)
+    with 0.3 mm noise.  One step is one view through lcr_super_resolve from
+    host buffers (upload, ECC registration of 15 frames, warp, upsampling,
+    ZE-mean, Lanczos-4, download); CUDA events on the library's stream.  The
+    CPU oracle runs one 3-frame view, scaled to 16 frames by its registrations."""
+    import torch
+
+    from lowcost3dreconstruction_gb300.core import Context
+    from oracle import sr as OSR
+    torch.cuda.set_device(0)
+    h, w, F, views = 480, 640, 16, 18
+    rng = np.random.default_rng(21)
+    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+
+    def scene(X, Y):
+        return (1000 + 120 * np.sin(X / 27.0) * np.cos(Y / 21.0) + 60 * np.exp(-((X - 320) ** 2 + (Y - 240) ** 2)
+                                                                            / 1800.0) + 0.3 * X - 0.2 * Y)
+    bursts = []
+    for v in range(views):
+        fr = []
+        for f in range(F):
+            a = 0.0 if f == 0 else np.deg2rad(rng.uniform(-0.4, 0.4))
+            tx, ty = (0.0, 0.0) if f == 0 else rng.uniform(-0.8, 0.8, 2)
+            X = np.cos(a) * x - np.sin(a) * y + tx + 7 * v
+            Y = np.sin(a) * x + np.cos(a) * y + ty
+            fr.append(np.clip(np.rint(scene(X, Y) + rng.normal(0, 0.3, x.shape)), 0, 65535).astype(np.uint16))
+        bursts.append(np.stack(fr))
+    ctx = Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=0)
+    for i in range(args.warmup):
+        ctx.super_resolve(bursts[i % views])
+    l0 = ctx.launches
+    iters = []
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(args.steps):
+        _, _, _, it = ctx.super_resolve(bursts[i % views])
+        iters.append(int(it.sum()))
+    e1 = torch.cuda.Event(enable_timing=True)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = (ctx.launches - l0) // args.steps
+    ctx.close()
+    t0 = time.perf_counter()
+    OSR.super_resolve(bursts[0][:3], 4)
+    dt = (time.perf_counter() - t0) / 2 * (F - 1)
+    return {"metric": "depth views/s through the super-resolution front end (ECC + warp + ZE-mean + Lanczos-4)",
+            "value": round(1000.0 / ms, 3), "unit": "views/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP64 ECC sums)", "data": "synthetic",
+            "config": {"workload": "18 views x 16-frame 640x480 Kinect v1 bursts, resample factor 4, ECC <= 200 "
+                                   "iterations, eps 1e-12", "mean_ecc_iterations_per_view": round(
+                                       float(np.mean(iters)), 1),
+                       "l2": "each view's burst (9.8 MB in, 4x upsampled 19.7 MB float) is uploaded per step"},
+            "roofline": None,
+            "e2e": {"value": round(1000.0 / ms, 3), "unit": "views/s", "h2d_bytes_per_step": F * h * w * 2,
+                    "d2h_bytes_per_step": h * w * 2 + F * 24 + 8 + F * 4},
+            "gpu_launches": launches,
+            "cpu_baseline": {"value": round(1.0 / dt, 5), "unit": "views/s", "cores": 1, "kind": "port",
+                             "sample": "the numpy oracle on a 3-frame view of the same burst, scaled by its two "
+                                       "registrations to 15"}}
+
+
 # ------------------------------------------------------------ CPU (oracle)
 def cpu_pipeline(pr, threads: int):
     from lowcost3dreconstruction_gb300 import synthetic as S
@@ -627,10 +696,11 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="config1",
-                    choices=["config1", "turntable36", "proposal", "large512", "sfm"],
+                    choices=["config1", "turntable36", "proposal", "large512", "sfm", "sr"],
                     help="config1: the headline pair pipeline; turntable36: batched ICP over a turntable cycle; "
                          "proposal: learned pose proposal + ICP vs plain ICP on held-out pairs; large512: the same "
-                         "on 512 pairs of 5k-500k points per view; sfm: the SfM-side filters on a 1M-point model")
+                         "on 512 pairs of 5k-500k points per view; sfm: the SfM-side filters on a 1M-point model; sr: the "
+                         "super-resolution front end on 16-frame 640x480 bursts")
     ap.add_argument("--pairs", type=int, default=2000, help="pairs of the proposal workload")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
@@ -646,6 +716,9 @@ def main():
     elif args.workload == "sfm":
         build.build_lib()
         out = sfm_arm(args) if rank == 0 else None
+    elif args.workload == "sr":
+        build.build_lib()
+        out = sr_arm(args) if rank == 0 else None
     elif args.workload in ("proposal", "large512"):
         build.build_lib()
         out = proposal_arm(args) if rank == 0 else None

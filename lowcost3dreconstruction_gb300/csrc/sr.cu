@@ -16,10 +16,13 @@
 //     saturated to uint16                                           :312-314
 //
 // All frames of a burst register at once: one pass per iteration accumulates
-// for every frame the 45 sums the Gauss-Newton step needs (FP32 products,
-// FP64 sums in a fixed order), and one thread per frame solves the 6x6 system.
+// for every frame the 45 sums the Gauss-Newton step needs (exact FP64 products
+// for the correlation coefficient, compensated FP32 for the Jacobian terms,
+// FP64 reductions in a fixed order), and one thread per frame solves the 6x6
+// system.
 // The smoothing and gradient filters mirror the border at its edge pixel
 // (reflect-101); the Lanczos taps clamp to the image.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -38,12 +41,12 @@ __device__ __forceinline__ int reflect101(int i, int n) {
 __global__ void k_sr_float(const uint16_t* __restrict__ in, size_t n, float* __restrict__ out,
                            unsigned int* __restrict__ minmax) {
   const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const uint16_t v = in[i];
-  out[i] = static_cast<float>(v);
-  if (v > 0) {
-    atomicMin(&minmax[0], v);
-    atomicMax(&minmax[1], v);
+  const unsigned v = i < n ? in[i] : 0u;
+  if (i < n) out[i] = static_cast<float>(v);
+  const unsigned lo = __reduce_min_sync(LCR_FULL, v > 0 ? v : 0xffffffffu), hi = __reduce_max_sync(LCR_FULL, v);
+  if ((threadIdx.x & 31) == 0 && hi > 0) {
+    atomicMin(&minmax[0], lo);
+    atomicMax(&minmax[1], hi);
   }
 }
 
@@ -96,149 +99,100 @@ __device__ __forceinline__ float bilinear(const float* __restrict__ f, int w, in
   return top * (1.f - ay) + bot * ay;
 }
 
-// One ECC pass for frame f = 1 + blockIdx.y: per template pixel (x, y) the
-// input sampled at W(x, y) = (m0 x + m1 y + m2, m3 x + m4 y + m5), its
-// gradients, the validity mask (all four bilinear taps inside the image: a
-// half-outside sample of a depth image is a large outlier) and the masked
-// Jacobian J = (x gx, x gy, y gx, y gy, gx, gy) with respect to
-// (m0, m3, m1, m4, m2, m5); the block's 45 sums go to part[frame][block][45].
-constexpr int kEccThreads = 256;
-__global__ void __launch_bounds__(kEccThreads) k_ecc_pass(const float* __restrict__ tmpl, const float* __restrict__ img,
-                                                           const float* __restrict__ gxs, const float* __restrict__ gys,
-                                                           int w, int h, const float* __restrict__ warps,
-                                                           const int* __restrict__ active, double* __restrict__ part) {
-  const int f = 1 + blockIdx.y;
-  if (!active[f]) return;
-  __shared__ double red[kEccThreads / 32][kSums];
-  const float* m = warps + 6 * f;
-  const size_t plane = static_cast<size_t>(w) * h;
-  const float* I = img + f * plane;
-  const float* GX = gxs + f * plane;
-  const float* GY = gys + f * plane;
-  double acc[kSums];
-#pragma unroll
-  for (int k = 0; k < kSums; ++k) acc[k] = 0.0;
-  const int npix = w * h;
-  for (int p = blockIdx.x * kEccThreads + threadIdx.x; p < npix; p += gridDim.x * kEccThreads) {
-    const int x = p % w, y = p / w;
-    const float u = m[0] * x + m[1] * y + m[2], v = m[3] * x + m[4] * y + m[5];
-    const float iw = bilinear(I, w, h, u, v), gx = bilinear(GX, w, h, u, v), gy = bilinear(GY, w, h, u, v);
-    const float fu = floorf(u), fv = floorf(v);
-    const float mk = (fu >= 0.f && fv >= 0.f && fu + 1.f < w && fv + 1.f < h) ? 1.f : 0.f;
-    const float t = tmpl[p];
-    const float J[6] = {mk * x * gx, mk * x * gy, mk * y * gx, mk * y * gy, mk * gx, mk * gy};
-    const float mi = mk * iw, mt = mk * t;
-    acc[0] += mk;
-    acc[1] += mi;
-    acc[2] += mi * iw;
-    acc[3] += mt;
-    acc[4] += mt * t;
-    acc[5] += mi * t;
-    int q = 24;
-#pragma unroll
-    for (int a = 0; a < 6; ++a) {
-      acc[6 + a] += mk * J[a];
-      acc[12 + a] += J[a] * mi;
-      acc[18 + a] += J[a] * mt;
-#pragma unroll
-      for (int b = a; b < 6; ++b) acc[q++] += J[a] * J[b];
-    }
-  }
-  // warp butterflies, then warps in order
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < kSums; ++k) {
-    double v = acc[k];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(LCR_FULL, v, o);
-    if (lane == 0) red[wid][k] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < kSums) {
-    double s = 0.0;
-    for (int j = 0; j < kEccThreads / 32; ++j) s += red[j][threadIdx.x];
-    part[(static_cast<size_t>(f) * gridDim.x + blockIdx.x) * kSums + threadIdx.x] = s;
-  }
+// (a.x + a.y) + (b.x + b.y) as a pair of FP32 values: the exact two-sum of
+// the leading parts, the trailing parts and its error renormalised into the
+// pair (about 44 significant bits for sums of like-signed terms).
+__device__ __forceinline__ float2 pair_add(float2 a, float2 b) {
+  const float sum = __fadd_rn(a.x, b.x), bp = __fsub_rn(sum, a.x);
+  const float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(sum, bp)), __fsub_rn(b.x, bp));
+  const float l = __fadd_rn(__fadd_rn(a.y, b.y), e);
+  const float hi = __fadd_rn(sum, l);
+  return make_float2(hi, __fsub_rn(l, __fsub_rn(hi, sum)));
 }
 
-// Solves the 6x6 SPD-ish system A x = b by Gaussian elimination with partial
-// pivoting (FP64); returns false when singular.
-__device__ bool solve6(double A[6][6], double b[6], double x[6]) {
-  for (int c = 0; c < 6; ++c) {
-    int piv = c;
-    for (int r = c + 1; r < 6; ++r)
-      if (fabs(A[r][c]) > fabs(A[piv][c])) piv = r;
-    if (!(fabs(A[piv][c]) > 0.0)) return false;
-    if (piv != c) {
-      for (int k = 0; k < 6; ++k) {
-        const double t = A[c][k];
-        A[c][k] = A[piv][k];
-        A[piv][k] = t;
-      }
-      const double t = b[c];
-      b[c] = b[piv];
-      b[piv] = t;
-    }
-    for (int r = c + 1; r < 6; ++r) {
-      const double fct = A[r][c] / A[c][c];
-      for (int k = c; k < 6; ++k) A[r][k] -= fct * A[c][k];
-      b[r] -= fct * b[c];
+// Solves H x1 = b1 and H x2 = b2 for the symmetric positive definite 6x6
+// Gauss-Newton matrix H = sum J^T J by one LDL^T factorisation (FP64, no
+// square roots, one reciprocal per pivot, every index fixed at compile time
+// so that it all stays in registers: FP64 latency is what bounds this
+// single-thread step); false when H is not positive definite.
+__device__ __forceinline__ bool ldl_solve6(const double H[6][6], const double b1[6], const double b2[6],
+                                           double x1[6], double x2[6]) {
+  double L[6][6], E[6][6], dinv[6];  // L unit lower triangular, E = L D
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    double d = H[j][j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) d -= E[j][k] * L[j][k];
+    if (!(d > 0.0)) return false;
+    dinv[j] = 1.0 / d;
+#pragma unroll
+    for (int i = j + 1; i < 6; ++i) {
+      double t = H[i][j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) t -= E[i][k] * L[j][k];
+      E[i][j] = t;
+      L[i][j] = t * dinv[j];
     }
   }
-  for (int r = 5; r >= 0; --r) {
-    double s = b[r];
-    for (int k = r + 1; k < 6; ++k) s -= A[r][k] * x[k];
-    x[r] = s / A[r][r];
+  double y1[6], y2[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double t1 = b1[i], t2 = b2[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) {
+      t1 -= L[i][k] * y1[k];
+      t2 -= L[i][k] * y2[k];
+    }
+    y1[i] = t1;
+    y2[i] = t2;
+  }
+#pragma unroll
+  for (int i = 5; i >= 0; --i) {
+    double t1 = y1[i] * dinv[i], t2 = y2[i] * dinv[i];
+#pragma unroll
+    for (int k = i + 1; k < 6; ++k) {
+      t1 -= L[k][i] * x1[k];
+      t2 -= L[k][i] * x2[k];
+    }
+    x1[i] = t1;
+    x2[i] = t2;
   }
   return true;
 }
 
-// One thread per frame: sums over the blocks in order, the ECC step, the
-// warp update and the convergence test |rho - rho_prev| < eps.
-__global__ void k_ecc_step(const double* __restrict__ part, int nblocks, int F, float* __restrict__ warps,
-                           double* __restrict__ rho, int* __restrict__ active, int* __restrict__ iters, double eps,
-                           int max_iter, int* __restrict__ any_active) {
-  const int f = 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= F || !active[f]) return;
-  double s[kSums];
-  for (int k = 0; k < kSums; ++k) s[k] = 0.0;
-  for (int bk = 0; bk < nblocks; ++bk)
-    for (int k = 0; k < kSums; ++k) s[k] += part[(static_cast<size_t>(f) * nblocks + bk) * kSums + k];
+// The ECC step of frame f from its 45 sums: correlation coefficient, the
+// Gauss-Newton update of the warp, the stopping tests (iteration limit,
+// |rho - rho_prev| < eps, a singular system, no improvement along the step).
+__device__ void ecc_step(const double* s, int f, float* warps, double* rho, int* active, int* iters, double eps,
+                         int max_iter) {
   const double n = s[0];
   iters[f] += 1;
   if (!(n > 0.0)) {
     active[f] = 0;
     return;
   }
-  const double mi = s[1] / n, mt = s[3] / n;
+  const double inv_n = 1.0 / n, mi = s[1] * inv_n, mt = s[3] * inv_n;
   const double img_var = s[2] - n * mi * mi, tmp_var = s[4] - n * mt * mt;
   const double corr = s[5] - mi * s[3] - mt * s[1] + n * mi * mt;
-  const double inorm = sqrt(fmax(img_var, 0.0)), tnorm = sqrt(fmax(tmp_var, 0.0));
-  const double r = inorm > 0 && tnorm > 0 ? corr / (inorm * tnorm) : 0.0;
+  const double r = img_var > 0.0 && tmp_var > 0.0 ? corr * rsqrt(img_var * tmp_var) : 0.0;
   double ip[6], tp[6], H[6][6];
+#pragma unroll
   for (int a = 0; a < 6; ++a) {
     ip[a] = s[12 + a] - mi * s[6 + a];
     tp[a] = s[18 + a] - mt * s[6 + a];
   }
   int q = 24;
+#pragma unroll
   for (int a = 0; a < 6; ++a)
+#pragma unroll
     for (int b = a; b < 6; ++b) H[a][b] = H[b][a] = s[q++];
-  // H^-1 ip and H^-1 tp
-  double Hc[6][6], b1[6], hi[6], ht[6];
-  for (int a = 0; a < 6; ++a) {
-    for (int b = 0; b < 6; ++b) Hc[a][b] = H[a][b];
-    b1[a] = ip[a];
-  }
-  bool ok = solve6(Hc, b1, hi);
-  for (int a = 0; a < 6; ++a) {
-    for (int b = 0; b < 6; ++b) Hc[a][b] = H[a][b];
-    b1[a] = tp[a];
-  }
-  ok = ok && solve6(Hc, b1, ht);
-  if (!ok) {
+  double hi[6], ht[6];  // H^-1 ip and H^-1 tp
+  if (!ldl_solve6(H, ip, tp, hi, ht)) {
     active[f] = 0;
     return;
   }
   double lam_n = img_var, lam_d = corr;
+#pragma unroll
   for (int a = 0; a < 6; ++a) {
     lam_n -= ip[a] * hi[a];
     lam_d -= tp[a] * hi[a];
@@ -250,6 +204,7 @@ __global__ void k_ecc_step(const double* __restrict__ part, int nblocks, int F, 
   const double lam = lam_n / lam_d;
   // deltaP = H^-1 (lam tp - ip) = lam ht - hi
   double dp[6];
+#pragma unroll
   for (int a = 0; a < 6; ++a) dp[a] = lam * ht[a] - hi[a];
   float* m = warps + 6 * f;
   m[0] += static_cast<float>(dp[0]);
@@ -261,95 +216,215 @@ __global__ void k_ecc_step(const double* __restrict__ part, int nblocks, int F, 
   const double prev = rho[f];
   rho[f] = r;
   if (fabs(r - prev) < eps || iters[f] >= max_iter) active[f] = 0;
-  if (active[f]) atomicExch(any_active, 1);
 }
 
-// Frames 1.. warped onto frame 0 (inverse map), frame 0 copied.
-__global__ void k_sr_warp(const float* __restrict__ in, int w, int h, const float* __restrict__ warps,
-                          float* __restrict__ out) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, f = blockIdx.z;
-  if (x >= w) return;
-  const size_t plane = static_cast<size_t>(w) * h, o = f * plane + static_cast<size_t>(y) * w + x;
-  if (f == 0) {
-    out[o] = in[o];
-    return;
+// One ECC pass for frame f = 1 + blockIdx.y: per template pixel (x, y) the
+// input sampled at W(x, y) = (m0 x + m1 y + m2, m3 x + m4 y + m5), its
+// gradients, the validity mask (all four bilinear taps inside the image: a
+// half-outside sample of a depth image is a large outlier) and the masked
+// Jacobian J = (x gx, x gy, y gx, y gy, gx, gy) with respect to
+// (m0, m3, m1, m4, m2, m5); the block's 45 sums go to part[frame][block][45].
+constexpr int kEccThreads = 256;
+__global__ void __launch_bounds__(kEccThreads, 2) k_ecc_pass(const float* __restrict__ tmpl, const float* __restrict__ img,
+                                                           const float* __restrict__ gxs, const float* __restrict__ gys,
+                                                           int w, int h, const int* __restrict__ list, float* warps,
+                                                           int* active, float2* part, unsigned int* done, double* rho,
+                                                           int* iters, double eps, int max_iter) {
+  const int f = list[blockIdx.y];
+  if (!active[f]) return;
+  __shared__ float2 red[kEccThreads / 32][kSums];
+  const float m[6] = {warps[6 * f], warps[6 * f + 1], warps[6 * f + 2],
+                      warps[6 * f + 3], warps[6 * f + 4], warps[6 * f + 5]};
+  const size_t plane = static_cast<size_t>(w) * h;
+  const float* I = img + f * plane;
+  const float* GX = gxs + f * plane;
+  const float* GY = gys + f * plane;
+  // Every sum is kept as an unevaluated pair hi + lo of FP32 values (FP32
+  // pipes only: the FP64 ones are a small fraction of them on this part).
+  // The five sums of the correlation coefficient are exact to ~2^-44: the
+  // products split exactly by an FMA (p + e = a b), p added by an exact
+  // two-sum, the errors collected in lo.  The coefficient's change is the
+  // stopping test, and FP32 rounding of I^2 at depths near 1000 would leave
+  // it jittering by ~1e-8 between iterations, so the iteration would never
+  // stop at eps ~1e-12.  The 39 Jacobian sums take FP32 products with Kahan
+  // compensation.  Pairs are added across the warp by the same two-sum and
+  // widened to FP64 for the block and grid reductions.
+  int rn = 0;
+  float rh[5], rl[5];  // SI, SII, ST, STT, SIT
+  float ks[kSums - 6], kc[kSums - 6];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) rh[k] = rl[k] = 0.f;
+#pragma unroll
+  for (int k = 0; k < kSums - 6; ++k) ks[k] = kc[k] = 0.f;
+  auto exact_add = [&](int k, float a, float b) {  // rh/rl[k] += a * b, b == 1 for a plain term
+    const float pp = __fmul_rn(a, b), pe = __fmaf_rn(a, b, -pp);
+    const float sum = __fadd_rn(rh[k], pp), bp = __fsub_rn(sum, rh[k]);
+    const float e = __fadd_rn(__fsub_rn(rh[k], __fsub_rn(sum, bp)), __fsub_rn(pp, bp));
+    rh[k] = sum;
+    rl[k] = __fadd_rn(rl[k], __fadd_rn(e, pe));
+  };
+  const int npix = w * h;
+  for (int p = blockIdx.x * kEccThreads + threadIdx.x; p < npix; p += gridDim.x * kEccThreads) {
+    const int y = p / w, x = p - y * w;
+    const float u = m[0] * x + m[1] * y + m[2], v = m[3] * x + m[4] * y + m[5];
+    const float fu = floorf(u), fv = floorf(v);
+    if (!(fu >= 0.f && fv >= 0.f && fu + 1.f < w && fv + 1.f < h)) continue;  // outside the mask: no terms
+    const float iw = bilinear(I, w, h, u, v), gx = bilinear(GX, w, h, u, v), gy = bilinear(GY, w, h, u, v);
+    const float t = tmpl[p];
+    rn += 1;
+    exact_add(0, iw, 1.f);
+    exact_add(1, iw, iw);
+    exact_add(2, t, 1.f);
+    exact_add(3, t, t);
+    exact_add(4, iw, t);
+    const float fx = static_cast<float>(x), fy = static_cast<float>(y);
+    const float J[6] = {fx * gx, fx * gy, fy * gx, fy * gy, gx, gy};
+    auto kadd = [&](int k, float val) {
+      const float yk = val - kc[k];
+      const float tk = ks[k] + yk;
+      kc[k] = (tk - ks[k]) - yk;
+      ks[k] = tk;
+    };
+    int q = 18;
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+      kadd(a, J[a]);
+      kadd(6 + a, J[a] * iw);
+      kadd(12 + a, J[a] * t);
+#pragma unroll
+      for (int b = a; b < 6; ++b) kadd(q++, J[a] * J[b]);
+    }
   }
-  const float* m = warps + 6 * f;
-  out[o] = bilinear(in + f * plane, w, h, m[0] * x + m[1] * y + m[2], m[3] * x + m[4] * y + m[5]);
+  // pairs across the warp (butterflies), then warps in order
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kSums; ++k) {
+    float2 v = k == 0 ? make_float2(static_cast<float>(rn), 0.f)
+             : k <= 5 ? make_float2(rh[k - 1], rl[k - 1]) : make_float2(ks[k - 6], -kc[k - 6]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float2 other = make_float2(__shfl_xor_sync(LCR_FULL, v.x, o), __shfl_xor_sync(LCR_FULL, v.y, o));
+      v = pair_add(v, other);
+    }
+    if (lane == 0) red[wid][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < kSums) {
+    float2 v = red[0][threadIdx.x];
+#pragma unroll
+    for (int j = 1; j < kEccThreads / 32; ++j) v = pair_add(v, red[j][threadIdx.x]);
+    part[(static_cast<size_t>(f) * gridDim.x + blockIdx.x) * kSums + threadIdx.x] = v;
+  }
+  // The last block of the frame to finish adds the blocks' sums in a fixed
+  // order (warp j takes blocks j, j + 8, ...; then the warps in order) and
+  // takes the step; every block has read the warp before it counts itself,
+  // so the update races with no reader.
+  __shared__ bool last;
+  __shared__ double total[kSums];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&done[f], 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const float2* pp = part + static_cast<size_t>(f) * gridDim.x * kSums;
+  for (int k = lane; k < kSums; k += 32) {
+    float2 v = make_float2(0.f, 0.f);
+#pragma unroll 8
+    for (unsigned bk = wid; bk < gridDim.x; bk += kEccThreads / 32)
+      v = pair_add(v, __ldcg(pp + static_cast<size_t>(bk) * kSums + k));
+    red[wid][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < kSums) {
+    float2 v = red[0][threadIdx.x];
+#pragma unroll
+    for (int j = 1; j < kEccThreads / 32; ++j) v = pair_add(v, red[j][threadIdx.x]);
+    total[threadIdx.x] = static_cast<double>(v.x) + static_cast<double>(v.y);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    done[f] = 0;
+    ecc_step(total, f, warps, rho, active, iters, eps, max_iter);
+  }
 }
 
-// High-resolution ZE-mean: HR(y, x) = mean of the positive warped_k(y / s, x / s)
-// (FP64 sum in frame order, divided by the count, to float; 0/0 = NaN).
-__global__ void k_sr_zemean(const float* __restrict__ warped, int w, int h, int F, int s, float* __restrict__ hr) {
-  const int W = w * s;
+// ZE-mean on the sensor grid (nearest upsampling by the factor commutes with
+// it, so the high-resolution image is never formed): ze(y, x) is the mean of
+// the positive values among frame 0 at (x, y) and frames k >= 1 sampled at
+// W_k(x, y) (the inverse-map bilinear warp, zero outside); FP64 sum in frame
+// order divided by the count, to float; 0/0 = NaN.
+__global__ void k_sr_fuse(const float* __restrict__ in, int w, int h, int F, const float* __restrict__ warps,
+                          float* __restrict__ ze) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-  if (x >= W) return;
-  const size_t src = static_cast<size_t>(y / s) * w + x / s, plane = static_cast<size_t>(w) * h;
+  if (x >= w) return;
+  const size_t plane = static_cast<size_t>(w) * h, o = static_cast<size_t>(y) * w + x;
   double sum = 0.0;
   int cnt = 0;
-  for (int k = 0; k < F; ++k) {
-    const float v = warped[k * plane + src];
+  for (int f = 0; f < F; ++f) {
+    const float* m = warps + 6 * f;
+    const float v = f == 0 ? in[o] : bilinear(in + f * plane, w, h, m[0] * x + m[1] * y + m[2], m[3] * x + m[4] * y + m[5]);
     if (v > 0.f) {
       sum += v;
       ++cnt;
     }
   }
-  hr[static_cast<size_t>(y) * W + x] = static_cast<float>(sum / cnt);
+  ze[o] = static_cast<float>(sum / cnt);
 }
 
-// Lanczos (a = 4) weights of the 8 taps at floor(p) - 3 .. floor(p) + 4 for
-// the fractional position t = p - floor(p): L(d) = sinc(d) sinc(d / 4),
-// normalised to sum 1; t = 0 takes the centre tap alone.
-__device__ void lanczos4(float t, float wgt[8]) {
-  if (t < 1.1920929e-7f) {
-    for (int i = 0; i < 8; ++i) wgt[i] = i == 3 ? 1.f : 0.f;
-    return;
-  }
-  const double pi = 3.14159265358979323846;
-  double sum = 0.0, ww[8];
-  for (int i = 0; i < 8; ++i) {
-    const double d = (i - 3) - static_cast<double>(t);
-    const double a = pi * d;
-    ww[i] = 4.0 * sin(a) * sin(a / 4.0) / (a * a);
-    sum += ww[i];
-  }
-  for (int i = 0; i < 8; ++i) wgt[i] = static_cast<float>(ww[i] / sum);
-}
-
-// Resampling by 1/s along x (pass 0) or y (pass 1): output sample o reads the
-// source around p = (o + 0.5) s - 0.5, taps clamped to the image.
-__global__ void k_sr_lanczos(const float* __restrict__ in, int win, int hin, int wout, int hout, int axis, int s,
-                             float* __restrict__ out) {
+// Lanczos-4 resampling of the upsampled image by 1/s, one axis per pass:
+// output o reads the 8 upsampled samples base[o] .. base[o] + 7 (clamped to
+// the upsampled extent) with weights wgt[o][0..7]; upsampled sample X is
+// sensor sample X / s.  The horizontal pass runs on the h distinct rows.
+__global__ void k_sr_lanczos_h(const float* __restrict__ ze, int w, int s, const int* __restrict__ base,
+                               const float* __restrict__ wgt, float* __restrict__ half) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-  if (x >= wout || y >= hout) return;
-  const int o = axis == 0 ? x : y;
-  const float p = (o + 0.5f) * s - 0.5f;
-  const float fl = floorf(p);
-  float wgt[8];
-  lanczos4(p - fl, wgt);
-  const int base = static_cast<int>(fl) - 3;
+  if (x >= w) return;
+  const int W = w * s;
+  const float* row = ze + static_cast<size_t>(y) * w;
   float acc = 0.f;
-  for (int i = 0; i < 8; ++i) {
-    if (axis == 0) {
-      const int xx = min(max(base + i, 0), win - 1);
-      acc += wgt[i] * in[static_cast<size_t>(y) * win + xx];
-    } else {
-      const int yy = min(max(base + i, 0), hin - 1);
-      acc += wgt[i] * in[static_cast<size_t>(yy) * win + x];
-    }
-  }
-  out[static_cast<size_t>(y) * wout + x] = acc;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc += wgt[8 * x + i] * row[min(max(base[x] + i, 0), W - 1) / s];
+  half[static_cast<size_t>(y) * w + x] = acc;
 }
 
-// uint16 by rounding half to even, saturating; NaN -> 0.
-__global__ void k_sr_u16(const float* __restrict__ in, size_t n, uint16_t* __restrict__ out) {
-  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float v = in[i];
-  float r = rintf(v);
+// The vertical pass, rounded half to even and saturated to uint16 (NaN -> 0).
+__global__ void k_sr_lanczos_v(const float* __restrict__ half, int w, int h, int s, const int* __restrict__ base,
+                               const float* __restrict__ wgt, uint16_t* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= w) return;
+  const int H = h * s;
+  float acc = 0.f;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc += wgt[8 * y + i] * half[static_cast<size_t>(min(max(base[y] + i, 0), H - 1) / s) * w + x];
+  float r = rintf(acc);
   if (!(r > 0.f)) r = 0.f;
   if (r > 65535.f) r = 65535.f;
-  out[i] = static_cast<uint16_t>(r);
+  out[static_cast<size_t>(y) * w + x] = static_cast<uint16_t>(r);
+}
+
+// Lanczos (a = 4) taps of output o = 0 .. n - 1 of a resampling by 1/s: the
+// source position p = (o + 0.5) s - 0.5 (exact in binary), taps floor(p) - 3
+// .. floor(p) + 4 with weights L(d) = sinc(d) sinc(d / 4), normalised to sum
+// 1; a whole p takes the centre tap alone.
+void lanczos_table(int n, int s, int* base, float* wgt) {
+  const double pi = 3.14159265358979323846;
+  for (int o = 0; o < n; ++o) {
+    const double p = (o + 0.5) * s - 0.5, fl = std::floor(p), t = static_cast<float>(p - fl);
+    base[o] = static_cast<int>(fl) - 3;
+    float* wo = wgt + 8 * o;
+    if (t < 1.1920929e-7) {
+      for (int i = 0; i < 8; ++i) wo[i] = i == 3 ? 1.f : 0.f;
+      continue;
+    }
+    double sum = 0.0, ww[8];
+    for (int i = 0; i < 8; ++i) {
+      const double a = pi * ((i - 3) - t);
+      ww[i] = 4.0 * std::sin(a) * std::sin(a / 4.0) / (a * a);
+      sum += ww[i];
+    }
+    for (int i = 0; i < 8; ++i) wo[i] = static_cast<float>(ww[i] / sum);
+  }
 }
 
 }  // namespace
@@ -357,11 +432,17 @@ __global__ void k_sr_u16(const float* __restrict__ in, size_t n, uint16_t* __res
 void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F, int factor, int max_iter,
                        double eps, uint16_t* out, float* warps_out, float minmax_out[2], int* iters_out) {
   const size_t plane = static_cast<size_t>(w) * h, all = plane * F;
-  const int W = w * factor, H = h * factor;
-  const int nblocks = std::min(64, static_cast<int>((plane + kEccThreads - 1) / kEccThreads));
-  const size_t bytes = all * 2 + 6 * all * 4 + static_cast<size_t>(W) * H * 4 + static_cast<size_t>(w) * H * 4 +
-                       plane * 4 + plane * 2 + F * (24 + 8 + 8) + static_cast<size_t>(F) * nblocks * kSums * 8 + 64;
-  char* blk = static_cast<char*>(dev_alloc(ctx, bytes + 1024));
+  // The pass runs one wave of resident blocks, shared among the frames still
+  // iterating (the others return at once): many pixels per thread while all
+  // frames register, the whole GPU on the last one.
+  int per_sm = 1;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ecc_pass, kEccThreads, 0));
+  const int resident = std::max(1, per_sm) * ctx->sms;
+  const int nblocks = std::max(1, std::min(resident, static_cast<int>((plane + kEccThreads - 1) / kEccThreads)));
+  const size_t table = static_cast<size_t>(w + h) * 9 * 4;
+  const size_t bytes = all * 2 + 5 * all * 4 + 2 * plane * 4 + plane * 2 + table + F * (24 + 8 + 8 + 4) +
+                       static_cast<size_t>(F) * nblocks * kSums * 8 + 64;
+  char* blk = static_cast<char*>(dev_alloc(ctx, bytes + 32 * 256));  // every take() below pads to 256
   char* q = blk;
   auto take = [&](size_t b) {
     char* r = q;
@@ -374,16 +455,17 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
   auto* blur = reinterpret_cast<float*>(take(all * 4));
   auto* gx = reinterpret_cast<float*>(take(all * 4));
   auto* gy = reinterpret_cast<float*>(take(all * 4));
-  auto* warped = reinterpret_cast<float*>(take(all * 4));
-  auto* hr = reinterpret_cast<float*>(take(static_cast<size_t>(W) * H * 4));
-  auto* half = reinterpret_cast<float*>(take(static_cast<size_t>(w) * H * 4));
-  auto* lr = reinterpret_cast<float*>(take(plane * 4));
+  auto* ze = reinterpret_cast<float*>(take(plane * 4));
+  auto* half = reinterpret_cast<float*>(take(plane * 4));
+  auto* tab = take(table);
   auto* o16 = reinterpret_cast<uint16_t*>(take(plane * 2));
   auto* warps = reinterpret_cast<float*>(take(F * 24));
   auto* rho = reinterpret_cast<double*>(take(F * 8));
   auto* active = reinterpret_cast<int*>(take(F * 4));
   auto* iters = reinterpret_cast<int*>(take(F * 4));
-  auto* part = reinterpret_cast<double*>(take(static_cast<size_t>(F) * nblocks * kSums * 8));
+  auto* done = reinterpret_cast<unsigned int*>(take(F * 4));
+  auto* list = reinterpret_cast<int*>(take(F * 4));
+  auto* part = reinterpret_cast<float2*>(take(static_cast<size_t>(F) * nblocks * kSums * 8));
   auto* flags = reinterpret_cast<unsigned int*>(take(64));
   CUDA_TRY(cudaMemcpyAsync(d16, frames, all * 2, cudaMemcpyHostToDevice, ctx->stream));
   const unsigned int init[3] = {0xffffffffu, 0u, 0u};
@@ -410,21 +492,42 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
   CUDA_TRY(cudaMemcpyAsync(active, hact.data(), F * 4, cudaMemcpyHostToDevice, ctx->stream));
   CUDA_TRY(cudaMemcpyAsync(rho, hrho.data(), F * 8, cudaMemcpyHostToDevice, ctx->stream));
   CUDA_TRY(cudaMemsetAsync(iters, 0, F * 4, ctx->stream));
-  for (int it = 0; it < max_iter && F > 1; ++it) {
-    CUDA_TRY(cudaMemsetAsync(flags + 2, 0, 4, ctx->stream));
-    LCR_LAUNCH(ctx, k_ecc_pass, dim3(nblocks, F - 1), kEccThreads, 0, blur, blur, gx, gy, w, h, warps, active, part);
-    LCR_LAUNCH(ctx, k_ecc_step, (F + 63) / 64, 64, 0, part, nblocks, F, warps, rho, active, iters, eps, max_iter,
-               reinterpret_cast<int*>(flags + 2));
-    int any = 0;
-    CUDA_TRY(cudaMemcpyAsync(&any, flags + 2, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaMemsetAsync(done, 0, F * 4, ctx->stream));
+  // The host reads which frames are still iterating after 2, 4, 8, ... 32
+  // iterations and every 32 after that; the next iterations' wave of blocks
+  // is shared among those frames alone (blockIdx.y indexes their list), and
+  // a frame that stops within a chunk costs its blocks an early return.
+  std::vector<int> hlist;
+  for (int f = 1; f < F; ++f) hlist.push_back(f);
+  for (int it = 0, chunk = 2; it < max_iter && !hlist.empty(); chunk = std::min(2 * chunk, 32)) {
+    const int na = static_cast<int>(hlist.size()), nb = std::max(1, nblocks / na);
+    CUDA_TRY(cudaMemcpyAsync(list, hlist.data(), na * 4, cudaMemcpyHostToDevice, ctx->stream));
+    const int todo = std::min(chunk, max_iter - it);
+    for (int k = 0; k < todo; ++k, ++it)
+      LCR_LAUNCH(ctx, k_ecc_pass, dim3(nb, na), kEccThreads, 0, blur, blur, gx, gy, w, h, list, warps, active, part,
+                 done, rho, iters, eps, max_iter);
+    CUDA_TRY(cudaMemcpyAsync(hact.data(), active, F * 4, cudaMemcpyDeviceToHost, ctx->stream));
     sync(ctx);
-    if (!any) break;
+    hlist.clear();
+    for (int f = 1; f < F; ++f)
+      if (hact[f]) hlist.push_back(f);
   }
-  LCR_LAUNCH(ctx, k_sr_warp, gimg, 128, 0, img, w, h, warps, warped);
-  LCR_LAUNCH(ctx, k_sr_zemean, dim3((W + 127) / 128, H), 128, 0, warped, w, h, F, factor, hr);
-  LCR_LAUNCH(ctx, k_sr_lanczos, dim3((w + 127) / 128, H), 128, 0, hr, W, H, w, H, 0, factor, half);
-  LCR_LAUNCH(ctx, k_sr_lanczos, dim3((w + 127) / 128, h), 128, 0, half, w, H, w, h, 1, factor, lr);
-  LCR_LAUNCH(ctx, k_sr_u16, static_cast<unsigned>((plane + 255) / 256), 256, 0, lr, plane, o16);
+  std::vector<char> htab(table);
+  auto* xbase = reinterpret_cast<int*>(htab.data());
+  auto* ybase = xbase + w;
+  auto* xw = reinterpret_cast<float*>(ybase + h);
+  auto* yw = xw + 8 * w;
+  lanczos_table(w, factor, xbase, xw);
+  lanczos_table(h, factor, ybase, yw);
+  CUDA_TRY(cudaMemcpyAsync(tab, htab.data(), table, cudaMemcpyHostToDevice, ctx->stream));
+  const auto* dxbase = reinterpret_cast<const int*>(tab);
+  const auto* dybase = dxbase + w;
+  const auto* dxw = reinterpret_cast<const float*>(dybase + h);
+  const auto* dyw = dxw + 8 * w;
+  const dim3 grow((w + 127) / 128, h);
+  LCR_LAUNCH(ctx, k_sr_fuse, grow, 128, 0, img, w, h, F, warps, ze);
+  LCR_LAUNCH(ctx, k_sr_lanczos_h, grow, 128, 0, ze, w, factor, dxbase, dxw, half);
+  LCR_LAUNCH(ctx, k_sr_lanczos_v, grow, 128, 0, half, w, h, factor, dybase, dyw, o16);
   CUDA_TRY(cudaMemcpyAsync(out, o16, plane * 2, cudaMemcpyDeviceToHost, ctx->stream));
   if (warps_out) CUDA_TRY(cudaMemcpyAsync(warps_out, warps, F * 24, cudaMemcpyDeviceToHost, ctx->stream));
   if (iters_out) CUDA_TRY(cudaMemcpyAsync(iters_out, iters, F * 4, cudaMemcpyDeviceToHost, ctx->stream));

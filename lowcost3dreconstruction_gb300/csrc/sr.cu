@@ -38,15 +38,39 @@ __device__ __forceinline__ int reflect101(int i, int n) {
   return i;
 }
 
+// uint16 frames to float, and the range of the positive values: per-thread
+// over a grid-stride loop, then warp and block reductions, one atomic pair
+// per block (a pair per warp contends on the two words).
 __global__ void k_sr_float(const uint16_t* __restrict__ in, size_t n, float* __restrict__ out,
                            unsigned int* __restrict__ minmax) {
-  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const unsigned v = i < n ? in[i] : 0u;
-  if (i < n) out[i] = static_cast<float>(v);
-  const unsigned lo = __reduce_min_sync(LCR_FULL, v > 0 ? v : 0xffffffffu), hi = __reduce_max_sync(LCR_FULL, v);
-  if ((threadIdx.x & 31) == 0 && hi > 0) {
-    atomicMin(&minmax[0], lo);
-    atomicMax(&minmax[1], hi);
+  unsigned lo = 0xffffffffu, hi = 0u;
+  for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const unsigned v = in[i];
+    out[i] = static_cast<float>(v);
+    if (v > 0) {
+      lo = min(lo, v);
+      hi = max(hi, v);
+    }
+  }
+  lo = __reduce_min_sync(LCR_FULL, lo);
+  hi = __reduce_max_sync(LCR_FULL, hi);
+  __shared__ unsigned slo[32], shi[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) {
+    slo[wid] = lo;
+    shi[wid] = hi;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    lo = lane < nw ? slo[lane] : 0xffffffffu;
+    hi = lane < nw ? shi[lane] : 0u;
+    lo = __reduce_min_sync(LCR_FULL, lo);
+    hi = __reduce_max_sync(LCR_FULL, hi);
+    if (lane == 0 && hi > 0) {
+      atomicMin(&minmax[0], lo);
+      atomicMax(&minmax[1], hi);
+    }
   }
 }
 
@@ -75,15 +99,17 @@ __global__ void k_sr_blur_v(const float* __restrict__ in, int w, int h, float g0
   out[(static_cast<size_t>(blockIdx.z) * h + y) * w + x] = s;
 }
 
-// Central differences 0.5 (f(x+1) - f(x-1)), reflect-101 borders.
-__global__ void k_sr_grad(const float* __restrict__ in, int w, int h, float* __restrict__ gx,
-                          float* __restrict__ gy) {
+// Central differences 0.5 (f(x+1) - f(x-1)), reflect-101 borders, packed with
+// the smoothed value as (value, d/dx, d/dy, 0): the registration reads all
+// three at each bilinear tap with one 16-byte load.
+__global__ void k_sr_grad(const float* __restrict__ in, int w, int h, float4* __restrict__ pk) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
   if (x >= w) return;
   const float* f = in + static_cast<size_t>(blockIdx.z) * h * w;
   const size_t o = (static_cast<size_t>(blockIdx.z) * h + y) * w + x;
-  gx[o] = 0.5f * (f[static_cast<size_t>(y) * w + reflect101(x + 1, w)] - f[static_cast<size_t>(y) * w + reflect101(x - 1, w)]);
-  gy[o] = 0.5f * (f[static_cast<size_t>(reflect101(y + 1, h)) * w + x] - f[static_cast<size_t>(reflect101(y - 1, h)) * w + x]);
+  const float gx = 0.5f * (f[static_cast<size_t>(y) * w + reflect101(x + 1, w)] - f[static_cast<size_t>(y) * w + reflect101(x - 1, w)]);
+  const float gy = 0.5f * (f[static_cast<size_t>(reflect101(y + 1, h)) * w + x] - f[static_cast<size_t>(reflect101(y - 1, h)) * w + x]);
+  pk[o] = make_float4(f[static_cast<size_t>(y) * w + x], gx, gy, 0.f);
 }
 
 // Bilinear sample with a zero border: a tap outside the image contributes 0.
@@ -225,9 +251,7 @@ __device__ void ecc_step(const double* s, int f, float* warps, double* rho, int*
 // Jacobian J = (x gx, x gy, y gx, y gy, gx, gy) with respect to
 // (m0, m3, m1, m4, m2, m5); the block's 45 sums go to part[frame][block][45].
 constexpr int kEccThreads = 256;
-__global__ void __launch_bounds__(kEccThreads, 2) k_ecc_pass(const float* __restrict__ tmpl, const float* __restrict__ img,
-                                                           const float* __restrict__ gxs, const float* __restrict__ gys,
-                                                           int w, int h, const int* __restrict__ list, float* warps,
+__global__ void __launch_bounds__(kEccThreads, 2) k_ecc_pass(const float4* __restrict__ pk, int w, int h, const int* __restrict__ list, float* warps,
                                                            int* active, float2* part, unsigned int* done, double* rho,
                                                            int* iters, double eps, int max_iter) {
   const int f = list[blockIdx.y];
@@ -236,9 +260,7 @@ __global__ void __launch_bounds__(kEccThreads, 2) k_ecc_pass(const float* __rest
   const float m[6] = {warps[6 * f], warps[6 * f + 1], warps[6 * f + 2],
                       warps[6 * f + 3], warps[6 * f + 4], warps[6 * f + 5]};
   const size_t plane = static_cast<size_t>(w) * h;
-  const float* I = img + f * plane;
-  const float* GX = gxs + f * plane;
-  const float* GY = gys + f * plane;
+  const float4* P = pk + f * plane;  // frame f: (smoothed, d/dx, d/dy, 0) per pixel
   // Every sum is kept as an unevaluated pair hi + lo of FP32 values (FP32
   // pipes only: the FP64 ones are a small fraction of them on this part).
   // The five sums of the correlation coefficient are exact to ~2^-44: the
@@ -264,13 +286,28 @@ __global__ void __launch_bounds__(kEccThreads, 2) k_ecc_pass(const float* __rest
     rl[k] = __fadd_rn(rl[k], __fadd_rn(e, pe));
   };
   const int npix = w * h;
-  for (int p = blockIdx.x * kEccThreads + threadIdx.x; p < npix; p += gridDim.x * kEccThreads) {
-    const int y = p / w, x = p - y * w;
+  const int stride = gridDim.x * kEccThreads, sy = stride / w, sx = stride - sy * w;
+  int p = blockIdx.x * kEccThreads + threadIdx.x, y = p / w, x = p - y * w;
+  for (; p < npix; p += stride, x += sx, y += sy) {
+    if (x >= w) {
+      x -= w;
+      ++y;
+    }
     const float u = m[0] * x + m[1] * y + m[2], v = m[3] * x + m[4] * y + m[5];
     const float fu = floorf(u), fv = floorf(v);
     if (!(fu >= 0.f && fv >= 0.f && fu + 1.f < w && fv + 1.f < h)) continue;  // outside the mask: no terms
-    const float iw = bilinear(I, w, h, u, v), gx = bilinear(GX, w, h, u, v), gy = bilinear(GY, w, h, u, v);
-    const float t = tmpl[p];
+    // all four taps are inside: the zero-border bilinear sample without its checks
+    const int x0 = static_cast<int>(fu), y0 = static_cast<int>(fv);
+    const float ax = u - fu, ay = v - fv;
+    const float4* r0 = P + static_cast<size_t>(y0) * w + x0;
+    const float4 a = r0[0], b = r0[1], c = r0[w], d = r0[w + 1];
+    auto lerp2 = [&](float va, float vb, float vc, float vd) {
+      const float top = va * (1.f - ax) + vb * ax;
+      const float bot = vc * (1.f - ax) + vd * ax;
+      return top * (1.f - ay) + bot * ay;
+    };
+    const float iw = lerp2(a.x, b.x, c.x, d.x), gx = lerp2(a.y, b.y, c.y, d.y), gy = lerp2(a.z, b.z, c.z, d.z);
+    const float t = pk[p].x;
     rn += 1;
     exact_add(0, iw, 1.f);
     exact_add(1, iw, iw);
@@ -440,7 +477,7 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
   const int resident = std::max(1, per_sm) * ctx->sms;
   const int nblocks = std::max(1, std::min(resident, static_cast<int>((plane + kEccThreads - 1) / kEccThreads)));
   const size_t table = static_cast<size_t>(w + h) * 9 * 4;
-  const size_t bytes = all * 2 + 5 * all * 4 + 2 * plane * 4 + plane * 2 + table + F * (24 + 8 + 8 + 4) +
+  const size_t bytes = all * 2 + 3 * all * 4 + all * 16 + 2 * plane * 4 + plane * 2 + table + F * (24 + 8 + 8 + 4) +
                        static_cast<size_t>(F) * nblocks * kSums * 8 + 64;
   char* blk = static_cast<char*>(dev_alloc(ctx, bytes + 32 * 256));  // every take() below pads to 256
   char* q = blk;
@@ -453,8 +490,7 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
   auto* img = reinterpret_cast<float*>(take(all * 4));
   auto* tmp = reinterpret_cast<float*>(take(all * 4));
   auto* blur = reinterpret_cast<float*>(take(all * 4));
-  auto* gx = reinterpret_cast<float*>(take(all * 4));
-  auto* gy = reinterpret_cast<float*>(take(all * 4));
+  auto* pk = reinterpret_cast<float4*>(take(all * 16));
   auto* ze = reinterpret_cast<float*>(take(plane * 4));
   auto* half = reinterpret_cast<float*>(take(plane * 4));
   auto* tab = take(table);
@@ -470,7 +506,8 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
   CUDA_TRY(cudaMemcpyAsync(d16, frames, all * 2, cudaMemcpyHostToDevice, ctx->stream));
   const unsigned int init[3] = {0xffffffffu, 0u, 0u};
   CUDA_TRY(cudaMemcpyAsync(flags, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
-  LCR_LAUNCH(ctx, k_sr_float, static_cast<unsigned>((all + 255) / 256), 256, 0, d16, all, img, flags);
+  LCR_LAUNCH(ctx, k_sr_float, static_cast<unsigned>(std::min<size_t>((all + 255) / 256, 4 * ctx->sms)), 256, 0, d16,
+             all, img, flags);
   // 5x5 Gaussian, sigma 0.3 ((5 - 1) / 2 - 1) + 0.8 = 1.1
   const double sg = 1.1;
   double g[3] = {1.0, std::exp(-1.0 / (2 * sg * sg)), std::exp(-4.0 / (2 * sg * sg))};
@@ -479,7 +516,7 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
   const dim3 gimg((w + 127) / 128, h, F);
   LCR_LAUNCH(ctx, k_sr_blur_h, gimg, 128, 0, img, w, h, g0, g1, g2, tmp);
   LCR_LAUNCH(ctx, k_sr_blur_v, gimg, 128, 0, tmp, w, h, g0, g1, g2, blur);
-  LCR_LAUNCH(ctx, k_sr_grad, gimg, 128, 0, blur, w, h, gx, gy);
+  LCR_LAUNCH(ctx, k_sr_grad, gimg, 128, 0, blur, w, h, pk);
   std::vector<float> hw(6 * F, 0.f);
   for (int f = 0; f < F; ++f) {
     hw[6 * f + 0] = 1.f;
@@ -504,8 +541,8 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
     CUDA_TRY(cudaMemcpyAsync(list, hlist.data(), na * 4, cudaMemcpyHostToDevice, ctx->stream));
     const int todo = std::min(chunk, max_iter - it);
     for (int k = 0; k < todo; ++k, ++it)
-      LCR_LAUNCH(ctx, k_ecc_pass, dim3(nb, na), kEccThreads, 0, blur, blur, gx, gy, w, h, list, warps, active, part,
-                 done, rho, iters, eps, max_iter);
+      LCR_LAUNCH(ctx, k_ecc_pass, dim3(nb, na), kEccThreads, 0, pk, w, h, list, warps, active, part, done, rho, iters,
+                 eps, max_iter);
     CUDA_TRY(cudaMemcpyAsync(hact.data(), active, F * 4, cudaMemcpyDeviceToHost, ctx->stream));
     sync(ctx);
     hlist.clear();

@@ -332,18 +332,42 @@ __global__ void __launch_bounds__(kEccThreads, 2) k_ecc_pass(const float4* __res
       for (int b = a; b < 6; ++b) kadd(q++, J[a] * J[b]);
     }
   }
-  // pairs across the warp (butterflies), then warps in order
+  // The warp's 45 pairs (padded to 48) by a reduce-scatter: at offsets 16, 8,
+  // 4, 2 each lane keeps the half of its values that its lane bit selects and
+  // adds the partner's copy of that half (48 pair additions per lane instead
+  // of 5 x 45 for a butterfly per sum); offset 1 is a butterfly on the last
+  // three.  Lane l then holds sums 24 b4 + 12 b3 + 6 b2 + 3 b1 + 0..2 of the
+  // warp, b the bits of l.
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float2 v[48];
 #pragma unroll
-  for (int k = 0; k < kSums; ++k) {
-    float2 v = k == 0 ? make_float2(static_cast<float>(rn), 0.f)
-             : k <= 5 ? make_float2(rh[k - 1], rl[k - 1]) : make_float2(ks[k - 6], -kc[k - 6]);
+  for (int k = 0; k < 48; ++k)
+    v[k] = k == 0 ? make_float2(static_cast<float>(rn), 0.f)
+         : k <= 5 ? make_float2(rh[k - 1], rl[k - 1])
+         : k < kSums ? make_float2(ks[k - 6], -kc[k - 6]) : make_float2(0.f, 0.f);
+  auto halve = [&](int n, int o) {  // v[0..2n) -> v[0..n)
+    const bool upper = lane & o;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float2 other = make_float2(__shfl_xor_sync(LCR_FULL, v.x, o), __shfl_xor_sync(LCR_FULL, v.y, o));
-      v = pair_add(v, other);
+    for (int j = 0; j < 24; ++j) {
+      if (j < n) {
+        const float2 keep = upper ? v[n + j] : v[j], send = upper ? v[j] : v[n + j];
+        const float2 got = make_float2(__shfl_xor_sync(LCR_FULL, send.x, o), __shfl_xor_sync(LCR_FULL, send.y, o));
+        v[j] = pair_add(keep, got);
+      }
     }
-    if (lane == 0) red[wid][k] = v;
+  };
+  halve(24, 16);
+  halve(12, 8);
+  halve(6, 4);
+  halve(3, 2);
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+    v[j] = pair_add(v[j], make_float2(__shfl_xor_sync(LCR_FULL, v[j].x, 1), __shfl_xor_sync(LCR_FULL, v[j].y, 1)));
+  if (!(lane & 1)) {
+    const int base = (lane & 16 ? 24 : 0) + (lane & 8 ? 12 : 0) + (lane & 4 ? 6 : 0) + (lane & 2 ? 3 : 0);
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (base + j < kSums) red[wid][base + j] = v[j];
   }
   __syncthreads();
   if (threadIdx.x < kSums) {

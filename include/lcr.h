@@ -101,17 +101,22 @@ LCR_API void lcr_cloud_free(lcr_ctx* ctx, lcr_cloud* c);
 LCR_API lcr_status lcr_cloud_concat(lcr_ctx* ctx, const lcr_cloud* a, const lcr_cloud* b, lcr_cloud** out);
 
 /* ------------------------------------------------------- back-projection */
-enum { LCR_DEPTH_KINECT_V1 = 0, LCR_DEPTH_KINECT_V2 = 1 };
+/* Depth models: KINECT_V1 = uint16 mm through the pinhole model of
+ * depth_capture.cpp:294-308; KINECT_V2 = float mm through libfreenect2's
+ * registration (kinect2.h:144-201); PINHOLE_F32 = float mm through the same
+ * pinhole model as V1, as super_resolution_kv2.cpp's save_ply (:25-118) writes
+ * the fused Kinect v2 depth. */
+enum { LCR_DEPTH_KINECT_V1 = 0, LCR_DEPTH_KINECT_V2 = 1, LCR_DEPTH_PINHOLE_F32 = 2 };
 
 typedef struct lcr_depth_params {
-  int model;                 /* LCR_DEPTH_KINECT_V1 (uint16 mm) or LCR_DEPTH_KINECT_V2 (float32 mm) */
+  int model;                 /* LCR_DEPTH_KINECT_V1 (uint16 mm), LCR_DEPTH_KINECT_V2 or LCR_DEPTH_PINHOLE_F32 (float32 mm) */
   int width, height;
   int frames;                /* burst length F >= 1; frames are fused by the zero-eliminated mean */
   double fx, fy, cx, cy;     /* intrinsics */
   double depth_min, depth_max; /* kept depth range in mm, inclusive */
   int roi_left, roi_right, roi_top, roi_bottom; /* kept pixel window, inclusive */
   double scale;              /* output units per mm (1: mm as the reference writes, 0.001: metres) */
-  int normals;               /* V1 only: 1 = image-gradient normals of depth_capture.cpp:231-265 */
+  int normals;               /* pinhole models: 1 = image-gradient normals of depth_capture.cpp:231-265 */
   uint8_t r, g, b, pad;      /* constant colour (super_resolution.cpp:114 writes 128,128,128) */
 } lcr_depth_params;
 
@@ -286,6 +291,11 @@ typedef struct lcr_sr_params {
 } lcr_sr_params;
 LCR_API lcr_status lcr_super_resolve(lcr_ctx* ctx, const uint16_t* frames, const lcr_sr_params* p,
                                      uint16_t* depth_out, float* warps, float minmax[2], int32_t* iterations);
+/* The Kinect v2 form (capture/super_resolution_kv2/super_resolution_kv2.cpp:
+ * 222-311): float frames and a float fused image, not rounded; a pixel that no
+ * frame covers is 0 (the reference leaves it uninitialised). */
+LCR_API lcr_status lcr_super_resolve_f32(lcr_ctx* ctx, const float* frames, const lcr_sr_params* p,
+                                         float* depth_out, float* warps, float minmax[2], int32_t* iterations);
 
 /* ------------------------------------------------------------ autotuning */
 /* Launch shapes of the search kernels.  Every result is independent of them;

@@ -32,7 +32,7 @@ STATUS = {
 OK, INVALID_ARG, EMPTY, NO_CORRESPONDENCES, NOT_CONVERGED = 0, 1, 2, 3, 4
 CUDA_ERR, TIMEOUT, OOM, IO, TOO_FEW_POINTS, NO_DEVICE = 5, 6, 7, 8, 9, 10
 
-KINECT_V1, KINECT_V2 = 0, 1
+KINECT_V1, KINECT_V2, PINHOLE_F32 = 0, 1, 2
 ICP_POINT_TO_POINT, ICP_POINT_TO_PLANE = 0, 1
 (ICP_STATE_NOT_CONVERGED, ICP_STATE_ITERATIONS, ICP_STATE_TRANSFORM, ICP_STATE_ABS_MSE, ICP_STATE_REL_MSE,
  ICP_STATE_NO_CORRESPONDENCES) = range(6)
@@ -144,6 +144,7 @@ _SIGS = {
     "lcr_plane_segment": (C.c_int, [_VP, _VP, C.c_double, C.c_int, C.c_uint64, _VP, C.POINTER(C.c_size_t),
                                     C.POINTER(_VP), C.POINTER(_VP)]),
     "lcr_super_resolve": (C.c_int, [_VP, _VP, C.POINTER(SrParams), _VP, _VP, _VP, _VP]),
+    "lcr_super_resolve_f32": (C.c_int, [_VP, _VP, C.POINTER(SrParams), _VP, _VP, _VP, _VP]),
     "lcr_tune_get": (C.c_int, [_VP, C.POINTER(Tune)]),
     "lcr_tune_set": (C.c_int, [_VP, C.POINTER(Tune)]),
     "lcr_autotune": (C.c_int, [_VP, _VP, _VP, C.c_char_p, C.POINTER(TuneReport)]),

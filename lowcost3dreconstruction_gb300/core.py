@@ -370,14 +370,18 @@ class Context:
     # ------------------------------------------------------ super-resolution
     def super_resolve(self, frames: np.ndarray, factor: int = 4, ecc_iterations: int = 200,
                       ecc_epsilon: float = 1e-12):
-        """lcr_super_resolve: (fused uint16 depth, warps [F][2][3], (min, max), iterations [F])."""
-        frames = np.ascontiguousarray(frames, dtype=np.uint16)
+        """lcr_super_resolve (uint16 frames, Kinect v1) or lcr_super_resolve_f32
+        (float32 frames, Kinect v2): (fused depth of the frames' type, warps
+        [F][2][3], (min, max), iterations [F])."""
+        f32 = np.asarray(frames).dtype == np.float32
+        dt = np.float32 if f32 else np.uint16
+        frames = np.ascontiguousarray(frames, dtype=dt)
         F, h, w = frames.shape
-        out = np.zeros((h, w), dtype=np.uint16)
+        out = np.zeros((h, w), dtype=dt)
         warps = np.zeros((F, 6), dtype=np.float32)
         mm = np.zeros(2, dtype=np.float32)
         it = np.zeros(F, dtype=np.int32)
         p = L.SrParams(w, h, F, factor, ecc_iterations, ecc_epsilon)
-        self._check(self.lib.lcr_super_resolve(self.h, L.ptr(frames), C.byref(p), L.ptr(out), L.ptr(warps),
-                                               L.ptr(mm), L.ptr(it)))
+        fn = self.lib.lcr_super_resolve_f32 if f32 else self.lib.lcr_super_resolve
+        self._check(fn(self.h, L.ptr(frames), C.byref(p), L.ptr(out), L.ptr(warps), L.ptr(mm), L.ptr(it)))
         return out, warps.reshape(F, 2, 3), (float(mm[0]), float(mm[1])), it

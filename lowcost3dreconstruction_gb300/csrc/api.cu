@@ -50,7 +50,8 @@ __global__ void k_invert(const uint8_t* __restrict__ in, size_t n, uint8_t* __re
 
 void check_depth(const lcr_depth_params* p) {
   REQUIRE(p, "null depth parameters");
-  REQUIRE(p->model == LCR_DEPTH_KINECT_V1 || p->model == LCR_DEPTH_KINECT_V2, "unknown depth model %d", p->model);
+  REQUIRE(p->model == LCR_DEPTH_KINECT_V1 || p->model == LCR_DEPTH_KINECT_V2 || p->model == LCR_DEPTH_PINHOLE_F32,
+          "unknown depth model %d", p->model);
   REQUIRE(p->width > 0 && p->height > 0 && static_cast<long long>(p->width) * p->height < (1LL << 31),
           "bad image size %dx%d", p->width, p->height);
   REQUIRE(p->frames >= 1 && p->frames <= 4096, "frames must be in [1, 4096]");
@@ -629,16 +630,33 @@ lcr_status lcr_plane_segment(lcr_ctx* ctx, const lcr_cloud* in, double threshold
   return LCR_OK;
 }
 
-lcr_status lcr_super_resolve(lcr_ctx* ctx, const uint16_t* frames, const lcr_sr_params* p, uint16_t* depth_out,
-                             float* warps, float minmax[2], int32_t* iterations) {
-  API_BEGIN(ctx)
-  REQUIRE(p && frames && depth_out, "null argument");
+namespace {
+void check_sr(const lcr_sr_params* p) {
   REQUIRE(p->width >= 1 && p->height >= 1 && static_cast<long long>(p->width) * p->height <= (1LL << 26),
           "bad image size %dx%d", p->width, p->height);
   REQUIRE(p->frames >= 1 && p->frames <= 1024, "frames must be in [1, 1024]");
   REQUIRE(p->factor >= 1 && p->factor <= 16, "factor must be in [1, 16]");
   REQUIRE(p->ecc_iterations >= 0 && p->ecc_epsilon >= 0, "bad ECC limits");
-  super_resolve_run(ctx, frames, p->width, p->height, p->frames, p->factor, p->ecc_iterations, p->ecc_epsilon,
+}
+}  // namespace
+
+lcr_status lcr_super_resolve(lcr_ctx* ctx, const uint16_t* frames, const lcr_sr_params* p, uint16_t* depth_out,
+                             float* warps, float minmax[2], int32_t* iterations) {
+  API_BEGIN(ctx)
+  REQUIRE(p && frames && depth_out, "null argument");
+  check_sr(p);
+  super_resolve_run(ctx, frames, false, p->width, p->height, p->frames, p->factor, p->ecc_iterations,
+                    p->ecc_epsilon, depth_out, warps, minmax, iterations);
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_super_resolve_f32(lcr_ctx* ctx, const float* frames, const lcr_sr_params* p, float* depth_out,
+                                 float* warps, float minmax[2], int32_t* iterations) {
+  API_BEGIN(ctx)
+  REQUIRE(p && frames && depth_out, "null argument");
+  check_sr(p);
+  super_resolve_run(ctx, frames, true, p->width, p->height, p->frames, p->factor, p->ecc_iterations, p->ecc_epsilon,
                     depth_out, warps, minmax, iterations);
   API_END(ctx)
   return LCR_OK;

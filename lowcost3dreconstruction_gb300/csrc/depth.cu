@@ -52,11 +52,17 @@ __global__ void k_fuse_f32(const float* __restrict__ frames, int F, size_t npix,
   out[p] = cnt ? __double2float_rn(__ddiv_rn(sum, static_cast<double>(cnt))) : 0.f;
 }
 
-__device__ __forceinline__ bool keep_v1(const BP& b, int i, int j, uint16_t z) {
-  return z != 0 && z >= b.dmin && z <= b.dmax && i >= b.top && i <= b.bottom && j >= b.left && j <= b.right;
+// The pinhole models keep a pixel with a depth in [dmin, dmax] inside the
+// window: uint16 depth (Kinect v1, depth_capture.cpp, super_resolution.cpp
+// save_ply) or float depth (super_resolution_kv2.cpp save_ply :25-118).
+template <typename T>
+__device__ __forceinline__ bool keep_v1(const BP& b, int i, int j, T z) {
+  return z != 0 && static_cast<double>(z) >= b.dmin && static_cast<double>(z) <= b.dmax && i >= b.top &&
+         i <= b.bottom && j >= b.left && j <= b.right;
 }
 
-__global__ void k_flags_v1(const uint16_t* __restrict__ depth, BP b, uint8_t* __restrict__ flags) {
+template <typename T>
+__global__ void k_flags_v1(const T* __restrict__ depth, BP b, uint8_t* __restrict__ flags) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= b.w * b.h) return;
   const int i = p / b.w, j = p - i * b.w;
@@ -89,18 +95,47 @@ __device__ __forceinline__ float3 image_normal(const uint16_t* __restrict__ d, i
                      __double2float_rn(__dmul_rn(d2, inv)));
 }
 
+// super_resolution_kv2.cpp:33-62, the same rule on float depth: the
+// differences and the threshold test are FP32, the slopes FP64.
+__device__ __forceinline__ float3 image_normal(const float* __restrict__ d, int w, int h, int i, int j) {
+  const float c = d[static_cast<size_t>(i) * w + j];
+  float right = 0.f, left = 0.f, down = 0.f, up = 0.f;
+  if (i > 0 && j > 0 && i < h - 1 && j < w - 1) {
+    right = d[static_cast<size_t>(i + 1) * w + j];
+    left = d[static_cast<size_t>(i - 1) * w + j];
+    down = d[static_cast<size_t>(i) * w + j + 1];
+    up = d[static_cast<size_t>(i) * w + j - 1];
+  }
+  if (fabsf(__fsub_rn(c, right)) > 20.f) right = 0.f;
+  if (fabsf(__fsub_rn(c, left)) > 20.f) left = 0.f;
+  if (fabsf(__fsub_rn(c, down)) > 20.f) down = 0.f;
+  if (fabsf(__fsub_rn(c, up)) > 20.f) up = 0.f;
+  const double dzdx = __ddiv_rn(static_cast<double>(__fsub_rn(right, left)), 2.0);
+  const double dzdy = __ddiv_rn(static_cast<double>(__fsub_rn(down, up)), 2.0);
+  const double d0 = -dzdx, d1 = -dzdy, d2 = 1.0;
+  double s = __dmul_rn(d0, d0);
+  s = __dadd_rn(s, __dmul_rn(d1, d1));
+  s = __dadd_rn(s, __dmul_rn(d2, d2));
+  const double nv = __dsqrt_rn(s);
+  const double inv = nv != 0.0 ? __ddiv_rn(1.0, nv) : 0.0;
+  return make_float3(__double2float_rn(__dmul_rn(d0, inv)), __double2float_rn(__dmul_rn(d1, inv)),
+                     __double2float_rn(__dmul_rn(d2, inv)));
+}
+
 // depth_capture.cpp:294-308: x = z*(j-cx)*(1/fx), y = -z*(i-cy)*(1/fy), z' = -z in
-// double, times `scale`, rounded once to float.
-__global__ void k_emit_v1(const uint16_t* __restrict__ depth, BP b, const uint32_t* __restrict__ idx, int n,
+// double, times `scale`, rounded once to float (the same for float depth,
+// super_resolution_kv2.cpp:96-106).
+template <typename T>
+__global__ void k_emit_v1(const T* __restrict__ depth, BP b, const uint32_t* __restrict__ idx, int n,
                           float4* __restrict__ xyz, float4* __restrict__ nrm, uint32_t* __restrict__ rgb) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const int p = static_cast<int>(idx[k]);
   const int i = p / b.w, j = p - i * b.w;
-  const int z = depth[p];
-  const double vx = __dmul_rn(__dmul_rn(static_cast<double>(z), __dsub_rn(static_cast<double>(j), b.cx)), b.ifx);
-  const double vy = __dmul_rn(__dmul_rn(static_cast<double>(-z), __dsub_rn(static_cast<double>(i), b.cy)), b.ify);
-  const double vz = static_cast<double>(-z);
+  const double z = static_cast<double>(depth[p]);
+  const double vx = __dmul_rn(__dmul_rn(z, __dsub_rn(static_cast<double>(j), b.cx)), b.ifx);
+  const double vy = __dmul_rn(__dmul_rn(-z, __dsub_rn(static_cast<double>(i), b.cy)), b.ify);
+  const double vz = -z;
   xyz[k] = make_float4(__double2float_rn(__dmul_rn(vx, b.scale)), __double2float_rn(__dmul_rn(vy, b.scale)),
                        __double2float_rn(__dmul_rn(vz, b.scale)), 0.f);
   float3 nn = make_float3(0.f, 0.f, 0.f);
@@ -209,18 +244,23 @@ int backproject_run(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p
   uint32_t* idx = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * npix));
   const unsigned grid = (npix + 255) / 256;
   if (p->model == LCR_DEPTH_KINECT_V1)
-    LCR_LAUNCH(ctx, k_flags_v1, grid, 256, 0, static_cast<const uint16_t*>(depth), b, flags);
+    LCR_LAUNCH(ctx, k_flags_v1<uint16_t>, grid, 256, 0, static_cast<const uint16_t*>(depth), b, flags);
+  else if (p->model == LCR_DEPTH_PINHOLE_F32)
+    LCR_LAUNCH(ctx, k_flags_v1<float>, grid, 256, 0, static_cast<const float*>(depth), b, flags);
   else
     LCR_LAUNCH(ctx, k_flags_v2, grid, 256, 0, static_cast<const float*>(depth), b, flags);
   const int n = compact_flags(ctx, flags, npix, idx);
   lcr_cloud* c = cloud_alloc(ctx, n);
   if (n > 0) {
+    const unsigned eg = (n + 255) / 256;
     if (p->model == LCR_DEPTH_KINECT_V1)
-      LCR_LAUNCH(ctx, k_emit_v1, (n + 255) / 256, 256, 0, static_cast<const uint16_t*>(depth), b, idx, n, c->xyz,
-                 c->nrm, c->rgb);
+      LCR_LAUNCH(ctx, k_emit_v1<uint16_t>, eg, 256, 0, static_cast<const uint16_t*>(depth), b, idx, n, c->xyz, c->nrm,
+                 c->rgb);
+    else if (p->model == LCR_DEPTH_PINHOLE_F32)
+      LCR_LAUNCH(ctx, k_emit_v1<float>, eg, 256, 0, static_cast<const float*>(depth), b, idx, n, c->xyz, c->nrm,
+                 c->rgb);
     else
-      LCR_LAUNCH(ctx, k_emit_v2, (n + 255) / 256, 256, 0, static_cast<const float*>(depth), b, idx, n, c->xyz,
-                 c->nrm, c->rgb);
+      LCR_LAUNCH(ctx, k_emit_v2, eg, 256, 0, static_cast<const float*>(depth), b, idx, n, c->xyz, c->nrm, c->rgb);
   }
   dev_free(ctx, flags);
   dev_free(ctx, idx);
@@ -262,30 +302,37 @@ unsigned char* into_scratch(int device) {
   return static_cast<unsigned char*>(g_into_addr[device]);
 }
 
-// Kept pixel test of one pixel, and its record, for either camera model.
-template <int V1>
+// Kept pixel test of one pixel, and its record, for each camera model M
+// (LCR_DEPTH_KINECT_V1, LCR_DEPTH_KINECT_V2, LCR_DEPTH_PINHOLE_F32).
+template <int M>
 __device__ __forceinline__ bool into_keep(const void* depth, const BP& b, int p) {
   const int i = p / b.w, j = p - i * b.w;
-  if (V1) return keep_v1(b, i, j, static_cast<const uint16_t*>(depth)[p]);
+  if (M == LCR_DEPTH_KINECT_V1) return keep_v1(b, i, j, static_cast<const uint16_t*>(depth)[p]);
+  if (M == LCR_DEPTH_PINHOLE_F32) return keep_v1(b, i, j, static_cast<const float*>(depth)[p]);
   float3 q;
   return point_v2(b, static_cast<const float*>(depth), i, j, q);
 }
 
-template <int V1>
+template <int M>
 __device__ __forceinline__ void into_record(const void* depth, const BP& b, int p, float4* __restrict__ rec) {
   const int i = p / b.w, j = p - i * b.w;
   float4 xyz;
   float3 nn = make_float3(0.f, 0.f, 0.f);
-  if (V1) {
+  if (M != LCR_DEPTH_KINECT_V2) {
     // depth_capture.cpp:294-308, as k_emit_v1
-    const uint16_t* d = static_cast<const uint16_t*>(depth);
-    const int z = d[p];
-    const double vx = __dmul_rn(__dmul_rn(static_cast<double>(z), __dsub_rn(static_cast<double>(j), b.cx)), b.ifx);
-    const double vy = __dmul_rn(__dmul_rn(static_cast<double>(-z), __dsub_rn(static_cast<double>(i), b.cy)), b.ify);
-    const double vz = static_cast<double>(-z);
+    const double z = M == LCR_DEPTH_KINECT_V1 ? static_cast<double>(static_cast<const uint16_t*>(depth)[p])
+                                              : static_cast<double>(static_cast<const float*>(depth)[p]);
+    const double vx = __dmul_rn(__dmul_rn(z, __dsub_rn(static_cast<double>(j), b.cx)), b.ifx);
+    const double vy = __dmul_rn(__dmul_rn(-z, __dsub_rn(static_cast<double>(i), b.cy)), b.ify);
+    const double vz = -z;
     xyz = make_float4(__double2float_rn(__dmul_rn(vx, b.scale)), __double2float_rn(__dmul_rn(vy, b.scale)),
                       __double2float_rn(__dmul_rn(vz, b.scale)), 1.f);
-    if (b.normals) nn = image_normal(d, b.w, b.h, i, j);
+    if (b.normals) {
+      if (M == LCR_DEPTH_KINECT_V1)
+        nn = image_normal(static_cast<const uint16_t*>(depth), b.w, b.h, i, j);
+      else
+        nn = image_normal(static_cast<const float*>(depth), b.w, b.h, i, j);
+    }
   } else {
     float3 q = make_float3(0.f, 0.f, 0.f);
     point_v2(b, static_cast<const float*>(depth), i, j, q);
@@ -297,10 +344,10 @@ __device__ __forceinline__ void into_record(const void* depth, const BP& b, int 
   rec[2] = make_float4(__uint_as_float(b.rgb), 0.f, 0.f, 0.f);
 }
 
-template <int V1>
+template <int M>
 __global__ void __launch_bounds__(kIntoBlock) k_into_count(const void* depth, BP b, uint32_t* __restrict__ counts) {
   const int p = blockIdx.x * kIntoBlock + threadIdx.x;
-  const bool k = p < b.w * b.h && into_keep<V1>(depth, b, p);
+  const bool k = p < b.w * b.h && into_keep<M>(depth, b, p);
   const int c = __syncthreads_count(k);
   if (threadIdx.x == 0) counts[blockIdx.x] = static_cast<uint32_t>(c);
 }
@@ -336,13 +383,13 @@ __global__ void __launch_bounds__(1024) k_into_scan(uint32_t* __restrict__ count
 
 // Each block recomputes its pixels' keep flags, ranks them in pixel order and
 // writes their records from its scanned offset; nothing past `capacity`.
-template <int V1>
+template <int M>
 __global__ void __launch_bounds__(kIntoBlock) k_into_emit(const void* depth, BP b, const uint32_t* __restrict__ offs,
                                                           float4* __restrict__ rec, size_t capacity) {
   __shared__ uint32_t s_w[kIntoBlock / 32];
   const int p = blockIdx.x * kIntoBlock + threadIdx.x;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const bool k = p < b.w * b.h && into_keep<V1>(depth, b, p);
+  const bool k = p < b.w * b.h && into_keep<M>(depth, b, p);
   const unsigned m = __ballot_sync(LCR_FULL, k);
   if (lane == 0) s_w[w] = __popc(m);
   __syncthreads();
@@ -350,7 +397,7 @@ __global__ void __launch_bounds__(kIntoBlock) k_into_emit(const void* depth, BP 
   for (int j = 0; j < w; ++j) before += s_w[j];
   if (!k) return;
   const size_t pos = static_cast<size_t>(offs[blockIdx.x]) + before + __popc(m & ((1u << lane) - 1u));
-  if (pos < capacity) into_record<V1>(depth, b, p, rec + 3 * pos);
+  if (pos < capacity) into_record<M>(depth, b, p, rec + 3 * pos);
 }
 
 }  // namespace
@@ -373,12 +420,16 @@ void backproject_into_run(lcr_ctx* ctx, const void* d_depth, const lcr_depth_par
   const int nblk = static_cast<int>((npix + kIntoBlock - 1) / kIntoBlock);
   float4* rec = reinterpret_cast<float4*>(d_points);
   if (p->model == LCR_DEPTH_KINECT_V1) {
-    LCR_LAUNCH(ctx, k_into_count<1>, nblk, kIntoBlock, 0, depth, b, counts);
+    LCR_LAUNCH(ctx, k_into_count<LCR_DEPTH_KINECT_V1>, nblk, kIntoBlock, 0, depth, b, counts);
     LCR_LAUNCH(ctx, k_into_scan, 1, 1024, 0, counts, nblk, d_count);
-    LCR_LAUNCH(ctx, k_into_emit<1>, nblk, kIntoBlock, 0, depth, b, counts, rec, capacity);
+    LCR_LAUNCH(ctx, k_into_emit<LCR_DEPTH_KINECT_V1>, nblk, kIntoBlock, 0, depth, b, counts, rec, capacity);
+  } else if (p->model == LCR_DEPTH_PINHOLE_F32) {
+    LCR_LAUNCH(ctx, k_into_count<LCR_DEPTH_PINHOLE_F32>, nblk, kIntoBlock, 0, depth, b, counts);
+    LCR_LAUNCH(ctx, k_into_scan, 1, 1024, 0, counts, nblk, d_count);
+    LCR_LAUNCH(ctx, k_into_emit<LCR_DEPTH_PINHOLE_F32>, nblk, kIntoBlock, 0, depth, b, counts, rec, capacity);
   } else {
-    LCR_LAUNCH(ctx, k_into_count<0>, nblk, kIntoBlock, 0, depth, b, counts);
+    LCR_LAUNCH(ctx, k_into_count<LCR_DEPTH_KINECT_V2>, nblk, kIntoBlock, 0, depth, b, counts);
     LCR_LAUNCH(ctx, k_into_scan, 1, 1024, 0, counts, nblk, d_count);
-    LCR_LAUNCH(ctx, k_into_emit<0>, nblk, kIntoBlock, 0, depth, b, counts, rec, capacity);
+    LCR_LAUNCH(ctx, k_into_emit<LCR_DEPTH_KINECT_V2>, nblk, kIntoBlock, 0, depth, b, counts, rec, capacity);
   }
 }

@@ -1,4 +1,4 @@
-// PNG codec for grayscale depth images (see png16.h).
+// PNG codec for depth images (see png16.h).
 #include "png16.h"
 
 #include <zlib.h>
@@ -39,7 +39,12 @@ int paeth(int a, int b, int c) {
 
 }  // namespace
 
-bool read(const std::string& path, std::vector<uint16_t>& pixels, int& width, int& height, std::string& err) {
+namespace {
+
+// The unfiltered image bytes of path (height rows of width * channels *
+// depth / 8 bytes) and its header; false with a message in err.
+bool decode(const std::string& path, std::vector<unsigned char>& img, int& width, int& height, int& depth,
+            int& ctype, std::string& err) {
   FILE* f = std::fopen(path.c_str(), "rb");
   if (!f) {
     err = "cannot open " + path;
@@ -55,7 +60,9 @@ bool read(const std::string& path, std::vector<uint16_t>& pixels, int& width, in
     return false;
   }
   size_t p = 8;
-  int depth = 0, ctype = -1, interlace = 0;
+  int interlace = 0;
+  depth = 0;
+  ctype = -1;
   std::vector<unsigned char> idat;
   bool have_hdr = false, ended = false;
   while (p + 12 <= buf.size() && !ended) {
@@ -85,26 +92,28 @@ bool read(const std::string& path, std::vector<uint16_t>& pixels, int& width, in
     err = path + ": truncated PNG";
     return false;
   }
-  if (ctype != 0 || (depth != 8 && depth != 16) || interlace != 0 || width <= 0 || height <= 0 ||
+  const int channels = ctype == 0 ? 1 : ctype == 6 ? 4 : 0;
+  if (channels == 0 || (depth != 8 && depth != 16) || interlace != 0 || width <= 0 || height <= 0 ||
       static_cast<long long>(width) * height > (1LL << 28)) {
-    err = path + ": only non-interlaced 8- or 16-bit grayscale PNG is supported";
+    err = path + ": only non-interlaced 8- or 16-bit grayscale or RGBA PNG is supported";
     return false;
   }
-  const size_t bpp = depth / 8, stride = static_cast<size_t>(width) * bpp;
+  const size_t bpp = static_cast<size_t>(channels) * depth / 8, stride = static_cast<size_t>(width) * bpp;
   std::vector<unsigned char> raw((stride + 1) * height);
   uLongf rawlen = static_cast<uLongf>(raw.size());
   if (uncompress(raw.data(), &rawlen, idat.data(), static_cast<uLong>(idat.size())) != Z_OK || rawlen != raw.size()) {
     err = path + ": corrupt image data";
     return false;
   }
-  std::vector<unsigned char> prev(stride, 0), cur(stride);
-  pixels.resize(static_cast<size_t>(width) * height);
+  img.assign(stride * height, 0);
   for (int y = 0; y < height; ++y) {
     const unsigned char* row = &raw[y * (stride + 1)];
+    const unsigned char* prev = y > 0 ? &img[(y - 1) * stride] : nullptr;
+    unsigned char* cur = &img[y * stride];
     const int filter = row[0];
     for (size_t i = 0; i < stride; ++i) {
       const int x = row[1 + i];
-      const int a = i >= bpp ? cur[i - bpp] : 0, b = prev[i], c = i >= bpp ? prev[i - bpp] : 0;
+      const int a = i >= bpp ? cur[i - bpp] : 0, b = prev ? prev[i] : 0, c = prev && i >= bpp ? prev[i - bpp] : 0;
       int v;
       switch (filter) {
         case 0: v = x; break;
@@ -118,25 +127,17 @@ bool read(const std::string& path, std::vector<uint16_t>& pixels, int& width, in
       }
       cur[i] = static_cast<unsigned char>(v & 255);
     }
-    for (int x = 0; x < width; ++x)
-      pixels[static_cast<size_t>(y) * width + x] =
-          bpp == 2 ? static_cast<uint16_t>((cur[2 * x] << 8) | cur[2 * x + 1]) : cur[x];
-    prev.swap(cur);
   }
   return true;
 }
 
-bool write(const std::string& path, const uint16_t* pixels, int width, int height, std::string& err) {
-  const size_t stride = static_cast<size_t>(width) * 2;
+// Writes rows of stride bytes with filter None under the given header.
+bool encode(const std::string& path, const unsigned char* img, size_t stride, int width, int height, int depth,
+            int ctype, std::string& err) {
   std::vector<unsigned char> raw((stride + 1) * height);
   for (int y = 0; y < height; ++y) {
-    unsigned char* row = &raw[y * (stride + 1)];
-    row[0] = 0;
-    for (int x = 0; x < width; ++x) {
-      const uint16_t v = pixels[static_cast<size_t>(y) * width + x];
-      row[1 + 2 * x] = static_cast<unsigned char>(v >> 8);
-      row[2 + 2 * x] = static_cast<unsigned char>(v & 255);
-    }
+    raw[y * (stride + 1)] = 0;
+    std::memcpy(&raw[y * (stride + 1) + 1], img + y * stride, stride);
   }
   uLongf zlen = compressBound(static_cast<uLong>(raw.size()));
   std::vector<unsigned char> z(zlen);
@@ -145,14 +146,12 @@ bool write(const std::string& path, const uint16_t* pixels, int width, int heigh
     return false;
   }
   std::vector<unsigned char> out(kSig, kSig + 8);
-  unsigned char hdr[13];
   const uint32_t w = static_cast<uint32_t>(width), h = static_cast<uint32_t>(height);
-  const unsigned char ih[13] = {static_cast<unsigned char>(w >> 24), static_cast<unsigned char>(w >> 16),
-                                static_cast<unsigned char>(w >> 8),  static_cast<unsigned char>(w),
-                                static_cast<unsigned char>(h >> 24), static_cast<unsigned char>(h >> 16),
-                                static_cast<unsigned char>(h >> 8),  static_cast<unsigned char>(h),
-                                16, 0, 0, 0, 0};
-  std::memcpy(hdr, ih, 13);
+  const unsigned char hdr[13] = {static_cast<unsigned char>(w >> 24), static_cast<unsigned char>(w >> 16),
+                                 static_cast<unsigned char>(w >> 8),  static_cast<unsigned char>(w),
+                                 static_cast<unsigned char>(h >> 24), static_cast<unsigned char>(h >> 16),
+                                 static_cast<unsigned char>(h >> 8),  static_cast<unsigned char>(h),
+                                 static_cast<unsigned char>(depth), static_cast<unsigned char>(ctype), 0, 0, 0};
   chunk(out, "IHDR", hdr, 13);
   chunk(out, "IDAT", z.data(), zlen);
   chunk(out, "IEND", nullptr, 0);
@@ -163,6 +162,48 @@ bool write(const std::string& path, const uint16_t* pixels, int width, int heigh
   }
   const bool ok = std::fwrite(out.data(), 1, out.size(), f) == out.size();
   return (std::fclose(f) == 0) && ok ? true : (err = "write failed: " + path, false);
+}
+
+}  // namespace
+
+bool read(const std::string& path, std::vector<uint16_t>& pixels, int& width, int& height, std::string& err) {
+  std::vector<unsigned char> img;
+  int depth = 0, ctype = 0;
+  if (!decode(path, img, width, height, depth, ctype, err)) return false;
+  if (ctype != 0) {
+    err = path + ": not a grayscale PNG";
+    return false;
+  }
+  const size_t n = static_cast<size_t>(width) * height;
+  pixels.resize(n);
+  for (size_t i = 0; i < n; ++i)
+    pixels[i] = depth == 16 ? static_cast<uint16_t>((img[2 * i] << 8) | img[2 * i + 1]) : img[i];
+  return true;
+}
+
+bool read_rgba8(const std::string& path, std::vector<unsigned char>& rgba, int& width, int& height,
+                std::string& err) {
+  int depth = 0, ctype = 0;
+  if (!decode(path, rgba, width, height, depth, ctype, err)) return false;
+  if (ctype != 6 || depth != 8) {
+    err = path + ": not an 8-bit RGBA PNG";
+    return false;
+  }
+  return true;
+}
+
+bool write_rgba8(const std::string& path, const unsigned char* rgba, int width, int height, std::string& err) {
+  return encode(path, rgba, static_cast<size_t>(width) * 4, width, height, 8, 6, err);
+}
+
+bool write(const std::string& path, const uint16_t* pixels, int width, int height, std::string& err) {
+  const size_t n = static_cast<size_t>(width) * height;
+  std::vector<unsigned char> img(2 * n);
+  for (size_t i = 0; i < n; ++i) {
+    img[2 * i] = static_cast<unsigned char>(pixels[i] >> 8);
+    img[2 * i + 1] = static_cast<unsigned char>(pixels[i] & 255);
+  }
+  return encode(path, img.data(), static_cast<size_t>(width) * 2, width, height, 16, 0, err);
 }
 
 }  // namespace png16

@@ -264,8 +264,9 @@ void euclidean_clusters_run(lcr_ctx* ctx, const lcr_cloud* in, double tolerance,
 void plane_segment_run(lcr_ctx* ctx, const lcr_cloud* in, double threshold, int hypotheses, uint64_t seed,
                        float coefficients[4], size_t* ninliers, lcr_cloud** plane, lcr_cloud** rest);
 // Super-resolution front end (sr.cu).
-void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F, int factor, int max_iter,
-                       double eps, uint16_t* out, float* warps_out, float minmax_out[2], int* iters_out);
+// frames and out are uint16 (Kinect v1) or, with f32, float (Kinect v2).
+void super_resolve_run(lcr_ctx* ctx, const void* frames, bool f32, int w, int h, int F, int factor, int max_iter,
+                       double eps, void* out, float* warps_out, float minmax_out[2], int* iters_out);
 // Launch-shape tuning (tune.cu).
 void tune_apply(lcr_ctx* ctx, const lcr_tune& t);
 lcr_tune tune_current(const lcr_ctx* ctx);

@@ -24,6 +24,7 @@
 // (reflect-101); the Lanczos taps clamp to the image.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "lcr_internal.cuh"
@@ -38,19 +39,24 @@ __device__ __forceinline__ int reflect101(int i, int n) {
   return i;
 }
 
-// uint16 frames to float, and the range of the positive values: per-thread
-// over a grid-stride loop, then warp and block reductions, one atomic pair
-// per block (a pair per warp contends on the two words).
-__global__ void k_sr_float(const uint16_t* __restrict__ in, size_t n, float* __restrict__ out,
+// Frames to float, and the range of the positive values (as their bit
+// patterns, which order positive floats as their values): per-thread over a
+// grid-stride loop, then warp and block reductions, one atomic pair per block
+// (a pair per warp contends on the two words).
+__device__ __forceinline__ unsigned range_key(uint16_t v) { return v; }
+__device__ __forceinline__ unsigned range_key(float v) { return __float_as_uint(v); }
+
+template <typename T>
+__global__ void k_sr_float(const T* __restrict__ in, size_t n, float* __restrict__ out,
                            unsigned int* __restrict__ minmax) {
   unsigned lo = 0xffffffffu, hi = 0u;
   for (size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
        i += static_cast<size_t>(gridDim.x) * blockDim.x) {
-    const unsigned v = in[i];
+    const T v = in[i];
     out[i] = static_cast<float>(v);
     if (v > 0) {
-      lo = min(lo, v);
-      hi = max(hi, v);
+      lo = min(lo, range_key(v));
+      hi = max(hi, range_key(v));
     }
   }
   lo = __reduce_min_sync(LCR_FULL, lo);
@@ -414,9 +420,12 @@ __global__ void __launch_bounds__(kEccThreads, 2) k_ecc_pass(const float4* __res
 // it, so the high-resolution image is never formed): ze(y, x) is the mean of
 // the positive values among frame 0 at (x, y) and frames k >= 1 sampled at
 // W_k(x, y) (the inverse-map bilinear warp, zero outside); FP64 sum in frame
-// order divided by the count, to float; 0/0 = NaN.
+// order divided by the count, to float; a pixel with no positive value is
+// 0/0 = NaN (super_resolution.cpp's mean of an empty vector) or, with
+// empty_zero, 0 (super_resolution_kv2.cpp:298 skips it; its output buffer is
+// uninitialised there, and 0 stands for that).
 __global__ void k_sr_fuse(const float* __restrict__ in, int w, int h, int F, const float* __restrict__ warps,
-                          float* __restrict__ ze) {
+                          int empty_zero, float* __restrict__ ze) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
   if (x >= w) return;
   const size_t plane = static_cast<size_t>(w) * h, o = static_cast<size_t>(y) * w + x;
@@ -430,7 +439,7 @@ __global__ void k_sr_fuse(const float* __restrict__ in, int w, int h, int F, con
       ++cnt;
     }
   }
-  ze[o] = static_cast<float>(sum / cnt);
+  ze[o] = cnt == 0 && empty_zero ? 0.f : static_cast<float>(sum / cnt);
 }
 
 // Lanczos-4 resampling of the upsampled image by 1/s, one axis per pass:
@@ -449,19 +458,26 @@ __global__ void k_sr_lanczos_h(const float* __restrict__ ze, int w, int s, const
   half[static_cast<size_t>(y) * w + x] = acc;
 }
 
-// The vertical pass, rounded half to even and saturated to uint16 (NaN -> 0).
+// The vertical pass; uint16 output is rounded half to even and saturated
+// (NaN -> 0), float output is the value itself.
+__device__ __forceinline__ void store_depth(uint16_t* out, float v) {
+  float r = rintf(v);
+  if (!(r > 0.f)) r = 0.f;
+  if (r > 65535.f) r = 65535.f;
+  *out = static_cast<uint16_t>(r);
+}
+__device__ __forceinline__ void store_depth(float* out, float v) { *out = v; }
+
+template <typename T>
 __global__ void k_sr_lanczos_v(const float* __restrict__ half, int w, int h, int s, const int* __restrict__ base,
-                               const float* __restrict__ wgt, uint16_t* __restrict__ out) {
+                               const float* __restrict__ wgt, T* __restrict__ out) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
   if (x >= w) return;
   const int H = h * s;
   float acc = 0.f;
 #pragma unroll
   for (int i = 0; i < 8; ++i) acc += wgt[8 * y + i] * half[static_cast<size_t>(min(max(base[y] + i, 0), H - 1) / s) * w + x];
-  float r = rintf(acc);
-  if (!(r > 0.f)) r = 0.f;
-  if (r > 65535.f) r = 65535.f;
-  out[static_cast<size_t>(y) * w + x] = static_cast<uint16_t>(r);
+  store_depth(out + static_cast<size_t>(y) * w + x, acc);
 }
 
 // Lanczos (a = 4) taps of output o = 0 .. n - 1 of a resampling by 1/s: the
@@ -490,8 +506,9 @@ void lanczos_table(int n, int s, int* base, float* wgt) {
 
 }  // namespace
 
-void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F, int factor, int max_iter,
-                       double eps, uint16_t* out, float* warps_out, float minmax_out[2], int* iters_out) {
+void super_resolve_run(lcr_ctx* ctx, const void* frames, bool f32, int w, int h, int F, int factor, int max_iter,
+                       double eps, void* out, float* warps_out, float minmax_out[2], int* iters_out) {
+  const size_t esz = f32 ? 4 : 2;
   const size_t plane = static_cast<size_t>(w) * h, all = plane * F;
   // The pass runs one wave of resident blocks, shared among the frames still
   // iterating (the others return at once): many pixels per thread while all
@@ -501,7 +518,7 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
   const int resident = std::max(1, per_sm) * ctx->sms;
   const int nblocks = std::max(1, std::min(resident, static_cast<int>((plane + kEccThreads - 1) / kEccThreads)));
   const size_t table = static_cast<size_t>(w + h) * 9 * 4;
-  const size_t bytes = all * 2 + 3 * all * 4 + all * 16 + 2 * plane * 4 + plane * 2 + table + F * (24 + 8 + 8 + 4) +
+  const size_t bytes = all * 4 + 3 * all * 4 + all * 16 + 2 * plane * 4 + plane * 4 + table + F * (24 + 8 + 8 + 4) +
                        static_cast<size_t>(F) * nblocks * kSums * 8 + 64;
   char* blk = static_cast<char*>(dev_alloc(ctx, bytes + 32 * 256));  // every take() below pads to 256
   char* q = blk;
@@ -510,7 +527,7 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
     q += (b + 255) & ~static_cast<size_t>(255);
     return r;
   };
-  auto* d16 = reinterpret_cast<uint16_t*>(take(all * 2));
+  void* din = take(all * esz);
   auto* img = reinterpret_cast<float*>(take(all * 4));
   auto* tmp = reinterpret_cast<float*>(take(all * 4));
   auto* blur = reinterpret_cast<float*>(take(all * 4));
@@ -518,7 +535,7 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
   auto* ze = reinterpret_cast<float*>(take(plane * 4));
   auto* half = reinterpret_cast<float*>(take(plane * 4));
   auto* tab = take(table);
-  auto* o16 = reinterpret_cast<uint16_t*>(take(plane * 2));
+  void* dout = take(plane * esz);
   auto* warps = reinterpret_cast<float*>(take(F * 24));
   auto* rho = reinterpret_cast<double*>(take(F * 8));
   auto* active = reinterpret_cast<int*>(take(F * 4));
@@ -527,11 +544,14 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
   auto* list = reinterpret_cast<int*>(take(F * 4));
   auto* part = reinterpret_cast<float2*>(take(static_cast<size_t>(F) * nblocks * kSums * 8));
   auto* flags = reinterpret_cast<unsigned int*>(take(64));
-  CUDA_TRY(cudaMemcpyAsync(d16, frames, all * 2, cudaMemcpyHostToDevice, ctx->stream));
+  CUDA_TRY(cudaMemcpyAsync(din, frames, all * esz, cudaMemcpyHostToDevice, ctx->stream));
   const unsigned int init[3] = {0xffffffffu, 0u, 0u};
   CUDA_TRY(cudaMemcpyAsync(flags, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
-  LCR_LAUNCH(ctx, k_sr_float, static_cast<unsigned>(std::min<size_t>((all + 255) / 256, 4 * ctx->sms)), 256, 0, d16,
-             all, img, flags);
+  const unsigned gconv = static_cast<unsigned>(std::min<size_t>((all + 255) / 256, 4 * ctx->sms));
+  if (f32)
+    LCR_LAUNCH(ctx, k_sr_float<float>, gconv, 256, 0, static_cast<const float*>(din), all, img, flags);
+  else
+    LCR_LAUNCH(ctx, k_sr_float<uint16_t>, gconv, 256, 0, static_cast<const uint16_t*>(din), all, img, flags);
   // 5x5 Gaussian, sigma 0.3 ((5 - 1) / 2 - 1) + 0.8 = 1.1
   const double sg = 1.1;
   double g[3] = {1.0, std::exp(-1.0 / (2 * sg * sg)), std::exp(-4.0 / (2 * sg * sg))};
@@ -586,18 +606,28 @@ void super_resolve_run(lcr_ctx* ctx, const uint16_t* frames, int w, int h, int F
   const auto* dxw = reinterpret_cast<const float*>(dybase + h);
   const auto* dyw = dxw + 8 * w;
   const dim3 grow((w + 127) / 128, h);
-  LCR_LAUNCH(ctx, k_sr_fuse, grow, 128, 0, img, w, h, F, warps, ze);
+  LCR_LAUNCH(ctx, k_sr_fuse, grow, 128, 0, img, w, h, F, warps, f32 ? 1 : 0, ze);
   LCR_LAUNCH(ctx, k_sr_lanczos_h, grow, 128, 0, ze, w, factor, dxbase, dxw, half);
-  LCR_LAUNCH(ctx, k_sr_lanczos_v, grow, 128, 0, half, w, h, factor, dybase, dyw, o16);
-  CUDA_TRY(cudaMemcpyAsync(out, o16, plane * 2, cudaMemcpyDeviceToHost, ctx->stream));
+  if (f32)
+    LCR_LAUNCH(ctx, k_sr_lanczos_v<float>, grow, 128, 0, half, w, h, factor, dybase, dyw, static_cast<float*>(dout));
+  else
+    LCR_LAUNCH(ctx, k_sr_lanczos_v<uint16_t>, grow, 128, 0, half, w, h, factor, dybase, dyw,
+               static_cast<uint16_t*>(dout));
+  CUDA_TRY(cudaMemcpyAsync(out, dout, plane * esz, cudaMemcpyDeviceToHost, ctx->stream));
   if (warps_out) CUDA_TRY(cudaMemcpyAsync(warps_out, warps, F * 24, cudaMemcpyDeviceToHost, ctx->stream));
   if (iters_out) CUDA_TRY(cudaMemcpyAsync(iters_out, iters, F * 4, cudaMemcpyDeviceToHost, ctx->stream));
   unsigned int mm[2];
   CUDA_TRY(cudaMemcpyAsync(mm, flags, 8, cudaMemcpyDeviceToHost, ctx->stream));
   sync(ctx);
   if (minmax_out) {
-    minmax_out[0] = mm[1] ? static_cast<float>(mm[0]) : 0.f;
-    minmax_out[1] = static_cast<float>(mm[1]);
+    auto value = [&](unsigned k) {
+      if (!f32) return static_cast<float>(k);
+      float v;
+      std::memcpy(&v, &k, 4);
+      return v;
+    };
+    minmax_out[0] = mm[1] ? value(mm[0]) : 0.f;
+    minmax_out[1] = mm[1] ? value(mm[1]) : 0.f;
   }
   dev_free(ctx, blk);
 }

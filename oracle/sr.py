@@ -138,7 +138,12 @@ def lanczos_down(img: np.ndarray, s: int) -> np.ndarray:
 
 
 def super_resolve(frames: np.ndarray, factor: int = 4, iters: int = 200, eps: float = 1e-12):
-    """(uint16 depth, warps [F][2][3], iterations [F])."""
+    """(depth, warps [F][2][3], iterations [F]).  uint16 frames (Kinect v1,
+    super_resolution.cpp): the fused image rounded half to even and saturated
+    to uint16, a pixel no frame covers NaN before the resampling.  float32
+    frames (Kinect v2, super_resolution_kv2.cpp:287-311): a pixel no frame
+    covers is 0 and the float result is returned as is."""
+    kv2 = np.asarray(frames).dtype == np.float32
     F, h, w = frames.shape
     img = frames.astype(np.float32)
     blur = gauss5(img)
@@ -157,8 +162,12 @@ def super_resolve(frames: np.ndarray, factor: int = 4, iters: int = 200, eps: fl
     pos = stack > 0
     with np.errstate(invalid="ignore", divide="ignore"):
         ze = (np.where(pos, stack, 0).sum(0) / pos.sum(0)).astype(np.float32)
+    if kv2:
+        ze[pos.sum(0) == 0] = 0
     hr = np.repeat(np.repeat(ze, factor, axis=0), factor, axis=1)
     lr = lanczos_down(hr, factor)
+    if kv2:
+        return lr.astype(np.float32), warps, its
     with np.errstate(invalid="ignore"):
         r = np.rint(lr)
         r = np.where(r > 0, r, 0)

@@ -117,22 +117,20 @@ def _paeth(a: int, b: int, c: int) -> int:
     return a if pa <= pb and pa <= pc else (b if pb <= pc else c)
 
 
-def write_png16(path, img: np.ndarray) -> None:
-    """16-bit grayscale PNG, row y filtered with filter type y % 5 so that the
-    tool's decoder meets every scanline filter."""
-    h, w = img.shape
-    be = img.astype(">u2").tobytes()
-    stride = 2 * w
+def _write_png(path, rows: bytes, w: int, h: int, depth: int, ctype: int, bpp: int) -> None:
+    """PNG of h rows of w * bpp bytes, row y filtered with filter type y % 5
+    so that the tool's decoder meets every scanline filter."""
+    stride = w * bpp
     raw = bytearray()
     prev = bytes(stride)
     for y in range(h):
-        row = be[y * stride:(y + 1) * stride]
+        row = rows[y * stride:(y + 1) * stride]
         ft = y % 5
         out = bytearray([ft])
         for i in range(stride):
-            a = row[i - 2] if i >= 2 else 0
+            a = row[i - bpp] if i >= bpp else 0
             b = prev[i]
-            c = prev[i - 2] if i >= 2 else 0
+            c = prev[i - bpp] if i >= bpp else 0
             pred = (0, a, b, (a + b) // 2, _paeth(a, b, c))[ft]
             out.append((row[i] - pred) & 255)
         raw += out
@@ -140,33 +138,61 @@ def write_png16(path, img: np.ndarray) -> None:
 
     def chunk(t: bytes, data: bytes) -> bytes:
         return struct.pack(">I", len(data)) + t + data + struct.pack(">I", zlib.crc32(t + data) & 0xFFFFFFFF)
-    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 16, 0, 0, 0, 0))
+    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, 0))
     png += chunk(b"IDAT", zlib.compress(bytes(raw), 6)) + chunk(b"IEND", b"")
     Path(path).write_bytes(png)
 
 
-def read_png16(path) -> np.ndarray:
-    """The tool's output: 16-bit grayscale, filter type 0 on every row."""
+def write_png16(path, img: np.ndarray) -> None:
+    h, w = img.shape
+    _write_png(path, img.astype(">u2").tobytes(), w, h, 16, 0, 2)
+
+
+def write_png_float(path, img: np.ndarray) -> None:
+    """A float depth image as the Kinect v2 tools store it: each float's
+    little-endian bytes b0..b3 are an OpenCV BGRA pixel, i.e. the PNG's RGBA
+    pixel (b2, b1, b0, b3)."""
+    h, w = img.shape
+    b = np.ascontiguousarray(img, dtype="<f4").view(np.uint8).reshape(h, w, 4)
+    _write_png(path, np.ascontiguousarray(b[..., [2, 1, 0, 3]]).tobytes(), w, h, 8, 6, 4)
+
+
+def _read_png(path):
+    """(unfiltered bytes [h][stride], w, h, depth, ctype) of the tool's
+    output: filter type 0 on every row."""
     data = Path(path).read_bytes()
     assert data[:8] == b"\x89PNG\r\n\x1a\n"
-    pos, idat, w, h = 8, b"", 0, 0
+    pos, idat, w, h, depth, ctype = 8, b"", 0, 0, 0, 0
     while pos < len(data):
         n, = struct.unpack(">I", data[pos:pos + 4])
         t, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
         assert struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])[0] == zlib.crc32(t + body) & 0xFFFFFFFF
         if t == b"IHDR":
-            w, h, depth, color = struct.unpack(">IIBB", body[:10])
-            assert depth == 16 and color == 0
+            w, h, depth, ctype = struct.unpack(">IIBB", body[:10])
         elif t == b"IDAT":
             idat += body
         pos += 12 + n
-    raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, 1 + 2 * w)
+    bpp = (1 if ctype == 0 else 4) * depth // 8
+    raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, 1 + bpp * w)
     assert np.all(raw[:, 0] == 0)
-    return raw[:, 1:].copy().view(">u2").astype(np.uint16).reshape(h, w)
+    return raw[:, 1:].copy(), w, h, depth, ctype
 
 
-def run_tool(*args, cwd):
-    return subprocess.run([str(BIN / "super_resolution"), *map(str, args)], capture_output=True, text=True,
+def read_png16(path) -> np.ndarray:
+    rows, w, h, depth, ctype = _read_png(path)
+    assert depth == 16 and ctype == 0
+    return rows.view(">u2").astype(np.uint16).reshape(h, w)
+
+
+def read_png_float(path) -> np.ndarray:
+    rows, w, h, depth, ctype = _read_png(path)
+    assert depth == 8 and ctype == 6
+    px = rows.reshape(h, w, 4)[..., [2, 1, 0, 3]]
+    return np.ascontiguousarray(px).view("<f4").reshape(h, w).astype(np.float32)
+
+
+def run_tool(*args, cwd, tool="super_resolution"):
+    return subprocess.run([str(BIN / tool), *map(str, args)], capture_output=True, text=True,
                           timeout=300, cwd=cwd)
 
 
@@ -175,8 +201,8 @@ def sr_tool():
     from lowcost3dreconstruction_gb300 import build
     build.build_lib()
     build.build_tools()
-    if not (BIN / "super_resolution").exists():
-        pytest.skip("super_resolution needs zlib headers")
+    if not (BIN / "super_resolution").exists() or not (BIN / "super_resolution_kv2").exists():
+        pytest.skip("the super-resolution tools need zlib headers")
 
 
 def test_png_writer_reader_round_trip(tmp_path):
@@ -186,19 +212,42 @@ def test_png_writer_reader_round_trip(tmp_path):
     assert data[:8] == b"\x89PNG\r\n\x1a\n" and b"IHDR" in data
 
 
-def test_tool_help_and_usage_errors(sr_tool, tmp_path):
-    r = run_tool("-h", cwd=tmp_path)
+def test_png_float_round_trip(tmp_path):
+    img = np.random.default_rng(1).uniform(500, 1500, (5, 9)).astype(np.float32)
+    write_png_float(tmp_path / "f.png", img)
+    data = (tmp_path / "f.png").read_bytes()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+
+
+@pytest.mark.parametrize("tool", ["super_resolution", "super_resolution_kv2"])
+def test_tool_help_and_usage_errors(sr_tool, tmp_path, tool):
+    r = run_tool("-h", cwd=tmp_path, tool=tool)
     assert r.returncode == 0
     for f in ("--capture_name", "--capture_step", "--num_captures", "--sr_size", "--resample_factor",
               "--view_angle", "--top", "--bottom"):
         assert f in r.stdout, f
     assert "(=artefact)" in r.stdout and "(=16)" in r.stdout and "(=4)" in r.stdout
-    r = run_tool("-f", "0", cwd=tmp_path)
+    r = run_tool("-f", "0", cwd=tmp_path, tool=tool)
     assert r.returncode == 255 and "must be bigger than zero" in r.stdout
-    r = run_tool("-a", "20", "-t", cwd=tmp_path)
+    r = run_tool("-a", "20", "-t", cwd=tmp_path, tool=tool)
     assert r.returncode == 255 and "can not be used together" in r.stdout
-    r = run_tool("-a", "20", "-n", "missing", cwd=tmp_path)
+    r = run_tool("-a", "20", "-n", "missing", cwd=tmp_path, tool=tool)
     assert r.returncode == 255 and "Image can not be read: missing_burst_20_0.png" in r.stdout
+
+
+def test_kv2_tool_rejects_a_grayscale_burst(sr_tool, tmp_path):
+    write_png16(tmp_path / "g_burst_0_0.png", np.ones((4, 4), np.uint16))
+    r = run_tool("-n", "g", "-a", "0", "-z", "1", cwd=tmp_path, tool="super_resolution_kv2")
+    assert r.returncode == 255 and "Image can not be read: g_burst_0_0.png" in r.stdout
+
+
+def test_oracle_kv2_leaves_uncovered_pixels_zero():
+    frames, _ = burst(F=2, seed=4, holes=False)
+    f = frames.astype(np.float32)
+    f[:, 10:30, 20:40] = 0  # no frame covers the middle of this square
+    out, _, _ = O.super_resolve(f, 4, 5, 1e-10)
+    assert out.dtype == np.float32 and np.all(np.isfinite(out))
+    assert np.all(out[15:25, 25:35] == 0)
 
 
 @pytest.mark.gpu
@@ -256,3 +305,72 @@ def test_ecc_stops_when_the_coefficient_settles(ctx):
     assert np.all(wits[1:] < 10)
     assert np.all(its[1:] < 20), its
     np.testing.assert_allclose(warps, wwarps, atol=5e-5)
+
+
+# ------------------------------------------------------------------ Kinect v2
+@pytest.mark.gpu
+def test_super_resolve_f32_matches_the_uint16_path(ctx):
+    """Float frames holding whole millimetres take the same arithmetic as the
+    uint16 frames: the same warps and iterations, and the float result
+    rounds to the uint16 result (every pixel is covered by frame 0)."""
+    frames, _ = burst(F=4, seed=6, holes=False)
+    out16, w16, mm16, it16 = ctx.super_resolve(frames, ecc_iterations=50, ecc_epsilon=1e-10)
+    outf, wf, mmf, itf = ctx.super_resolve(frames.astype(np.float32), ecc_iterations=50, ecc_epsilon=1e-10)
+    assert outf.dtype == np.float32 and out16.dtype == np.uint16
+    np.testing.assert_array_equal(wf, w16)
+    np.testing.assert_array_equal(itf, it16)
+    assert mmf == mm16
+    np.testing.assert_array_equal(np.clip(np.rint(outf), 0, 65535).astype(np.uint16), out16)
+
+
+@pytest.mark.gpu
+def test_super_resolve_f32_matches_oracle(ctx):
+    rng = np.random.default_rng(8)
+    frames, _ = burst(F=3, seed=7, holes=False)
+    f = (frames.astype(np.float32) + rng.uniform(-0.5, 0.5, frames.shape)).astype(np.float32)
+    out, warps, mm, _ = ctx.super_resolve(f, ecc_iterations=40, ecc_epsilon=1e-10)
+    want, wwarps, _ = O.super_resolve(f, 4, 40, 1e-10)
+    pos = f[f > 0]
+    assert mm == (float(pos.min()), float(pos.max()))
+    for k in range(1, 3):
+        np.testing.assert_allclose(warps[k], wwarps[k], atol=2e-3)
+    assert np.mean(np.abs(out - want) <= 0.05) > 0.995
+
+
+@pytest.mark.gpu
+def test_pinhole_f32_backprojection_equals_v1_on_whole_millimetres(ctx):
+    """LCR_DEPTH_PINHOLE_F32 (super_resolution_kv2.cpp save_ply) on float
+    depth that holds whole millimetres: the same points and normals as the
+    uint16 model, bit for bit."""
+    from lowcost3dreconstruction_gb300 import _lib as L
+    frames, _ = burst(h=48, w=64, F=1, seed=9, holes=True)
+    d = frames[0]
+    args = (64, 48, 1, 365.531799, 365.531799, 256.136810, 206.013901, 900.0, 1200.0, 0, 63, 0, 47, 1.0, 1,
+            128, 128, 128, 0)
+    a = ctx.backproject(d, L.DepthParams(L.KINECT_V1, *args)).download()
+    b = ctx.backproject(d.astype(np.float32), L.DepthParams(L.PINHOLE_F32, *args)).download()
+    assert len(a) == len(b) > 0
+    for k in a.dtype.names:
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+@pytest.mark.gpu
+def test_kv2_tool_writes_the_fused_depth_and_cloud(sr_tool, tmp_path, ctx):
+    from lowcost3dreconstruction_gb300 import _lib as L
+    rng = np.random.default_rng(10)
+    frames, _ = burst(h=48, w=64, F=4, seed=11, holes=False)
+    f = (frames.astype(np.float32) + rng.uniform(-0.5, 0.5, frames.shape)).astype(np.float32)
+    for i, fr in enumerate(f):
+        write_png_float(tmp_path / f"obj_burst_40_{i}.png", fr)
+    r = run_tool("-n", "obj", "-a", 40, "-z", 4, cwd=tmp_path, tool="super_resolution_kv2")
+    assert r.returncode == 0, r.stdout + r.stderr
+    want, _, mm, _ = ctx.super_resolve(f)
+    assert f"Observed Global Min: {mm[0]:.0f}" in r.stdout
+    assert "View(40) Alignment 3-> 0 = [" in r.stdout
+    np.testing.assert_array_equal(read_png_float(tmp_path / "obj_srdepth_40.png"), want)
+    pts = L.read_ply(tmp_path / "obj_srmesh_40.ply")
+    p = L.DepthParams(L.PINHOLE_F32, 64, 48, 1, 365.531799, 365.531799, 256.136810, 206.013901, mm[0], mm[1],
+                      0, 63, 0, 47, 1.0, 1, 128, 128, 128, 0)
+    cloud = ctx.backproject(want, p).download()
+    assert len(pts) == len(cloud) > 0
+    np.testing.assert_allclose(pts["z"], cloud["z"], rtol=1e-6, atol=1e-4)

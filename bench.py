@@ -245,10 +245,12 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
     launch_ms = sor_ms / max(1, sor_launches)
     pk = peaks()
     achieved = bytes_per_launch / (launch_ms * 1e-3) / 1e9
-    ncu_traffic = None
+    ncu_traffic, ncu_context = None, {}
     tfile = ROOT / "profiles" / "k_sor_dist_config1_traffic.json"
     if tfile.exists():
-        ncu_traffic = json.loads(tfile.read_text()).get("bytes_per_launch")
+        tj = json.loads(tfile.read_text())
+        ncu_traffic = tj.get("bytes_per_launch")
+        ncu_context = {k: tj[k] for k in ("l2_hit_rate", "issue_active", "bound_note") if k in tj}
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 4), "higher_is_better": True,
@@ -266,7 +268,7 @@ def gpu_arm(args, rank: int, world: int, dist) -> dict | None:
                      "achieved": round(achieved, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / pk["hbm_gbs"], 5), "peak_src": pk["src"],
                      "algorithmic_bytes_per_launch": int(bytes_per_launch), "avg_launch_ms": round(launch_ms, 5),
-                     "launches": int(sor_launches), "traffic": ncu_traffic},
+                     "launches": int(sor_launches), "traffic": ncu_traffic, **ncu_context},
         "e2e": {"value": round(e2e_value, 3), "unit": "pairs/s",
                 "h2d_bytes_per_step": int(sum(f.nbytes for f in frames)), "d2h_bytes_per_step": 4 * 16 + 8 * 16},
         "gpu_launches": int(launches),

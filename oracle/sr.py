@@ -96,7 +96,11 @@ def ecc_affine(tmpl: np.ndarray, img: np.ndarray, gx: np.ndarray, gy: np.ndarray
         r = corr / (inorm * tnorm) if inorm > 0 and tnorm > 0 else 0.0
         H = J @ J.T
         ip, tp = J @ izm, J @ tzm
-        hi, ht = np.linalg.solve(H, ip), np.linalg.solve(H, tp)
+        try:  # a singular (or indefinite) system stops the iteration, as on the GPU
+            np.linalg.cholesky(H)
+            hi, ht = np.linalg.solve(H, ip), np.linalg.solve(H, tp)
+        except np.linalg.LinAlgError:
+            break
         lam_n = izm @ izm - ip @ hi
         lam_d = corr - tp @ hi
         if not lam_d > 0:

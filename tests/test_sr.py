@@ -374,3 +374,32 @@ def test_kv2_tool_writes_the_fused_depth_and_cloud(sr_tool, tmp_path, ctx):
     cloud = ctx.backproject(want, p).download()
     assert len(pts) == len(cloud) > 0
     np.testing.assert_allclose(pts["z"], cloud["z"], rtol=1e-6, atol=1e-4)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("h,w,F,factor", [(5, 7, 3, 4), (1, 9, 2, 4), (33, 130, 4, 1), (40, 40, 2, 3), (24, 20, 1, 16)])
+def test_super_resolve_odd_shapes_match_oracle(ctx, h, w, F, factor):
+    """Ragged sizes (no multiple of a block, a single row, factor 1 and 16,
+    one frame): the same result as the oracle within one unit."""
+    frames, _ = burst(h=h, w=w, F=F, seed=h * w + F, holes=False)
+    out, warps, mm, its = ctx.super_resolve(frames, factor=factor, ecc_iterations=30, ecc_epsilon=1e-10)
+    want, wwarps, wits = O.super_resolve(frames, factor, 30, 1e-10)
+    assert out.shape == (h, w) and np.all(its <= 30)
+    if h * w < 100:  # a handful of pixels: the registration is too ill-posed to compare paths
+        assert mm == (float(frames[frames > 0].min()), float(frames.max()))
+        return
+    np.testing.assert_allclose(warps, wwarps, atol=2e-3)
+    assert np.mean(np.abs(out.astype(np.int64) - want.astype(np.int64)) <= 1) > 0.99
+
+
+@pytest.mark.gpu
+def test_super_resolve_all_zero_burst(ctx):
+    """No depth anywhere: the registration stops at once (singular system),
+    the range is (0, 0) and the fused image is all zero, as the oracle says."""
+    frames = np.zeros((3, 24, 32), np.uint16)
+    out, warps, mm, its = ctx.super_resolve(frames)
+    want, wwarps, wits = O.super_resolve(frames)
+    assert mm == (0.0, 0.0)
+    assert np.all(out == 0) and np.all(want == 0)
+    np.testing.assert_array_equal(its, wits)
+    np.testing.assert_array_equal(warps, wwarps)

@@ -403,3 +403,23 @@ def test_super_resolve_all_zero_burst(ctx):
     assert np.all(out == 0) and np.all(want == 0)
     np.testing.assert_array_equal(its, wits)
     np.testing.assert_array_equal(warps, wwarps)
+
+
+@pytest.mark.gpu
+def test_tool_iterates_the_views_and_wraps_the_angle(sr_tool, tmp_path):
+    """-c 2 -s 20 fuses views 0 and 20; -a 380 names view 20 (the angle is
+    taken modulo 360, super_resolution.cpp:194)."""
+    for view in (0, 20):
+        frames, _ = burst(h=24, w=32, F=2, seed=20 + view, holes=False)
+        for i, f in enumerate(frames):
+            write_png16(tmp_path / f"m_burst_{view}_{i}.png", f)
+    r = run_tool("-n", "m", "-c", 2, "-s", 20, "-z", 2, cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Step: 20" in r.stdout and "N. of captures: 2" in r.stdout
+    for view in (0, 20):
+        assert (tmp_path / f"m_srdepth_{view}.png").exists() and (tmp_path / f"m_srmesh_{view}.ply").exists()
+    first = (tmp_path / "m_srdepth_20.png").read_bytes()
+    (tmp_path / "m_srdepth_20.png").unlink()
+    r = run_tool("-n", "m", "-a", 380, "-z", 2, cwd=tmp_path)
+    assert r.returncode == 0 and "View angle: 20" in r.stdout
+    assert (tmp_path / "m_srdepth_20.png").read_bytes() == first

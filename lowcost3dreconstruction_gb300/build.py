@@ -85,8 +85,8 @@ def build_lib(jobs: int | None = None, verbose: bool = False) -> Path:
 
 
 # Tools with extra sources and libraries, built only where the library is present.
-EXTRA_TOOLS = {"super_resolution": (["sr_tool.cpp", "png16.cpp"], ["-lz"], "zlib.h"),
-               "super_resolution_kv2": (["sr_tool.cpp", "png16.cpp"], ["-lz"], "zlib.h")}
+EXTRA_TOOLS = {"super_resolution": (["sr_tool.cpp", "png16.cpp"], ["-lz", "-pthread"], "zlib.h"),
+               "super_resolution_kv2": (["sr_tool.cpp", "png16.cpp"], ["-lz", "-pthread"], "zlib.h")}
 
 
 def _have_header(name: str) -> bool:

@@ -106,26 +106,34 @@ bool decode(const std::string& path, std::vector<unsigned char>& img, int& width
     return false;
   }
   img.assign(stride * height, 0);
+  const std::vector<unsigned char> zero(stride, 0);
   for (int y = 0; y < height; ++y) {
-    const unsigned char* row = &raw[y * (stride + 1)];
-    const unsigned char* prev = y > 0 ? &img[(y - 1) * stride] : nullptr;
+    const unsigned char* x = &raw[y * (stride + 1) + 1];
+    const unsigned char* b = y > 0 ? &img[(y - 1) * stride] : zero.data();  // the row above
     unsigned char* cur = &img[y * stride];
-    const int filter = row[0];
-    for (size_t i = 0; i < stride; ++i) {
-      const int x = row[1 + i];
-      const int a = i >= bpp ? cur[i - bpp] : 0, b = prev ? prev[i] : 0, c = prev && i >= bpp ? prev[i - bpp] : 0;
-      int v;
-      switch (filter) {
-        case 0: v = x; break;
-        case 1: v = x + a; break;
-        case 2: v = x + b; break;
-        case 3: v = x + ((a + b) >> 1); break;
-        case 4: v = x + paeth(a, b, c); break;
-        default:
-          err = path + ": unknown scanline filter";
-          return false;
-      }
-      cur[i] = static_cast<unsigned char>(v & 255);
+    // one loop per filter type; a = the byte bpp to the left, c = the one above it
+    switch (raw[y * (stride + 1)]) {
+      case 0:
+        std::memcpy(cur, x, stride);
+        break;
+      case 1:
+        for (size_t i = 0; i < stride; ++i) cur[i] = static_cast<unsigned char>(x[i] + (i >= bpp ? cur[i - bpp] : 0));
+        break;
+      case 2:
+        for (size_t i = 0; i < stride; ++i) cur[i] = static_cast<unsigned char>(x[i] + b[i]);
+        break;
+      case 3:
+        for (size_t i = 0; i < stride; ++i)
+          cur[i] = static_cast<unsigned char>(x[i] + (((i >= bpp ? cur[i - bpp] : 0) + b[i]) >> 1));
+        break;
+      case 4:
+        for (size_t i = 0; i < stride; ++i)
+          cur[i] = static_cast<unsigned char>(
+              x[i] + (i >= bpp ? paeth(cur[i - bpp], b[i], b[i - bpp]) : paeth(0, b[i], 0)));
+        break;
+      default:
+        err = path + ": unknown scanline filter";
+        return false;
     }
   }
   return true;

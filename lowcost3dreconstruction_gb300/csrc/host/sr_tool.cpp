@@ -12,10 +12,13 @@
 // 128, millimetres, ASCII as save_ply writes).
 #include "sr_tool.h"
 
+#include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <iostream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "cli_common.h"
@@ -80,36 +83,64 @@ int run(int argc, char* argv[], bool kv2) {
       std::vector<uint16_t> burst;
       std::vector<float> burst_f;
       int w = 0, h = 0;
-      for (long i = 0; i < sr_size; ++i) {
-        const std::string file = name + "_burst_" + view + "_" + std::to_string(i) + ".png";
-        int wi = 0, hi = 0;
+      // The frames decode in parallel (PNG inflate and unfiltering are the
+      // tool's largest host cost); the first unreadable frame in index order,
+      // or one whose size differs from frame 0, is reported.
+      struct Frame {
+        std::vector<uint16_t> px;
+        std::vector<float> pf;
+        int w = 0, h = 0;
+        bool ok = false;
+      };
+      std::vector<Frame> fr(static_cast<size_t>(sr_size));
+      auto file_of = [&](long i) { return name + "_burst_" + view + "_" + std::to_string(i) + ".png"; };
+      auto decode = [&](long i) {
+        Frame& f = fr[static_cast<size_t>(i)];
         std::string err;
-        bool ok;
         if (kv2) {
           std::vector<unsigned char> rgba;
-          ok = png16::read_rgba8(file, rgba, wi, hi, err);
-          if (ok) {
+          f.ok = png16::read_rgba8(file_of(i), rgba, f.w, f.h, err);
+          if (f.ok) {
             // the four bytes of each float, stored by OpenCV as a BGRA pixel
-            const size_t n = static_cast<size_t>(wi) * hi;
-            const size_t at = burst_f.size();
-            burst_f.resize(at + n);
+            const size_t n = static_cast<size_t>(f.w) * f.h;
+            f.pf.resize(n);
             for (size_t k = 0; k < n; ++k) {
-              const unsigned char b[4] = {rgba[4 * k + 2], rgba[4 * k + 1], rgba[4 * k], rgba[4 * k + 3]};
-              std::memcpy(&burst_f[at + k], b, 4);
+              const unsigned char by[4] = {rgba[4 * k + 2], rgba[4 * k + 1], rgba[4 * k], rgba[4 * k + 3]};
+              std::memcpy(&f.pf[k], by, 4);
             }
           }
         } else {
-          std::vector<uint16_t> px;
-          ok = png16::read(file, px, wi, hi, err);
-          if (ok) burst.insert(burst.end(), px.begin(), px.end());
+          f.ok = png16::read(file_of(i), f.px, f.w, f.h, err);
         }
-        if (!ok || (i > 0 && (wi != w || hi != h))) {
-          std::cout << "Image can not be read: " << file << std::endl;
+      };
+      {
+        const long nt = std::max(1L, std::min<long>(sr_size, std::thread::hardware_concurrency()));
+        std::atomic<long> next{0};
+        std::vector<std::thread> pool;
+        for (long t = 0; t < nt; ++t)
+          pool.emplace_back([&] {
+            for (long i; (i = next++) < sr_size;) decode(i);
+          });
+        for (auto& t : pool) t.join();
+      }
+      for (long i = 0; i < sr_size; ++i) {
+        const Frame& f = fr[static_cast<size_t>(i)];
+        if (!f.ok || f.w != fr[0].w || f.h != fr[0].h) {
+          std::cout << "Image can not be read: " << file_of(i) << std::endl;
           return -1;
         }
-        w = wi;
-        h = hi;
       }
+      w = fr[0].w;
+      h = fr[0].h;
+      const size_t plane = static_cast<size_t>(w) * h;
+      if (kv2) {
+        burst_f.resize(plane * sr_size);
+        for (long i = 0; i < sr_size; ++i) std::copy(fr[i].pf.begin(), fr[i].pf.end(), burst_f.begin() + plane * i);
+      } else {
+        burst.resize(plane * sr_size);
+        for (long i = 0; i < sr_size; ++i) std::copy(fr[i].px.begin(), fr[i].px.end(), burst.begin() + plane * i);
+      }
+      fr.clear();
       lcr::Context& ctx = lcr::Context::thread_default();
       lcr_sr_params sp;
       sp.width = w;

@@ -80,6 +80,20 @@ def test_into_kinect_v2_and_single_frame():
         _same(_into(ctx, f0, one), _device(ctx, f0, one))
 
 
+def test_into_pinhole_float_burst():
+    """LCR_DEPTH_PINHOLE_F32 (the Kinect v2 super-resolution cloud): a fused
+    float burst with normals, through both entry points."""
+    cam = S.KINECT_V2
+    d = S.raycast(S.sphere_on_cube_room(), cam)
+    fr = S.kinect_frames(d, 3, np.random.default_rng(11), as_float=True).astype(np.float32)
+    with Context(0) as ctx:
+        p = ctx.depth_params(L.PINHOLE_F32, 512, 424, frames=3, fx=365.531799, fy=365.531799, cx=256.136810,
+                             cy=206.013901, depth_min=500, depth_max=2500, scale=1.0, normals=True)
+        a = _into(ctx, fr, p)
+        assert len(a) > 10_000
+        _same(a, _device(ctx, fr, p))
+
+
 def test_into_truncates_at_capacity_and_reports_the_count():
     pr = S.config1_pair(2)
     frames = np.ascontiguousarray(pr.src_frames[0], dtype=np.uint16)

@@ -14,12 +14,14 @@
 //  4. nearest upsampling by the factor and the ZE-mean per pixel     :274-310
 //  5. Lanczos-4 resampling back to the sensor grid, rounded and
 //     saturated to uint16                                           :312-314
+// The Kinect v2 form (super_resolution_kv2.cpp:222-311) takes float frames,
+// leaves an uncovered pixel at 0 and returns the float result unrounded.
 //
 // All frames of a burst register at once: one pass per iteration accumulates
-// for every frame the 45 sums the Gauss-Newton step needs (exact FP64 products
-// for the correlation coefficient, compensated FP32 for the Jacobian terms,
-// FP64 reductions in a fixed order), and one thread per frame solves the 6x6
-// system.
+// for every frame the 45 sums the Gauss-Newton step needs (FP32 pairs: exact
+// to ~2^-44 for the correlation coefficient, Kahan-compensated for the
+// Jacobian terms, added in a fixed order), and the last block of each frame
+// takes the FP64 step on one thread.
 // The smoothing and gradient filters mirror the border at its edge pixel
 // (reflect-101); the Lanczos taps clamp to the image.
 #include <algorithm>
@@ -250,16 +252,17 @@ __device__ void ecc_step(const double* s, int f, float* warps, double* rho, int*
   if (fabs(r - prev) < eps || iters[f] >= max_iter) active[f] = 0;
 }
 
-// One ECC pass for frame f = 1 + blockIdx.y: per template pixel (x, y) the
+// One ECC pass for frame f = list[blockIdx.y] (the frames still iterating),
+// blockIdx.x striding over the pixels: per template pixel (x, y) the
 // input sampled at W(x, y) = (m0 x + m1 y + m2, m3 x + m4 y + m5), its
 // gradients, the validity mask (all four bilinear taps inside the image: a
 // half-outside sample of a depth image is a large outlier) and the masked
 // Jacobian J = (x gx, x gy, y gx, y gy, gx, gy) with respect to
 // (m0, m3, m1, m4, m2, m5); the block's 45 sums go to part[frame][block][45].
 constexpr int kEccThreads = 256;
-__global__ void __launch_bounds__(kEccThreads, 2) k_ecc_pass(const float4* __restrict__ pk, int w, int h, const int* __restrict__ list, float* warps,
-                                                           int* active, float2* part, unsigned int* done, double* rho,
-                                                           int* iters, double eps, int max_iter) {
+__global__ void __launch_bounds__(kEccThreads, 2)
+    k_ecc_pass(const float4* __restrict__ pk, int w, int h, const int* __restrict__ list, float* warps, int* active,
+               float2* part, unsigned int* done, double* rho, int* iters, double eps, int max_iter) {
   const int f = list[blockIdx.y];
   if (!active[f]) return;
   __shared__ float2 red[kEccThreads / 32][kSums];

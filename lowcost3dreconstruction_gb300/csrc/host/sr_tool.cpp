@@ -54,7 +54,8 @@ int run(int argc, char* argv[], bool kv2) {
       std::cout << "The command option 'resample_factor', must be bigger than zero" << std::endl;
       return -1;
     }
-    if (sr_size <= 0 || step < 0 || ncap < 0) throw std::logic_error("sr_size must be positive");
+    if (sr_size <= 0) throw std::logic_error("sr_size must be positive");
+    if (step < 0 || ncap < 0) throw std::logic_error("capture_step and num_captures must not be negative");
     std::string view;
     const bool va = desc.count("view_angle"), top = desc.count("top"), bottom = desc.count("bottom");
     const bool single = va || top || bottom;
@@ -200,7 +201,8 @@ int run(int argc, char* argv[], bool kv2) {
       dp.normals = 1;
       dp.r = dp.g = dp.b = 128;
       lcr_cloud* cl = nullptr;
-      ctx.check(lcr_backproject(ctx.get(), kv2 ? static_cast<const void*>(fused_f.data()) : fused.data(), &dp, &cl));
+      const void* fused_px = kv2 ? static_cast<const void*>(fused_f.data()) : fused.data();
+      ctx.check(lcr_backproject(ctx.get(), fused_px, &dp, &cl));
       lcr::PointCloud pc;
       lcr::DeviceCloud(ctx, cl).download(pc);
       const std::string ply = name + "_srmesh_" + view + ".ply";

@@ -54,6 +54,41 @@ def test_oracle_lanczos_weights():
     np.testing.assert_array_equal(O.lanczos4_weights(0.0), np.eye(8, dtype=np.float32)[3])
 
 
+def test_oracle_filters_agree_with_scipy():
+    """The oracle's smoothing, gradients and bilinear sampling against
+    scipy.ndimage, an independent implementation of the same operations
+    (reflect-101 is scipy's 'mirror'; the zero border is 'constant', 0)."""
+    nd = pytest.importorskip("scipy.ndimage")
+    img = burst(F=1, seed=12, holes=True)[0][0].astype(np.float32)
+    s = 1.1
+    g = np.array([np.exp(-4 / (2 * s * s)), np.exp(-1 / (2 * s * s)), 1.0, np.exp(-1 / (2 * s * s)),
+                  np.exp(-4 / (2 * s * s))])
+    g /= g.sum()
+    want = nd.correlate1d(nd.correlate1d(img.astype(np.float64), g, axis=1, mode="mirror"), g, axis=0, mode="mirror")
+    np.testing.assert_allclose(O.gauss5(img), want, rtol=1e-6, atol=1e-3)
+    gx, gy = O.grad(img)
+    np.testing.assert_allclose(gx[:, 1:-1], np.gradient(img.astype(np.float64), axis=1)[:, 1:-1], atol=1e-3)
+    np.testing.assert_allclose(gy[1:-1], np.gradient(img.astype(np.float64), axis=0)[1:-1], atol=1e-3)
+    rng = np.random.default_rng(13)
+    u = rng.uniform(0, img.shape[1] - 1, 500).astype(np.float32)
+    v = rng.uniform(0, img.shape[0] - 1, 500).astype(np.float32)
+    ref = nd.map_coordinates(img.astype(np.float64), [v, u], order=1, mode="constant", cval=0.0)
+    np.testing.assert_allclose(O.bilinear(img, u, v), ref, rtol=1e-6, atol=1e-3)
+
+
+def test_oracle_lanczos_reproduces_a_linear_ramp():
+    """Downsampling by 4 samples at p = 4 o + 1.5, where the normalised
+    Lanczos-4 weights are symmetric: a linear ramp comes out as its value at
+    p (away from the clamped borders) -- a property, not a restatement."""
+    H, W = 64, 96
+    y, x = np.mgrid[0:H, 0:W].astype(np.float64)
+    ramp = (100 + 3 * x - 2 * y).astype(np.float32)
+    out = O.lanczos_down(ramp, 4)
+    oy, ox = np.mgrid[0:H // 4, 0:W // 4].astype(np.float64)
+    want = 100 + 3 * (4 * ox + 1.5) - 2 * (4 * oy + 1.5)
+    np.testing.assert_allclose(out[1:-1, 1:-1], want[1:-1, 1:-1], atol=2e-3)
+
+
 def test_oracle_ecc_recovers_a_known_motion():
     frames, truth = burst(F=2, holes=False)
     blur = O.gauss5(frames.astype(np.float32))

@@ -1,7 +1,7 @@
 """ctypes wrapper of liboracle.so -- TEST INFRASTRUCTURE ONLY.
 
 Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
-checker / CPU timing reference; never by the library.  Parity is UNPINNED (the
+parity reference and CPU timing baseline; never by the library.  Parity is UNPINNED (the
 reference has no tests or golden vectors and its PCL/OpenCV code cannot be
 built here); see oracle.h for what each function restates.
 """

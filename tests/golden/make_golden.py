@@ -1,8 +1,9 @@
 """Generates the golden fixtures in this folder from the CPU oracle on small
 seeded inputs.  The fixtures pin the oracle's own outputs (a regression guard
-for the checker); the reference itself has no tests or vectors to pin to.
+for the oracle); the reference itself has no tests or vectors to pin to.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # oracle_small.npz and sr_small.npz
+    python tests/golden/make_golden.py sr       # sr_small.npz only
 """
 from __future__ import annotations
 
@@ -81,5 +82,34 @@ def main() -> None:
     print("wrote", HERE / "oracle_small.npz", sum(v.nbytes for v in g.values()), "bytes raw")
 
 
+def sr_fixtures() -> None:
+    """The super-resolution oracle (oracle/sr.py) on a 4-frame 40 x 48 burst of
+    a smooth scene under small rigid motions with 1% holes, uint16 and float."""
+    from oracle import sr as OS
+    rng = np.random.default_rng(20261204)
+    h, w = 40, 48
+    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+    frames = []
+    for f in range(4):
+        a = 0.0 if f == 0 else np.deg2rad(rng.uniform(-0.4, 0.4))
+        tx, ty = (0.0, 0.0) if f == 0 else rng.uniform(-0.6, 0.6, 2)
+        X = np.cos(a) * x - np.sin(a) * y + tx
+        Y = np.sin(a) * x + np.cos(a) * y + ty
+        d = 1000 + 90 * np.sin(X / 6.0) * np.cos(Y / 5.0) + 0.5 * X + rng.normal(0, 0.3, x.shape)
+        d[rng.random(d.shape) < 0.01] = 0
+        frames.append(np.clip(np.rint(d), 0, 65535).astype(np.uint16))
+    frames = np.stack(frames)
+    g = {"frames": frames}
+    g["fused"], g["warps"], g["iters"] = OS.super_resolve(frames, 4, 30, 1e-10)
+    ff = frames.astype(np.float32) + rng.uniform(-0.5, 0.5, frames.shape).astype(np.float32)
+    ff[frames == 0] = 0
+    g["frames_f32"] = ff
+    g["fused_f32"], g["warps_f32"], g["iters_f32"] = OS.super_resolve(ff, 4, 30, 1e-10)
+    np.savez_compressed(HERE / "sr_small.npz", **g)
+    print("wrote", HERE / "sr_small.npz", sum(v.nbytes for v in g.values()), "bytes raw")
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] != ["sr"]:
+        main()
+    sr_fixtures()

@@ -458,3 +458,32 @@ def test_tool_iterates_the_views_and_wraps_the_angle(sr_tool, tmp_path):
     r = run_tool("-n", "m", "-a", 380, "-z", 2, cwd=tmp_path)
     assert r.returncode == 0 and "View angle: 20" in r.stdout
     assert (tmp_path / "m_srdepth_20.png").read_bytes() == first
+
+
+# ------------------------------------------------------------------ fixtures
+GOLD = Path(__file__).resolve().parent / "golden" / "sr_small.npz"
+
+
+def test_oracle_reproduces_the_committed_fixture():
+    """tests/golden/sr_small.npz (made by tests/golden/make_golden.py sr)
+    pins the oracle's own outputs on a holed 4-frame burst, uint16 and float."""
+    g = np.load(GOLD)
+    out, warps, its = O.super_resolve(g["frames"], 4, 30, 1e-10)
+    np.testing.assert_array_equal(its, g["iters"])
+    np.testing.assert_allclose(warps, g["warps"], atol=1e-6)
+    assert np.abs(out.astype(np.int64) - g["fused"].astype(np.int64)).max() <= 1
+    outf, warpsf, itsf = O.super_resolve(g["frames_f32"], 4, 30, 1e-10)
+    np.testing.assert_array_equal(itsf, g["iters_f32"])
+    np.testing.assert_allclose(warpsf, g["warps_f32"], atol=1e-6)
+    np.testing.assert_allclose(outf, g["fused_f32"], atol=1e-3)
+
+
+@pytest.mark.gpu
+def test_super_resolve_matches_the_committed_fixture(ctx):
+    g = np.load(GOLD)
+    for key in ("", "_f32"):
+        out, warps, _, _ = ctx.super_resolve(g["frames" + key], ecc_iterations=30, ecc_epsilon=1e-10)
+        np.testing.assert_allclose(warps, g["warps" + key], atol=2e-3)
+        want = g["fused" + key]
+        tol = 1 if key == "" else 0.05
+        assert np.mean(np.abs(out.astype(np.float64) - want.astype(np.float64)) <= tol) > 0.99

@@ -2,8 +2,8 @@
 seeded inputs.  The fixtures pin the oracle's own outputs (a regression guard
 for the oracle); the reference itself has no tests or vectors to pin to.
 
-    python tests/golden/make_golden.py          # oracle_small.npz and sr_small.npz
-    python tests/golden/make_golden.py sr       # sr_small.npz only
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py sr sfm     # sr_small.npz and sfm_small.npz only
 """
 from __future__ import annotations
 
@@ -109,7 +109,32 @@ def sr_fixtures() -> None:
     print("wrote", HERE / "sr_small.npz", sum(v.nbytes for v in g.values()), "bytes raw")
 
 
+def sfm_fixtures() -> None:
+    """The SfM filters' oracle (oracle/sfm.py) on a 3000-point floor with two
+    blobs, stray points and NaN records: the CropBox masks, the Euclidean
+    cluster labels and the RANSAC plane with its inliers and hypothesis counts."""
+    from oracle import sfm as OF
+    rng = np.random.default_rng(20261205)
+    floor = np.c_[rng.uniform(-0.5, 0.5, (2400, 2)), rng.normal(0, 0.002, 2400)]
+    blobs = [rng.normal(c, 0.02, (m, 3)) for c, m in (((0.2, 0.1, 0.2), 300), ((-0.2, -0.1, 0.25), 200))]
+    xyz = np.concatenate([floor] + blobs + [rng.uniform(-0.5, 0.5, (100, 3))]).astype(np.float32)
+    xyz = xyz[rng.permutation(len(xyz))]
+    xyz[::97] = np.nan
+    g = {"xyz": xyz}
+    g["crop_in"], g["crop_out"] = OF.crop_box(xyz, (-0.25, -0.25, -0.05), (0.25, 0.25, 0.3))
+    g["labels"], nk = OF.euclidean_clusters(xyz, 0.03, 50, len(xyz))
+    g["nclusters"] = np.array(nk)
+    c, inl, counts, best = OF.plane_segment(xyz, 0.01, 64, 7)
+    g["plane"], g["plane_inliers"], g["plane_counts"], g["plane_best"] = c, inl, counts, np.array(best)
+    np.savez_compressed(HERE / "sfm_small.npz", **g)
+    print("wrote", HERE / "sfm_small.npz", sum(v.nbytes for v in g.values()), "bytes raw")
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] != ["sr"]:
+    only = set(sys.argv[1:])
+    if not only:
         main()
-    sr_fixtures()
+    if not only or "sr" in only:
+        sr_fixtures()
+    if not only or "sfm" in only:
+        sfm_fixtures()

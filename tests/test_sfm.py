@@ -114,3 +114,38 @@ def test_sfm_tools_chain(tmp_path):
     assert r.returncode == 0, r.stderr
     assert len(L.read_ply(tmp_path / "x.ply")) + len(L.read_ply(tmp_path / "x_negative.ply")) == \
         int(np.all(np.isfinite(xyz), axis=1).sum())
+
+
+# ------------------------------------------------------------------ fixtures
+GOLD = Path(__file__).resolve().parent / "golden" / "sfm_small.npz"
+
+
+def test_oracle_reproduces_the_committed_fixture():
+    """tests/golden/sfm_small.npz (tests/golden/make_golden.py sfm) pins the
+    oracle's own outputs: masks, labels and plane on a cloud with NaN records."""
+    g = np.load(GOLD)
+    xyz = g["xyz"]
+    a, b = O.crop_box(xyz, (-0.25, -0.25, -0.05), (0.25, 0.25, 0.3))
+    np.testing.assert_array_equal(a, g["crop_in"])
+    np.testing.assert_array_equal(b, g["crop_out"])
+    labels, k = O.euclidean_clusters(xyz, 0.03, 50, len(xyz))
+    np.testing.assert_array_equal(labels, g["labels"])
+    assert k == int(g["nclusters"])
+    c, inl, counts, best = O.plane_segment(xyz, 0.01, 64, 7)
+    np.testing.assert_array_equal(counts, g["plane_counts"])
+    assert best == int(g["plane_best"])
+    np.testing.assert_allclose(c, g["plane"], atol=1e-6)
+    np.testing.assert_array_equal(inl, g["plane_inliers"])
+
+
+@pytest.mark.gpu
+def test_library_matches_the_committed_fixture(ctx):
+    from lowcost3dreconstruction_gb300.core import points_from_xyz
+    g = np.load(GOLD)
+    cloud = ctx.upload(points_from_xyz(g["xyz"]))
+    labels, k, _, _ = ctx.euclidean_clusters(cloud, 0.03, 50, len(g["xyz"]))
+    np.testing.assert_array_equal(labels, g["labels"])
+    assert k == int(g["nclusters"])
+    coef, m, _, _ = ctx.plane_segment(cloud, 0.01, 64, 7)
+    np.testing.assert_allclose(coef, g["plane"], atol=2e-6)
+    assert m == int(g["plane_inliers"].sum())

@@ -118,9 +118,10 @@ def build_tools() -> None:
 
 
 def build_oracle() -> Path:
-    if _stale(ORACLE_LIB, [ORACLE_SRC, ORACLE_SRC.with_suffix(".h")]):
+    srcs = [ORACLE_SRC, ORACLE_SRC.parent / "sr_oracle.cpp"]
+    if _stale(ORACLE_LIB, srcs + [ORACLE_SRC.with_suffix(".h")]):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp", "-o", str(ORACLE_LIB),
-              str(ORACLE_SRC)])
+              *map(str, srcs)])
     return ORACLE_LIB
 
 

@@ -122,6 +122,11 @@ void orc_centroid(const orc_point* in, size_t n, float* c);
 
 /* FP64 helpers exposed for tests (independent of the GPU implementations). */
 void orc_svd3(const double* a, double* u, double* s, double* v);
+/* Super-resolution front end of one view (sr_oracle.cpp): F frames of w x h,
+ * uint16 (f32 = 0) or float (f32 = 1); out the fused image of the same type,
+ * warps [F][6], iterations [F]. */
+void orc_super_resolve(const void* frames, int f32, int F, int w, int h, int factor, int iters, double eps,
+                       void* out, float* warps, int* iterations);
 void orc_eig3(const double* a, double* evals, double* evecs);
 
 #ifdef __cplusplus

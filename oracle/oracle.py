@@ -64,6 +64,8 @@ _SIGS = {
     "orc_centroid": (None, [_VP, C.c_size_t, _VP]),
     "orc_svd3": (None, [_VP, _VP, _VP, _VP]),
     "orc_eig3": (None, [_VP, _VP, _VP]),
+    "orc_super_resolve": (None, [_VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _VP, _VP,
+                                 _VP]),
 }
 
 _lib = None
@@ -245,3 +247,17 @@ def eig3(a):
     w, v = np.zeros(3), np.zeros(9)
     lib().orc_eig3(_p(a), _p(w), _p(v))
     return w, v.reshape(3, 3)
+
+
+def super_resolve(frames: np.ndarray, factor: int = 4, iters: int = 200, eps: float = 1e-12):
+    """The C restatement of the super-resolution front end (sr_oracle.cpp):
+    (fused image of the frames' type, warps [F][2][3], iterations [F]);
+    uint16 or float32 frames [F][h][w]."""
+    f32 = np.asarray(frames).dtype == np.float32
+    frames = np.ascontiguousarray(frames, dtype=np.float32 if f32 else np.uint16)
+    F, h, w = frames.shape
+    out = np.zeros((h, w), dtype=frames.dtype)
+    warps = np.zeros((F, 6), dtype=np.float32)
+    its = np.zeros(F, dtype=np.int32)
+    lib().orc_super_resolve(_p(frames), int(f32), F, w, h, factor, iters, eps, _p(out), _p(warps), _p(its))
+    return out, warps.reshape(F, 2, 3), its

@@ -89,6 +89,24 @@ def test_oracle_lanczos_reproduces_a_linear_ramp():
     np.testing.assert_allclose(out[1:-1, 1:-1], want[1:-1, 1:-1], atol=2e-3)
 
 
+@pytest.mark.parametrize("kind", ["holed", "clean", "float"])
+def test_c_oracle_agrees_with_the_numpy_oracle(kind):
+    """oracle/sr_oracle.cpp (the CPU baseline) against oracle/sr.py: the same
+    iterations and warps; the fused image within one unit (float: 1e-3)."""
+    from oracle import oracle as OC
+    frames, _ = burst(F=4, seed=1 if kind == "holed" else 3, holes=kind == "holed")
+    if kind == "float":
+        frames = frames.astype(np.float32) + np.float32(0.25)
+    a, wa, ia = O.super_resolve(frames, 4, 60, 1e-10)
+    b, wb, ib = OC.super_resolve(frames, 4, 60, 1e-10)
+    np.testing.assert_array_equal(ia, ib)
+    np.testing.assert_allclose(wa, wb, atol=1e-6)
+    if kind == "float":
+        np.testing.assert_allclose(a, b, atol=1e-3)
+    else:
+        assert np.abs(a.astype(np.int64) - b.astype(np.int64)).max() <= 1
+
+
 def test_oracle_ecc_recovers_a_known_motion():
     frames, truth = burst(F=2, holes=False)
     blur = O.gauss5(frames.astype(np.float32))

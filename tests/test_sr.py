@@ -505,3 +505,18 @@ def test_super_resolve_matches_the_committed_fixture(ctx):
         want = g["fused" + key]
         tol = 1 if key == "" else 0.05
         assert np.mean(np.abs(out.astype(np.float64) - want.astype(np.float64)) <= tol) > 0.99
+
+
+@pytest.mark.gpu
+def test_super_resolve_rejects_bad_arguments(ctx):
+    """Invalid sizes and limits come back as LCR_ERR_INVALID_ARG with a
+    message, and the context stays usable."""
+    from lowcost3dreconstruction_gb300 import _lib as L
+    frames, _ = burst(h=16, w=20, F=2, seed=30, holes=False)
+    for kw, msg in (({"factor": 0}, "factor"), ({"factor": 17}, "factor"), ({"ecc_iterations": -1}, "ECC"),
+                    ({"ecc_epsilon": -1.0}, "ECC")):
+        with pytest.raises(L.LcrError) as e:
+            ctx.super_resolve(frames, **kw)
+        assert e.value.status == L.INVALID_ARG and msg in str(e.value)
+    out, _, _, _ = ctx.super_resolve(frames, ecc_iterations=5)
+    assert out.shape == (16, 20)

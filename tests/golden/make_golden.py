@@ -3,7 +3,7 @@ seeded inputs.  The fixtures pin the oracle's own outputs (a regression guard
 for the oracle); the reference itself has no tests or vectors to pin to.
 
     python tests/golden/make_golden.py            # every fixture
-    python tests/golden/make_golden.py sr sfm     # sr_small.npz and sfm_small.npz only
+    python tests/golden/make_golden.py sr sfm     # only the named fixtures (sr, sfm, posenet)
 """
 from __future__ import annotations
 
@@ -130,6 +130,21 @@ def sfm_fixtures() -> None:
     print("wrote", HERE / "sfm_small.npz", sum(v.nbytes for v in g.values()), "bytes raw")
 
 
+def posenet_fixtures() -> None:
+    """The pose network's oracle forward (oracle/posenet.py) on seeded weights
+    (scaled normal draws of the seed below) and two pairs of 1024-point clouds:
+    features, max-pool winners and the head's outputs."""
+    from oracle import posenet as OP
+    rng = np.random.default_rng(20261206)
+    params = (rng.standard_normal(OP.PARAMS) * 0.05).astype(np.float32)
+    pts = rng.uniform(-0.1, 0.1, (4, 1024, 4)).astype(np.float32)
+    feat, argmax, y, _ = OP.forward(params, pts)
+    g = {"seed": np.array(20261206), "pts": pts, "feat": feat.astype(np.float32), "argmax": argmax.astype(np.int32),
+         "y": y}
+    np.savez_compressed(HERE / "posenet_small.npz", **g)
+    print("wrote", HERE / "posenet_small.npz", sum(v.nbytes for v in g.values()), "bytes raw")
+
+
 if __name__ == "__main__":
     only = set(sys.argv[1:])
     if not only:
@@ -138,3 +153,5 @@ if __name__ == "__main__":
         sr_fixtures()
     if not only or "sfm" in only:
         sfm_fixtures()
+    if not only or "posenet" in only:
+        posenet_fixtures()

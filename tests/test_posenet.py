@@ -256,3 +256,18 @@ def test_trained_proposal_gains_over_plain_icp(ctx):
     assert np.mean(r.proposal_rot_err_deg < 30.0) > 0.9
     assert r.aligned_proposal >= r.aligned_plain
     assert r.pairs_per_s_proposal > 1.2 * r.pairs_per_s_plain
+
+
+def test_oracle_reproduces_the_committed_fixture():
+    """tests/golden/posenet_small.npz (tests/golden/make_golden.py posenet)
+    pins the oracle's forward on seeded weights: winners exactly, values to
+    FP32 rounding."""
+    from pathlib import Path
+    from oracle import posenet as OP
+    g = np.load(Path(__file__).resolve().parent / "golden" / "posenet_small.npz")
+    rng = np.random.default_rng(int(g["seed"]))
+    params = (rng.standard_normal(OP.PARAMS) * 0.05).astype(np.float32)
+    feat, argmax, y, _ = OP.forward(params, g["pts"])
+    np.testing.assert_array_equal(argmax, g["argmax"])
+    np.testing.assert_allclose(feat, g["feat"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(y, g["y"], rtol=1e-5, atol=1e-5)

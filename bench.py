@@ -350,6 +350,19 @@ def turntable_arm(args) -> dict:
         out[batch] = (ok / (total / 1000.0), total / args.steps, ok, res)
     v, ms, ok, res = out[True]
     sizes = [len(c) for c in src]
+    # CPU baseline: the oracle's point-to-plane ICP (own k-d tree, OpenMP over
+    # the host cores) on the same 36 clouds, guesses and parameters
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    hs, ht = [c.download() for c in src], [c.download() for c in tgt]
+    t0 = time.perf_counter()
+    cpu_ok = 0
+    for i in range(views):
+        r = O.icp(hs[i], ht[i], max_corr_dist=0.02, max_iterations=100, transformation_epsilon=1e-10,
+                  euclidean_fitness_epsilon=1e-8, point_to_plane=True, guess=guesses[i].astype(np.float64))
+        cpu_ok += int(r["converged"] and S.rmse(r["transform"], T_gt[i], xyz[i]) <= RMSE_LIMIT)
+    cpu_dt = time.perf_counter() - t0
     ctx.close()
     return {"metric": METRIC, "value": round(v, 3), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
@@ -361,7 +374,10 @@ def turntable_arm(args) -> dict:
                        "pairs_aligned": int(ok), "pairs_timed": views * args.steps,
                        "iterations": [min(r.iterations for r in res), max(r.iterations for r in res)],
                        "sequential_lcr_icp_pairs_per_s": round(out[False][0], 3),
-                       "l2": "flushed between steps (256 MB write)"}}
+                       "l2": "flushed between steps (256 MB write)"},
+            "cpu_baseline": {"value": round(cpu_ok / cpu_dt, 3), "unit": "pairs/s", "cores": cores, "kind": "port",
+                             "sample": f"the 36 pairs through the oracle's point-to-plane ICP (own k-d tree, OpenMP), "
+                                       f"{cpu_ok} aligned in {cpu_dt:.2f} s"}}
 
 
 # ------------------------------------------- learned proposal vs plain ICP
@@ -451,6 +467,34 @@ def proposal_arm(args) -> dict:
         out[arm] = dict(pairs_per_s=ok / (total / 1000.0), ms=total / steps, aligned=ok / steps,
                         fallbacks=fbs / steps, launches=launches // steps, enc=enc)
     clk = clocks.stop()
+    # CPU baseline: the plain method (centroid alignment, then the same two
+    # point-to-plane ICP stages) through the oracle, OpenMP over the host
+    # cores, on the first pairs up to 400k points in all
+    from lowcost3dreconstruction_gb300 import synthetic as S
+    from lowcost3dreconstruction_gb300.core import xyz_of
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    sample, pts_in = [], 0
+    for i in range(npairs):
+        if sample and pts_in + 2 * int(sizes[i]) > 400_000:
+            break
+        sample.append(i)
+        pts_in += 2 * int(sizes[i])
+    hs = [srcs[i].download() for i in sample]
+    ht = [tgts[i].download() for i in sample]
+    t0 = time.perf_counter()
+    cpu_ok = 0
+    for j, i in enumerate(sample):
+        G = np.eye(4)
+        G[:3, 3] = O.centroid(ht[j])[:3].astype(np.float64) - O.centroid(hs[j])[:3].astype(np.float64)
+        r1 = O.icp(hs[j], ht[j], max_corr_dist=0.05, max_iterations=100, transformation_epsilon=1e-8,
+                   euclidean_fitness_epsilon=1e-7, point_to_plane=True, guess=G)
+        r2 = O.icp(hs[j], ht[j], max_corr_dist=0.01, max_iterations=50, transformation_epsilon=1e-9,
+                   euclidean_fitness_epsilon=1e-8, point_to_plane=True, guess=r1["transform"])
+        r = r2 if r2["state"] != 5 else r1
+        cpu_ok += int(r["converged"] and S.rmse(r["transform"], T[i], xyz_of(hs[j])) <= RMSE_LIMIT)
+    cpu_dt = time.perf_counter() - t0
     pr = peaks()
     enc_ms, enc_n = out["proposal"]["enc"]
     flops = 2 * npairs * 1024 * (2 * (64 * 128 + 128 * 1024))
@@ -482,7 +526,11 @@ def proposal_arm(args) -> dict:
                          "unit": "TFLOP/s", "frac": round(achieved / bf16_peak, 4) if achieved else None,
                          "peak_src": pr["src"], "algorithmic_flops_per_launch": flops,
                          "avg_launch_ms": round(enc_ms / enc_n, 5) if enc_n else None, "traffic": None},
-            "e2e": None, "gpu_launches": P["launches"], "clocks": clk}
+            "e2e": None, "gpu_launches": P["launches"], "clocks": clk,
+            "cpu_baseline": {"value": round(cpu_ok / cpu_dt, 3), "unit": "pairs/s", "cores": cores, "kind": "port",
+                             "sample": f"the plain method (centroid alignment, then point-to-plane ICP 5 cm and 1 cm) "
+                                       f"through the oracle on the first {len(sample)} pairs ({pts_in} points), "
+                                       f"{cpu_ok} aligned in {cpu_dt:.2f} s"}}
 
 
 # ------------------------------------------------------ SfM-side filters
@@ -720,6 +768,7 @@ def main():
         out = reference_arm(args, rank)
     elif args.workload == "turntable36":
         build.build_lib()
+        build.build_oracle()
         out = turntable_arm(args) if rank == 0 else None
     elif args.workload == "sfm":
         build.build_lib()
@@ -730,6 +779,7 @@ def main():
         out = sr_arm(args) if rank == 0 else None
     elif args.workload in ("proposal", "large512"):
         build.build_lib()
+        build.build_oracle()
         out = proposal_arm(args) if rank == 0 else None
     else:
         build.build_lib()

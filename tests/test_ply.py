@@ -101,3 +101,30 @@ def test_text_instances_split_over_lines(tmp_path):
     np.testing.assert_array_equal(p["x"], np.float32([1.5, -4.0]))
     np.testing.assert_array_equal(p["y"], np.float32([2.5, 0.5]))
     np.testing.assert_array_equal(p["z"], np.float32([3.5, 6.0]))
+
+
+def _meshlab_header(n: int, fmt: str) -> bytes:
+    """The layout meshlabserver writes between the tools in alignment.sh
+    (:99-100, :110): VCG vertex properties with alpha, and an empty face list."""
+    return (f"ply\nformat {fmt} 1.0\ncomment VCGLIB generated\nelement vertex {n}\n"
+            "property float x\nproperty float y\nproperty float z\n"
+            "property float nx\nproperty float ny\nproperty float nz\n"
+            "property uchar red\nproperty uchar green\nproperty uchar blue\nproperty uchar alpha\n"
+            "element face 0\nproperty list uchar int vertex_indices\nend_header\n").encode()
+
+
+@pytest.mark.parametrize("fmt", ["binary_little_endian", "binary_big_endian"])
+def test_meshlab_vertex_layout(tmp_path, fmt):
+    n = 7
+    rng = np.random.default_rng(5)
+    xyz = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    nrm = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    rgba = rng.integers(0, 256, (n, 4)).astype(np.uint8)
+    e = "<f4" if fmt == "binary_little_endian" else ">f4"
+    body = b"".join(xyz[i].astype(e).tobytes() + nrm[i].astype(e).tobytes() + rgba[i].tobytes() for i in range(n))
+    (tmp_path / "m.ply").write_bytes(_meshlab_header(n, fmt) + body)
+    p = L.read_ply(tmp_path / "m.ply")
+    assert len(p) == n
+    np.testing.assert_array_equal(np.c_[p["x"], p["y"], p["z"]], xyz)
+    np.testing.assert_array_equal(np.c_[p["normal_x"], p["normal_y"], p["normal_z"]], nrm)
+    np.testing.assert_array_equal(np.c_[p["r"], p["g"], p["b"]], rgba[:, :3])

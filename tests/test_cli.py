@@ -196,3 +196,13 @@ def test_pose_proposal_drops_into_the_coarse_stage(tmp_path, ctx, units):
     (tmp_path / "t.txt").write_text("\n".join(lines[2:]) + "\n")   # sed -i '1,2d'
     assert run("transform", "-i", tmp_path / "Q.ply", "-o", tmp_path / "q2.ply", "-t", tmp_path / "t.txt").returncode == 0
     np.testing.assert_allclose(L.read_ply(tmp_path / "q2.ply")["x"], L.read_ply(tmp_path / "reg.ply")["x"], atol=1e-4)
+
+
+@pytest.mark.parametrize("form", [["--input={f}", "--output={o}"], ["-i{f}", "-o", "{o}"], ["-i", "{f}", "--output", "{o}"]])
+def test_option_spellings(tmp_path, form):
+    """boost::program_options spellings the scripts may use: --name=value,
+    -xvalue and separate values all reach the same load step."""
+    args = [a.format(f=tmp_path / "nope.ply", o=tmp_path / "o.ply") for a in form]
+    r = run("outlier_removal", *args)
+    assert r.returncode == 255
+    assert f"Couldn't load input point cloud: {tmp_path / 'nope.ply'}" in (r.stdout + r.stderr)

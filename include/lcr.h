@@ -282,7 +282,10 @@ LCR_API lcr_status lcr_plane_segment(lcr_ctx* ctx, const lcr_cloud* in, double t
  * zero-eliminated mean and resampled back by Lanczos-4, rounded and
  * saturated to uint16 (depth_out [height][width]).  Optional outputs: warps
  * [frames][6] (2x3 row-major inverse maps, frame 0 the identity), minmax the
- * observed nonzero range, iterations [frames]. */
+ * observed nonzero range, iterations [frames].  LCR_ERR_INVALID_ARG unless
+ * 1 <= frames <= 1024, 1 <= factor <= 16, width * height <= 2^26,
+ * ecc_iterations >= 0 and ecc_epsilon >= 0.  Synchronous: the outputs are
+ * ready when the call returns. */
 typedef struct lcr_sr_params {
   int width, height, frames;
   int factor;          /* resample factor (the tool's default 4) */

@@ -138,6 +138,8 @@ LCR_API lcr_status lcr_backproject_device(lcr_ctx* ctx, const void* d_depth, con
  * device memory, capacity records), and their number to *d_count (a
  * caller-owned device uint32); records past capacity are not written, so
  * compare *d_count with capacity (capacity = width*height always suffices).
+ * d_points must be 16-byte aligned and d_count 4-byte aligned (the records are
+ * written as 16-byte vectors); other pointers return LCR_ERR_INVALID_ARG.
  * The points are the ones lcr_backproject_device gives, bit for bit.  The
  * scratch (the fused image of a burst and the compaction's block counts) is
  * one static device buffer of 1.2 MB per device, so width*height may be at
@@ -145,9 +147,12 @@ LCR_API lcr_status lcr_backproject_device(lcr_ctx* ctx, const void* d_depth, con
  * in the scratch carries over between calls (every block count is written
  * before it is read), so it needs no clearing.  The first call on a device
  * looks up the scratch's address (cudaGetSymbolAddress): make it before any
- * stream capture.  All contexts on a device share the scratch: calls that
- * overlap in time (other streams, contexts or threads) race on it.  Returns
- * without synchronising; the results are ready when the context's stream is. */
+ * stream capture.  The address is kept for the life of the process: after a
+ * cudaDeviceReset (which unloads the module and its scratch) this entry point
+ * must not be called again in that process.  All contexts on a device share
+ * the scratch: calls that overlap in time (other streams, contexts or
+ * threads) race on it.  Returns without synchronising; the results are ready
+ * when the context's stream is. */
 LCR_API lcr_status lcr_backproject_into(lcr_ctx* ctx, const void* d_depth, const lcr_depth_params* p,
                                         lcr_point* d_points, size_t capacity, uint32_t* d_count);
 /* The fused (zero-eliminated mean) depth image alone, host in/out: uint16 for
@@ -344,6 +349,33 @@ typedef struct lcr_synth_params {
 LCR_API lcr_status lcr_synthetic_pairs(lcr_ctx* ctx, uint64_t seed, size_t npairs, int points,
                                        const lcr_synth_params* p, lcr_cloud** src, lcr_cloud** tgt,
                                        float* transforms);
+
+/* Depth images of the same objects (the seed and pair index pick the object,
+ * its views and the exact transform as lcr_synthetic_pairs does).  Each
+ * object's distance from the camera is distance[i] (m) when distance is given;
+ * else, when points is given, the distance at which the object's mean
+ * projected area (a quarter of its surface) covers points[i] pixels of this
+ * camera, within [0.4, 8] m; with neither, 1 m.  Images:
+ * the source and the target view of pair i are images 2i and 2i+1 of d_depth
+ * (caller-owned device memory, [2 npairs][height][width]), uint16 mm for
+ * LCR_DEPTH_KINECT_V1, float32 mm for LCR_DEPTH_KINECT_V2 and
+ * LCR_DEPTH_PINHOLE_F32, 0 where no surface is seen.  The camera follows the
+ * back-projection's conventions for the model (the reference's x = z(j-cx)/fx,
+ * y = -z(i-cy)/fy looking down -z; Kinect v2 pixel centres at +0.5), so
+ * lcr_backproject_device of an image gives points on the object's surface.
+ * Surface samples are z-buffered, samples_per_pixel (0: 6) per frontal pixel
+ * footprint; noise adds sigma = 1.5 mm (z/1 m)^2 per pixel.  transforms
+ * [npairs][16] receives the exact source-to-target transforms.
+ * Synchronises before returning.  npairs <= 32767. */
+typedef struct lcr_render_params {
+  int model;                 /* LCR_DEPTH_KINECT_V1, LCR_DEPTH_KINECT_V2 or LCR_DEPTH_PINHOLE_F32 */
+  int width, height;
+  double fx, fy, cx, cy;
+  float samples_per_pixel;
+} lcr_render_params;
+LCR_API lcr_status lcr_synthetic_depth(lcr_ctx* ctx, uint64_t seed, size_t npairs, const lcr_synth_params* p,
+                                       const lcr_render_params* camera, const float* distance,
+                                       const float* points, void* d_depth, float* transforms);
 
 /* Alignment error of n clouds: out[i] = RMS over the finite points p of
  * clouds[i] of |Ta_i p - Tb_i p| (FP64; Ta, Tb [n][16] row-major), the RMSE

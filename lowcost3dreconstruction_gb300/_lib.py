@@ -85,6 +85,11 @@ class SynthParams(C.Structure):
     _fields_ = [("yaw_deg", C.c_float), ("tilt_deg", C.c_float), ("translation", C.c_float), ("noise", C.c_int)]
 
 
+class RenderParams(C.Structure):
+    _fields_ = [("model", C.c_int), ("width", C.c_int), ("height", C.c_int), ("fx", C.c_double), ("fy", C.c_double),
+                ("cx", C.c_double), ("cy", C.c_double), ("samples_per_pixel", C.c_float)]
+
+
 class Tune(C.Structure):
     _fields_ = [("sor_warps", C.c_int), ("normals_warps", C.c_int), ("icp_blocks_per_sm", C.c_int)]
 
@@ -150,6 +155,8 @@ _SIGS = {
     "lcr_autotune": (C.c_int, [_VP, _VP, _VP, C.c_char_p, C.POINTER(TuneReport)]),
     "lcr_synthetic_pairs": (C.c_int, [_VP, C.c_uint64, C.c_size_t, C.c_int, C.POINTER(SynthParams), _VP, _VP,
                                       _VP]),
+    "lcr_synthetic_depth": (C.c_int, [_VP, C.c_uint64, C.c_size_t, C.POINTER(SynthParams), C.POINTER(RenderParams),
+                                      _VP, _VP, _VP, _VP]),
     "lcr_rmse_batch": (C.c_int, [_VP, _VP, C.c_size_t, _VP, _VP, _VP]),
     "lcr_posenet_create": (C.c_int, [_VP, C.c_uint64, C.POINTER(_VP)]),
     "lcr_posenet_free": (C.c_int, [_VP, _VP]),

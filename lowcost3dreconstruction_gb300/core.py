@@ -308,6 +308,25 @@ class Context:
         return ([Cloud(self, C.c_void_p(hs[i])) for i in range(npairs)],
                 [Cloud(self, C.c_void_p(ht[i])) for i in range(npairs)], T[:npairs].reshape(npairs, 4, 4))
 
+    def synthetic_depth(self, seed: int, npairs: int, model: int, width: int, height: int, fx: float, fy: float,
+                        cx: float, cy: float, dev_ptr: int, distance: np.ndarray | None = None,
+                        points: np.ndarray | None = None, yaw_deg: float = 180.0, tilt_deg: float = 20.0,
+                        translation: float = 0.1, noise: bool = True, samples_per_pixel: float = 0.0) -> np.ndarray:
+        """lcr_synthetic_depth: renders the source and target views of npairs
+        objects into the device buffer at dev_ptr ([2 npairs][height][width],
+        uint16 mm for Kinect v1, float32 mm otherwise) at the given distances,
+        or at distances that give about `points` pixels per view; returns the
+        exact source-to-target transforms [n][4][4]."""
+        T = np.zeros((max(npairs, 1), 16), dtype=np.float32)
+        p = L.SynthParams(yaw_deg, tilt_deg, translation, 1 if noise else 0)
+        cam = L.RenderParams(model, width, height, fx, fy, cx, cy, samples_per_pixel)
+        d = None if distance is None else np.ascontiguousarray(distance, dtype=np.float32)
+        w = None if points is None else np.ascontiguousarray(points, dtype=np.float32)
+        self._check(self.lib.lcr_synthetic_depth(self.h, seed, npairs, C.byref(p), C.byref(cam),
+                                                 L.ptr(d) if d is not None else None,
+                                                 L.ptr(w) if w is not None else None, C.c_void_p(dev_ptr), L.ptr(T)))
+        return T[:npairs].reshape(npairs, 4, 4)
+
     def rmse_batch(self, clouds: list[Cloud], Ta: np.ndarray, Tb: np.ndarray) -> np.ndarray:
         """lcr_rmse_batch: RMS over each cloud's points of |Ta p - Tb p|."""
         n = len(clouds)

@@ -257,6 +257,9 @@ lcr_status lcr_backproject_into(lcr_ctx* ctx, const void* d_depth, const lcr_dep
   API_BEGIN(ctx)
   check_depth(p);
   REQUIRE(d_depth && d_count && (d_points || capacity == 0), "null argument");
+  // the records are stored as two 16-byte vectors each, the count as one word
+  REQUIRE(reinterpret_cast<uintptr_t>(d_points) % 16 == 0 && reinterpret_cast<uintptr_t>(d_count) % 4 == 0,
+          "d_points must be 16-byte aligned and d_count 4-byte aligned");
   backproject_into_run(ctx, d_depth, p, d_points, capacity, d_count);
   API_END(ctx)
   return LCR_OK;
@@ -708,6 +711,31 @@ lcr_status lcr_synthetic_pairs(lcr_ctx* ctx, uint64_t seed, size_t npairs, int p
     }
     throw;
   }
+  API_END(ctx)
+  return LCR_OK;
+}
+
+lcr_status lcr_synthetic_depth(lcr_ctx* ctx, uint64_t seed, size_t npairs, const lcr_synth_params* p,
+                               const lcr_render_params* cam, const float* distance, const float* points,
+                               void* d_depth, float* transforms) {
+  API_BEGIN(ctx)
+  REQUIRE(p && cam && (npairs == 0 || (d_depth && transforms)), "null argument");
+  REQUIRE(npairs <= 32767, "too many pairs (%zu)", npairs);
+  REQUIRE(cam->model == LCR_DEPTH_KINECT_V1 || cam->model == LCR_DEPTH_KINECT_V2 ||
+              cam->model == LCR_DEPTH_PINHOLE_F32,
+          "unknown depth model %d", cam->model);
+  REQUIRE(cam->width >= 1 && cam->height >= 1 && static_cast<long long>(cam->width) * cam->height <= (1ll << 26),
+          "image size %dx%d out of range", cam->width, cam->height);
+  REQUIRE(cam->fx > 0 && cam->fy > 0 && std::isfinite(cam->cx) && std::isfinite(cam->cy), "bad intrinsics");
+  REQUIRE(cam->samples_per_pixel >= 0 && cam->samples_per_pixel <= 64, "samples_per_pixel out of [0, 64]");
+  REQUIRE(p->yaw_deg >= 0.f && p->tilt_deg >= 0.f && p->translation >= 0.f, "ranges must be non-negative");
+  if (distance)
+    for (size_t i = 0; i < npairs; ++i)
+      REQUIRE(distance[i] >= 0.2f && distance[i] <= 20.f, "distance[%zu] out of [0.2, 20] m", i);
+  REQUIRE(!(distance && points), "give distance or points, not both");
+  if (points)
+    for (size_t i = 0; i < npairs; ++i) REQUIRE(points[i] >= 1.f, "points[%zu] must be >= 1", i);
+  synth_depth(ctx, seed, static_cast<int>(npairs), p, cam, distance, points, d_depth, transforms);
   API_END(ctx)
   return LCR_OK;
 }

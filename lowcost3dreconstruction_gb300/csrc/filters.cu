@@ -579,6 +579,24 @@ __global__ void k_crop(IndexView tgt, IndexView src, double r, uint8_t* __restri
   if (qv && v.found) removed[__float_as_uint(p.w)] = 1;
 }
 
+// PCL's CropBox (accumulate_clouds.cpp:103-110, negative mode) drops a source
+// point that is not finite, and a box built on a non-finite target point holds
+// every source point: each comparison with a NaN bound is false, so no point
+// tests as outside it.  Pass 1 flags a non-finite target point; pass 2 starts
+// the removed flags from that and from the source point's own finiteness.
+__global__ void k_any_nonfinite(const float4* __restrict__ p, size_t n, int* __restrict__ flag) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const bool bad = i < n && !finite3(p[i].x, p[i].y, p[i].z);
+  if (__any_sync(LCR_FULL, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+__global__ void k_crop_init(const float4* __restrict__ src, size_t n, const int* __restrict__ tgt_bad,
+                            uint8_t* __restrict__ removed) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  removed[i] = (*tgt_bad || !finite3(src[i].x, src[i].y, src[i].z)) ? 1 : 0;
+}
+
 size_t list_smem(int nw, int K) { return nw * knn_warp_bytes(K); }
 
 constexpr int kListMaxK = 64;  // neighbour lists handed to the inliers hold at most this many keys
@@ -788,8 +806,15 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
 
 void crop_run(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, double radius, uint8_t* d_removed) {
   if (src->n == 0) return;
-  CUDA_TRY(cudaMemsetAsync(d_removed, 0, src->n, ctx->stream));
-  if (tgt->n == 0) return;
+  if (tgt->n == 0) {  // no box at all: nothing is cropped, non-finite points included
+    CUDA_TRY(cudaMemsetAsync(d_removed, 0, src->n, ctx->stream));
+    return;
+  }
+  int* bad = static_cast<int*>(dev_alloc(ctx, 256));
+  CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream));
+  LCR_LAUNCH(ctx, k_any_nonfinite, static_cast<unsigned>((tgt->n + 255) / 256), 256, 0, tgt->xyz, tgt->n, bad);
+  LCR_LAUNCH(ctx, k_crop_init, static_cast<unsigned>((src->n + 255) / 256), 256, 0, src->xyz, src->n, bad, d_removed);
+  dev_free(ctx, bad);
   const IndexView tv = cloud_index(ctx, tgt).v;
   const IndexView sv = cloud_index(ctx, src).v;
   LCR_LAUNCH(ctx, k_crop, (sv.nleaf + 7) / 8, 256, 0, tv, sv, radius, d_removed);

@@ -50,26 +50,40 @@ int run(int argc, char* argv[], bool kv2) {
     const std::string name = desc.str("capture_name");
     long step = desc.integer("capture_step"), ncap = desc.integer("num_captures");
     const long sr_size = desc.integer("sr_size"), factor = desc.integer("resample_factor");
-    if (factor <= 0) {
-      std::cout << "The command option 'resample_factor', must be bigger than zero" << std::endl;
-      return -1;
+    const int picks = static_cast<int>(desc.count("view_angle")) + static_cast<int>(desc.count("top")) +
+                      static_cast<int>(desc.count("bottom"));
+    // Option rules, checked in this order.  A rule that holds prints its
+    // message; kStop ends the tool with -1 (message on stdout, as the capture
+    // tools print it), kError throws (stderr), kNote only informs.
+    enum Action { kStop, kError, kNote };
+    struct Rule {
+      bool holds;
+      Action action;
+      const char* message;
+    };
+    const Rule rules[] = {
+        {factor <= 0, kStop, "The command option 'resample_factor', must be bigger than zero"},
+        {sr_size <= 0, kError, "sr_size must be positive"},
+        {step < 0 || ncap < 0, kError, "capture_step and num_captures must not be negative"},
+        {picks > 1, kStop,
+         "The command options: 'view_angle', 'top' and 'bottom' can not be used together. Choose only one of them"},
+        {picks == 1, kNote,
+         "When using the command options: 'view_angle', 'top' or 'bottom', the options 'capture_step' and "
+         "'num_captures' are ignored"},
+    };
+    for (const Rule& r : rules) {
+      if (!r.holds) continue;
+      if (r.action == kError) throw std::logic_error(r.message);
+      std::cout << r.message << std::endl;
+      if (r.action == kStop) return -1;
     }
-    if (sr_size <= 0) throw std::logic_error("sr_size must be positive");
-    if (step < 0 || ncap < 0) throw std::logic_error("capture_step and num_captures must not be negative");
+    const bool single = picks == 1;
     std::string view;
-    const bool va = desc.count("view_angle"), top = desc.count("top"), bottom = desc.count("bottom");
-    const bool single = va || top || bottom;
     if (single) {
-      if ((va && top) || (va && bottom) || (top && bottom)) {
-        std::cout << "The command options: 'view_angle', 'top' and 'bottom'"
-                  << " can not be used together. Choose only one of them" << std::endl;
-        return -1;
-      }
-      std::cout << "When using the command options: 'view_angle', 'top' or 'bottom'"
-                << ", the options 'capture_step' and 'num_captures' are ignored" << std::endl;
       step = 0;
       ncap = 1;
-      view = va ? std::to_string(desc.integer("view_angle") % 360) : (top ? "top" : "bottom");
+      view = desc.count("view_angle") ? std::to_string(desc.integer("view_angle") % 360)
+                                      : (desc.count("top") ? "top" : "bottom");
     }
     std::cout << "Capture name: " << name << std::endl;
     if (single) {

@@ -234,6 +234,8 @@ void gather_cloud(lcr_ctx* ctx, const lcr_cloud* in, const uint32_t* idx, int n,
 // RMS over each cloud's finite points of |Ta p - Tb p| (synth.cu); host Ta, Tb [n][16], out [n].
 void rmse_batch(lcr_ctx* ctx, const lcr_cloud* const* clouds, int n, const double* Ta, const double* Tb, double* out);
 // Seeded synthetic capture pairs (synth.cu); allocates src[i], tgt[i].
+void synth_depth(lcr_ctx* ctx, uint64_t seed, int npairs, const lcr_synth_params* prm, const lcr_render_params* cam,
+                 const float* distance, const float* points, void* d_out, float* transforms);
 void synth_pairs(lcr_ctx* ctx, uint64_t seed, int npairs, int npts, const lcr_synth_params* prm, lcr_cloud** src,
                  lcr_cloud** tgt, float* transforms);
 // Device-side bounding box of the finite points of an xyz array: out[0] = lo, out[1] = hi.

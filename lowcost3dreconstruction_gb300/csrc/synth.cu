@@ -130,8 +130,14 @@ __device__ void surface_point(const Part& p, uint64_t& s, float* o, float* n) {
 }
 
 // One thread per pair: the object and the two view poses.
+// dist gives each pair's camera-to-object distance; else want gives the
+// visible pixels wanted per view of a camera with focal lengths fx fy
+// (fxfy = fx * fy): the distance at which the object's mean projected area
+// (a quarter of its surface, Cauchy's formula for a convex body) covers that
+// many pixels, within [0.4, 8] m; with neither, 1 m.
 __global__ void k_synth_objects(uint64_t seed, int npairs, lcr_synth_params prm, SynthObject* __restrict__ objs,
-                                float* __restrict__ T) {
+                                float* __restrict__ T, const float* __restrict__ dist = nullptr,
+                                const float* __restrict__ want = nullptr, float fxfy = 0.f) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= npairs) return;
   uint64_t s = mix(seed * 0x2545f4914f6cdd1dull + static_cast<uint64_t>(b) * 0x9e3779b97f4a7c15ull + 1);
@@ -188,10 +194,13 @@ __global__ void k_synth_objects(uint64_t seed, int npairs, lcr_synth_params prm,
     o.cum[k] = acc;
   }
   o.cum[3] = 1.0f;
-  // source view: the object turned about its vertical axis, 1 m in front of the camera
+  // source view: the object turned about its vertical axis, in front of the camera
   float Rs[9];
   rot_y(2.0f * 3.14159265f * uni(s), Rs);
-  const float cs[3] = {0.f, 0.f, -1.0f};
+  float z = 1.0f;
+  if (dist) z = dist[b];
+  else if (want) z = fminf(fmaxf(sqrtf(0.25f * tot * fxfy / fmaxf(want[b], 1.f)), 0.4f), 8.0f);
+  const float cs[3] = {0.f, 0.f, -z};
   // relative motion about the object centre: yaw, tilt, translation
   float Ryaw[9], Rtilt[9], Rrel[9], Rt[9];
   rot_y((2.0f * uni(s) - 1.0f) * prm.yaw_deg * d2r, Ryaw);
@@ -295,7 +304,131 @@ __global__ void __launch_bounds__(256) k_rmse(const float4* const* __restrict__ 
   if (threadIdx.x == 0) out[c] = red[1][0] > 0 ? sqrt(red[0][0] / red[1][0]) : 0.0;
 }
 
+// ---------------------------------------------------------- depth images
+// The same objects as a depth camera sees them.  Surface samples of each view
+// (back-facing and covered ones dropped, as above) are splatted into a
+// z-buffer, the smallest depth per pixel winning.  A sample gives the depth of
+// its pixel's centre ray from its tangent plane, so planar faces render
+// exactly and curved ones to second order; at grazing angles (or where the
+// plane would move the depth by more than 2 cm) the sample's own depth is
+// used.  Samples per view: spp per frontal pixel footprint (z/f)^2 of the
+// object's whole area, so a visible pixel is missed with probability about
+// exp(-spp/2) on a frontal surface and less where it is inclined.
+struct RenderCam {
+  int w, h;
+  float fx, fy, cx, cy;
+  float off;  // 0.5 for the Kinect v2 pixel-centre convention (kinect2.h:262-265), 0 otherwise
+  float spp;
+};
+
+__global__ void k_render_splat(uint64_t seed, const SynthObject* __restrict__ objs, RenderCam cam,
+                               uint32_t* __restrict__ zbuf) {
+  const int v = blockIdx.y, b = v >> 1;
+  const SynthObject& o = objs[b];
+  const float* P = (v & 1) ? o.Pt : o.Ps;
+  const float zc = fmaxf(-P[11], 0.05f);
+  float area = 0.f;
+  for (int k = 0; k < 4; ++k) area += o.part[k].area;
+  const long long m = min(static_cast<long long>(cam.spp * area * cam.fx * cam.fy / (zc * zc)), 1ll << 28);
+  const size_t plane = static_cast<size_t>(cam.w) * cam.h;
+  uint32_t* zb = zbuf + static_cast<size_t>(v) * plane;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < m;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    uint64_t s = mix(seed ^ mix((static_cast<uint64_t>(v) << 36) ^ static_cast<uint64_t>(i) ^ 0x6a09e667f3bcc909ull));
+    const float u = uni(s);
+    int k = 0;
+    while (k < 3 && u > o.cum[k]) ++k;
+    float ob[3], on[3];
+    surface_point(o.part[k], s, ob, on);
+    bool hidden = false;
+    for (int j = 0; j < 4 && !hidden; ++j)
+      if (j != k && inside(o.part[j], ob)) hidden = true;
+    if (hidden) continue;
+    float pc[3], pn[3];
+    for (int r = 0; r < 3; ++r) {
+      pc[r] = P[4 * r] * ob[0] + P[4 * r + 1] * ob[1] + P[4 * r + 2] * ob[2] + P[4 * r + 3];
+      pn[r] = P[4 * r] * on[0] + P[4 * r + 1] * on[1] + P[4 * r + 2] * on[2];
+    }
+    if (pn[0] * pc[0] + pn[1] * pc[1] + pn[2] * pc[2] >= 0.f) continue;  // faces away from the camera
+    const float depth = -pc[2];
+    if (!(depth > 0.05f)) continue;
+    const int col = __float2int_rn(pc[0] * cam.fx / depth + cam.cx - cam.off);
+    const int row = __float2int_rn(-pc[1] * cam.fy / depth + cam.cy - cam.off);
+    if (col < 0 || col >= cam.w || row < 0 || row >= cam.h) continue;
+    // the pixel centre's ray X = t d, d = ((col - cx + off)/fx, -(row - cy + off)/fy, -1): depth t
+    const float dx = (static_cast<float>(col) - cam.cx + cam.off) / cam.fx;
+    const float dy = -(static_cast<float>(row) - cam.cy + cam.off) / cam.fy;
+    const float den = pn[0] * dx + pn[1] * dy - pn[2];
+    float t = depth;
+    if (fabsf(den) > 0.2f * sqrtf(dx * dx + dy * dy + 1.f)) {
+      const float tp = (pn[0] * pc[0] + pn[1] * pc[1] + pn[2] * pc[2]) / den;
+      if (fabsf(tp - depth) < 0.02f) t = tp;
+    }
+    atomicMin(zb + static_cast<size_t>(row) * cam.w + col, __float_as_uint(t));  // positive floats order as integers
+  }
+}
+
+// z-buffer -> depth image: model 0 uint16 mm (rounded, saturated), else float
+// mm; Kinect noise sigma = 1.5 mm (z / 1 m)^2 per pixel when noise is set;
+// pixels without surface are 0.
+__global__ void k_render_finish(uint64_t seed, const uint32_t* __restrict__ zbuf, int npix, int f32, int noise,
+                                void* __restrict__ out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npix) return;
+  const size_t at = static_cast<size_t>(blockIdx.y) * npix + p;
+  const float z = __uint_as_float(zbuf[at]);
+  float mm = 0.f;
+  if (z < 1e30f) {
+    mm = 1000.f * z;
+    if (noise) {
+      uint64_t s = mix(seed ^ mix((static_cast<uint64_t>(blockIdx.y) << 33) ^ static_cast<uint64_t>(p) ^
+                                  0xbb67ae8584caa73bull));
+      mm += 1.5f * z * z * gauss(s);
+    }
+  }
+  if (f32) {
+    static_cast<float*>(out)[at] = fmaxf(mm, 0.f);
+  } else {
+    static_cast<uint16_t*>(out)[at] = static_cast<uint16_t>(fminf(fmaxf(rintf(mm), 0.f), 65535.f));
+  }
+}
+
 }  // namespace
+
+void synth_depth(lcr_ctx* ctx, uint64_t seed, int npairs, const lcr_synth_params* prm, const lcr_render_params* cam,
+                 const float* distance, const float* points, void* d_out, float* transforms) {
+  if (npairs == 0) return;
+  const size_t plane = static_cast<size_t>(cam->width) * cam->height;
+  const size_t zbytes = plane * 4 * 2 * static_cast<size_t>(npairs);
+  const size_t head = (npairs * sizeof(SynthObject) + npairs * 64 + npairs * 4 + 255) & ~static_cast<size_t>(255);
+  char* d = static_cast<char*>(dev_alloc(ctx, head + zbytes));
+  auto* objs = reinterpret_cast<SynthObject*>(d);
+  auto* T = reinterpret_cast<float*>(d + npairs * sizeof(SynthObject));
+  auto* dd = reinterpret_cast<float*>(d + npairs * sizeof(SynthObject) + npairs * 64);
+  auto* zb = reinterpret_cast<uint32_t*>(d + head);
+  const float* per_pair = distance ? distance : points;
+  if (per_pair) CUDA_TRY(cudaMemcpyAsync(dd, per_pair, npairs * 4ull, cudaMemcpyHostToDevice, ctx->stream));
+  CUDA_TRY(cudaMemsetAsync(zb, 0x7f, zbytes, ctx->stream));  // 0x7f7f7f7f: a float above any depth
+  LCR_LAUNCH(ctx, k_synth_objects, (npairs + 127) / 128, 128, 0, seed, npairs, *prm, objs, T,
+             distance ? static_cast<const float*>(dd) : nullptr, points ? static_cast<const float*>(dd) : nullptr,
+             static_cast<float>(cam->fx * cam->fy));
+  RenderCam rc;
+  rc.w = cam->width;
+  rc.h = cam->height;
+  rc.fx = static_cast<float>(cam->fx);
+  rc.fy = static_cast<float>(cam->fy);
+  rc.cx = static_cast<float>(cam->cx);
+  rc.cy = static_cast<float>(cam->cy);
+  rc.off = cam->model == LCR_DEPTH_KINECT_V2 ? 0.5f : 0.f;
+  rc.spp = cam->samples_per_pixel > 0 ? cam->samples_per_pixel : 6.f;
+  LCR_LAUNCH(ctx, k_render_splat, dim3(64, 2 * npairs), 256, 0, seed, objs, rc, zb);
+  const int f32 = cam->model == LCR_DEPTH_KINECT_V1 ? 0 : 1;
+  LCR_LAUNCH(ctx, k_render_finish, dim3(static_cast<unsigned>((plane + 255) / 256), 2 * npairs), 256, 0, seed, zb,
+             static_cast<int>(plane), f32, prm->noise, d_out);
+  CUDA_TRY(cudaMemcpyAsync(transforms, T, npairs * 64ull, cudaMemcpyDeviceToHost, ctx->stream));
+  sync(ctx);
+  dev_free(ctx, d);
+}
 
 void rmse_batch(lcr_ctx* ctx, const lcr_cloud* const* clouds, int n, const double* Ta, const double* Tb,
                 double* out) {

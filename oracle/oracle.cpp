@@ -1005,11 +1005,17 @@ size_t orc_crop_redundant(const orc_point* src, size_t ns, const orc_point* tgt,
     if (!finite3(tgt[j])) continue;
     grid[key(cellof(tgt[j].x), cellof(tgt[j].y), cellof(tgt[j].z))].push_back(static_cast<int>(j));
   }
+  /* PCL's CropBox (negative) drops a non-finite source point, and a box on a
+   * non-finite target point holds every point (no NaN comparison says
+   * "outside"): with any target point present, both remove. */
+  bool tgt_bad = false;
+  for (size_t j = 0; j < nt; ++j) tgt_bad = tgt_bad || !finite3(tgt[j]);
   size_t nrem = 0;
 #pragma omp parallel for schedule(dynamic, 512) reduction(+ : nrem) num_threads(nthreads())
   for (long long i = 0; i < static_cast<long long>(ns); ++i) {
     removed[i] = 0;
     const orc_point& p = src[i];
+    if (nt > 0 && (tgt_bad || !finite3(p))) { removed[i] = 1; ++nrem; continue; }
     if (!finite3(p)) continue;
     long long cx = cellof(p.x), cy = cellof(p.y), cz = cellof(p.z);
     bool hit = false;

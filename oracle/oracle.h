@@ -111,7 +111,10 @@ int orc_correspondences(const orc_point* src, size_t ns, const orc_point* tgt, s
                         const double* T, double max_corr_dist, int32_t* idx, float* dist);
 
 /* CropBox-radius redundancy mask (accumulate_clouds.cpp:100-111): removed[i]=1 when some target
- * point q has float(q-r) <= p <= float(q+r) on all axes. Returns the removed count. */
+ * point q has float(q-r) <= p <= float(q+r) on all axes; with at least one target point, a
+ * non-finite source point, or every source point when some target point is non-finite (CropBox
+ * drops non-finite points, and no NaN comparison puts a point outside a NaN box). Returns the
+ * removed count. */
 size_t orc_crop_redundant(const orc_point* src, size_t ns, const orc_point* tgt, size_t nt,
                           double radius, uint8_t* removed);
 

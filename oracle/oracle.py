@@ -235,6 +235,46 @@ def centroid(pts) -> np.ndarray:
     return c
 
 
+def centroid_align(src, tgt, roll=0.0, pitch=0.0, yaw=0.0, elevation=0.0, exact: bool = False):
+    """centroid_align.cpp:102-130: translate the source by -c_src, rotate it by
+    R = Rx(roll) Ry(pitch) Rz(yaw) (degrees, AngleAxis products in that order),
+    translate by c_tgt, then by (0, elevation, 0).  exact=False restates PCL's
+    float path: compute3DCentroid summed sequentially in FP32 and four
+    transformPointCloudWithNormals passes with float matrices.  exact=True
+    forms the centroids and the composed matrix in FP64 and applies it once.
+    Returns (moved cloud, composed FP64 matrix)."""
+    src, tgt = _pts(src), _pts(tgt)
+    d2r = np.pi / 180.0
+    a, b, c = roll * d2r, pitch * d2r, yaw * d2r
+    Rx = np.array([[1, 0, 0], [0, np.cos(a), -np.sin(a)], [0, np.sin(a), np.cos(a)]])
+    Ry = np.array([[np.cos(b), 0, np.sin(b)], [0, 1, 0], [-np.sin(b), 0, np.cos(b)]])
+    Rz = np.array([[np.cos(c), -np.sin(c), 0], [np.sin(c), np.cos(c), 0], [0, 0, 1]])
+    R = Rx @ Ry @ Rz
+
+    def tr(t):
+        m = np.eye(4)
+        m[:3, 3] = t
+        return m
+
+    rot = np.eye(4)
+    rot[:3, :3] = R
+    if exact:
+        def c64(p):
+            f = np.isfinite(p["x"]) & np.isfinite(p["y"]) & np.isfinite(p["z"])
+            return np.c_[p["x"][f], p["y"][f], p["z"][f]].astype(np.float64).mean(0)
+        cs, ct = c64(src), c64(tgt)
+    else:
+        cs, ct = centroid(src)[:3].astype(np.float64), centroid(tgt)[:3].astype(np.float64)
+    steps = [tr(-cs), rot, tr(ct), tr((0.0, elevation, 0.0))]
+    M = steps[3] @ steps[2] @ steps[1] @ steps[0]
+    if exact:
+        return transform(src, M.astype(np.float32)), M
+    out = src
+    for m in steps:
+        out = transform(out, m.astype(np.float32))
+    return out, M
+
+
 def svd3(a):
     a = np.ascontiguousarray(a, dtype=np.float64).reshape(9)
     u, s, v = np.zeros(9), np.zeros(3), np.zeros(9)

@@ -353,13 +353,15 @@ def test_icp_p2p_matches_oracle(ctx, cfg0):
     o = O.icp(s, t, max_corr_dist=0.05, max_iterations=50, transformation_epsilon=1e-8)
     assert g.converged == o["converged"]
     assert abs(g.iterations - o["iterations"]) <= 1
-    # 50 iterations of a slowly creeping point-to-point trajectory (the sphere is
-    # symmetric about the motion axis): round-off differences of the reductions
-    # shift where the trajectory stops, so the end points agree to 1e-5 rad and
-    # 1e-5 x extent; per-iteration agreement is tested tightly below.
-    _assert_transform_close(g.transform64, o["transform"], _extent(s), rot_tol=1e-5, trans_rel=1e-5,
-                            at=_centroid(s))
+    _assert_transform_close(g.transform64, o["transform"], _extent(s), at=_centroid(s))
     assert abs(g.fitness - o["fitness"]) <= 1e-4 * o["fitness"]
+    # The end point of this slowly creeping trajectory (the sphere is symmetric
+    # about the motion axis) moves by more than the GPU-oracle gap when the
+    # oracle itself starts 1e-7 rad away: the gap is round-off, amplified.
+    Gp = S.rigid(S.rot_y(np.rad2deg(1e-7)), (0.0, 0.0, 0.0))
+    o2 = O.icp(s, t, max_corr_dist=0.05, max_iterations=50, transformation_epsilon=1e-8, guess=Gp)
+    spread = _rot_angle(o2["transform"], o["transform"])
+    assert _rot_angle(g.transform64, o["transform"]) <= max(spread, 1e-6)
 
 
 def test_icp_p2plane_matches_oracle_and_ground_truth(ctx, cfg0):
@@ -392,16 +394,22 @@ def test_icp_single_iteration_matches_oracle(ctx, cfg0, p2pl):
         _assert_transform_close(g.transform64, o["transform"], _extent(s), rot_tol=1e-6, at=_centroid(s))
 
 
-def test_icp_exact_rigid_copy(ctx, cfg0):
-    """Known answer: a noiseless rigid copy is registered to FP32 round-off."""
+@pytest.mark.parametrize("p2pl", [False, True])
+def test_icp_exact_rigid_copy(ctx, cfg0, p2pl):
+    """Known answer: a noiseless rigid copy is registered to FP32 round-off of
+    the copy (measured: 0 rad, <= 5e-8 x extent), by both implementations."""
     s = O.normals(cfg0["vsrc"], 30)
     R = S.rot_x(2.0) @ S.rot_y(-3.0)
     T = S.rigid(R, (0.004, -0.002, 0.003))
     t = O.transform(s, T.astype(np.float32))
     prm = ctx.icp_params(max_correspondence_distance=0.05, max_iterations=100, transformation_epsilon=1e-12,
-                         euclidean_fitness_epsilon=1e-12, point_to_plane=True)
+                         euclidean_fitness_epsilon=1e-12, point_to_plane=p2pl)
     g = ctx.icp(ctx.upload(s), ctx.upload(t), prm)
-    _assert_transform_close(g.transform64, T, _extent(s), rot_tol=1e-5, trans_rel=1e-5, at=_centroid(s))
+    _assert_transform_close(g.transform64, T, _extent(s), rot_tol=1e-6, trans_rel=1e-6, at=_centroid(s))
+    o = O.icp(s, t, max_corr_dist=0.05, max_iterations=100, transformation_epsilon=1e-12,
+              euclidean_fitness_epsilon=1e-12, point_to_plane=p2pl)
+    _assert_transform_close(g.transform64, o["transform"], _extent(s), rot_tol=1e-6, trans_rel=1e-6,
+                            at=_centroid(s))
 
 
 def test_icp_no_correspondences(ctx, cfg0):

@@ -142,10 +142,12 @@ def test_gradients_match_oracle(ctx, net):
     loss, g = net.gradients(pts, labels)
     _, arg, _ = net.forward(pts, train=True)
     l_ref, g_ref, _ = O.loss_and_grads(params, pts, labels, argmax=arg)
-    assert abs(loss - l_ref) <= 1e-2 * abs(l_ref)
+    # same winners, same bf16 roundings: what is left is fp32 summation order
+    # (measured: loss 1.2e-4, every tensor <= 5.2e-4)
+    assert abs(loss - l_ref) <= 1e-3 * abs(l_ref)
     G, R = O.split(g), O.split(g_ref)
     for name, _ in O.LAYOUT:
-        assert rel_err(G[name], R[name]) < 3e-2, name
+        assert rel_err(G[name], R[name]) < 1e-3, name
     loss2, g2 = net.gradients(pts, labels)
     assert loss2 == loss
     np.testing.assert_array_equal(g2, g)         # fixed summation orders: bit-reproducible

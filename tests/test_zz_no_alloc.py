@@ -121,3 +121,18 @@ def test_into_rejects_images_above_its_scratch():
             ctx.backproject_into(d_in.data_ptr(), p, d_pts.data_ptr(), 1, d_cnt.data_ptr())
         assert e.value.status == L.INVALID_ARG
         assert "scratch" in str(e.value)
+
+
+def test_into_rejects_misaligned_outputs():
+    """The records are written as 16-byte vectors: a point buffer that is not
+    16-byte aligned (or a count that is not 4-byte aligned) is refused on the
+    host, before any launch."""
+    with Context(0) as ctx:
+        p = ctx.depth_params(L.KINECT_V1, 640, 480, frames=1)
+        d_in = torch.zeros(640 * 480, dtype=torch.int16, device="cuda")
+        d_pts = torch.zeros(48 * 16 + 16, dtype=torch.uint8, device="cuda")
+        d_cnt = torch.zeros(2, dtype=torch.int32, device="cuda")
+        for pts_off, cnt_off in ((4, 0), (0, 2)):
+            with pytest.raises(LcrError) as e:
+                ctx.backproject_into(d_in.data_ptr(), p, d_pts.data_ptr() + pts_off, 16, d_cnt.data_ptr() + cnt_off)
+            assert e.value.status == L.INVALID_ARG and "aligned" in str(e.value)

@@ -195,6 +195,13 @@ typedef struct lcr_icp_params {
   double euclidean_fitness_epsilon;     /* :118 (default 0.001) */
   int method;                           /* LCR_ICP_POINT_TO_POINT (the tool's) or _TO_PLANE */
   int compute_fitness;                  /* 1: run getFitnessScore() after align (default) */
+  /* No counterpart in PCL (0 = off, the default, PCL's behaviour): a pair whose
+   * root-mean-square correspondence distance is still above stop_rms after
+   * stop_iteration iterations ends there, not converged, with state
+   * LCR_ICP_STATE_STOPPED -- a batch stops spending rounds on pairs that
+   * cannot settle (views that share too little surface). */
+  int stop_iteration;
+  double stop_rms;
 } lcr_icp_params;
 
 enum {
@@ -203,7 +210,8 @@ enum {
   LCR_ICP_STATE_TRANSFORM = 2,
   LCR_ICP_STATE_ABS_MSE = 3,
   LCR_ICP_STATE_REL_MSE = 4,
-  LCR_ICP_STATE_NO_CORRESPONDENCES = 5
+  LCR_ICP_STATE_NO_CORRESPONDENCES = 5,
+  LCR_ICP_STATE_STOPPED = 6             /* the stop_iteration / stop_rms rule ended the pair */
 };
 
 typedef struct lcr_icp_result {

@@ -35,7 +35,7 @@ CUDA_ERR, TIMEOUT, OOM, IO, TOO_FEW_POINTS, NO_DEVICE = 5, 6, 7, 8, 9, 10
 KINECT_V1, KINECT_V2, PINHOLE_F32 = 0, 1, 2
 ICP_POINT_TO_POINT, ICP_POINT_TO_PLANE = 0, 1
 (ICP_STATE_NOT_CONVERGED, ICP_STATE_ITERATIONS, ICP_STATE_TRANSFORM, ICP_STATE_ABS_MSE, ICP_STATE_REL_MSE,
- ICP_STATE_NO_CORRESPONDENCES) = range(6)
+ ICP_STATE_NO_CORRESPONDENCES, ICP_STATE_STOPPED) = range(7)
 NORMALS_FLIP_ALL = 1
 ACCUM_ALL = 1
 
@@ -67,7 +67,8 @@ POSENET_PARAMS, POSENET_POINTS = 1323401, 1024
 class IcpParams(C.Structure):
     _fields_ = [("max_correspondence_distance", C.c_double), ("max_iterations", C.c_int),
                 ("transformation_epsilon", C.c_double), ("euclidean_fitness_epsilon", C.c_double),
-                ("method", C.c_int), ("compute_fitness", C.c_int)]
+                ("method", C.c_int), ("compute_fitness", C.c_int), ("stop_iteration", C.c_int),
+                ("stop_rms", C.c_double)]
 
 
 class IcpResult(C.Structure):

@@ -211,10 +211,14 @@ class Context:
     @staticmethod
     def icp_params(max_correspondence_distance: float = 0.1, max_iterations: int = 50,
                    transformation_epsilon: float = 1e-9, euclidean_fitness_epsilon: float = 0.001,
-                   point_to_plane: bool = False, compute_fitness: bool = True) -> L.IcpParams:
+                   point_to_plane: bool = False, compute_fitness: bool = True, stop_iteration: int = 0,
+                   stop_rms: float = 0.0) -> L.IcpParams:
+        """stop_iteration / stop_rms: a pair whose RMS correspondence distance is
+        still above stop_rms after stop_iteration iterations ends, not converged
+        (0: off, PCL's criteria only)."""
         return L.IcpParams(max_correspondence_distance, max_iterations, transformation_epsilon,
                            euclidean_fitness_epsilon, L.ICP_POINT_TO_PLANE if point_to_plane else L.ICP_POINT_TO_POINT,
-                           1 if compute_fitness else 0)
+                           1 if compute_fitness else 0, stop_iteration, stop_rms)
 
     def icp(self, src: Cloud, tgt: Cloud, params: L.IcpParams, guess: np.ndarray | None = None,
             want_registered: bool = False):

@@ -345,6 +345,8 @@ void lcr_icp_params_default(lcr_icp_params* p) {
   p->euclidean_fitness_epsilon = 0.001;
   p->method = LCR_ICP_POINT_TO_POINT;
   p->compute_fitness = 1;
+  p->stop_iteration = 0;
+  p->stop_rms = 0.0;
 }
 
 lcr_status lcr_icp(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, const lcr_icp_params* p,
@@ -353,6 +355,7 @@ lcr_status lcr_icp(lcr_ctx* ctx, const lcr_cloud* src, const lcr_cloud* tgt, con
   API_BEGIN(ctx)
   REQUIRE(src && tgt && p && res, "null argument");
   REQUIRE(p->method == LCR_ICP_POINT_TO_POINT || p->method == LCR_ICP_POINT_TO_PLANE, "unknown ICP method");
+  REQUIRE(p->stop_iteration >= 0 && p->stop_rms >= 0, "negative stop rule");
   if (registered) *registered = nullptr;
   icp_run(ctx, src, tgt, p, guess, res);
   if (registered) *registered = transform_run(ctx, src, res->transform);
@@ -372,6 +375,7 @@ lcr_status lcr_icp_batch(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cl
   REQUIRE(p && (npairs == 0 || (src && tgt && results)), "null argument");
   REQUIRE(npairs < (1u << 20), "too many pairs (%zu)", npairs);
   REQUIRE(p->method == LCR_ICP_POINT_TO_POINT || p->method == LCR_ICP_POINT_TO_PLANE, "unknown ICP method");
+  REQUIRE(p->stop_iteration >= 0 && p->stop_rms >= 0, "negative stop rule");
   icp_batch_run(ctx, src, tgt, static_cast<int>(npairs), p, guesses, results);
   for (size_t i = 0; i < npairs; ++i)
     if (results[i].state == LCR_ICP_STATE_NO_CORRESPONDENCES) {

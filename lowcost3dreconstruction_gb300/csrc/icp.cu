@@ -50,6 +50,8 @@ struct IcpParams {
   int min_corr;
   int max_iter;
   double teps, feps;
+  int stop_iter;          // 0: off
+  double stop_mse;        // stop_rms^2
 };
 
 // Per pair, device-resident across rounds.
@@ -368,6 +370,11 @@ __device__ __forceinline__ void icp_update(const double* S, const IcpParams* prm
     return;
   }
   st->prev_mse = mse;
+  if (prm->stop_iter > 0 && st->iter >= prm->stop_iter && mse > prm->stop_mse) {
+    st->converged = 0;
+    st->state = LCR_ICP_STATE_STOPPED;
+    st->done = 1;
+  }
 }
 // Terms of one correspondence (all zero when the source point has none):
 // point-to-point S[0..2] s', S[3..5] t', S[6+3a+b] t'_a s'_b, S[15] count,
@@ -1012,6 +1019,8 @@ void icp_batch_run(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* c
     q.max_iter = p->max_iterations;
     q.teps = p->transformation_epsilon;
     q.feps = p->euclidean_fitness_epsilon;
+    q.stop_iter = p->stop_iteration;
+    q.stop_mse = p->stop_rms * p->stop_rms;
     tile0[i] = tiles;
     chunk0[i] = chunks;
     tiles += si.v.nleaf;

@@ -19,6 +19,16 @@ KINECT_V1 = dict(width=640, height=480, fx=525.0, fy=525.0, cx=319.5, cy=239.5)
 KINECT_V2 = dict(width=512, height=424, fx=365.0, fy=365.0, cx=255.5, cy=211.5)
 
 
+def upsampled(cam: dict, s: int) -> dict:
+    """The camera of an image upsampled s times per axis, as the
+    super-resolution tools' resample factor makes it (super_resolution.cpp:
+    274-314): s x the pixels, focal lengths scaled, pixel centres kept."""
+    c = dict(cam)
+    c.update(width=cam["width"] * s, height=cam["height"] * s, fx=cam["fx"] * s, fy=cam["fy"] * s,
+             cx=(cam["cx"] + 0.5) * s - 0.5, cy=(cam["cy"] + 0.5) * s - 0.5)
+    return c
+
+
 def rot_y(deg: float) -> np.ndarray:
     a = np.deg2rad(deg)
     c, s = np.cos(a), np.sin(a)

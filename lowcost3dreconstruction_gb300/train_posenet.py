@@ -17,6 +17,12 @@ aligned when ICP converged and the RMS over its source points of
 |T_est p - T_gt p| is at most 1 mm.
 
     python -m lowcost3dreconstruction_gb300.train_posenet --steps 16000 --out posenet.npy
+    python -m lowcost3dreconstruction_gb300.train_posenet --steps 0 --init posenet.npy \
+        --depth-steps 4000 --out posenet.npy
+
+The second form fine-tunes on depth-image pairs (depth_pairs: rendered by
+lcr_synthetic_depth at Kinect v1 and v2 geometry and back-projected), the
+input the depth pipeline hands the network.
 """
 from __future__ import annotations
 
@@ -40,10 +46,18 @@ def label_params() -> L.IcpParams:
                               euclidean_fitness_epsilon=1e-7, point_to_plane=True, compute_fitness=False)
 
 
+# A coarse stage still at 15 mm RMS correspondence distance after 20 iterations
+# does not settle: on the 512-pair depth workload every pair that aligned had
+# converged below 15 mm, in 14 iterations on average.
+STOP_ITERATION, STOP_RMS = 20, 0.015
+
+
 def eval_params() -> L.IcpParams:
-    """Coarse refinement: a 5 cm correspondence threshold pulls guesses tens of degrees off into place."""
+    """Coarse refinement: a 5 cm correspondence threshold pulls guesses tens of degrees off into place; a pair
+    still above STOP_RMS after STOP_ITERATION iterations stops there."""
     return Context.icp_params(max_correspondence_distance=0.05, max_iterations=100, transformation_epsilon=1e-8,
-                              euclidean_fitness_epsilon=1e-7, point_to_plane=True, compute_fitness=False)
+                              euclidean_fitness_epsilon=1e-7, point_to_plane=True, compute_fitness=False,
+                              stop_iteration=STOP_ITERATION, stop_rms=STOP_RMS)
 
 
 def fine_params() -> L.IcpParams:
@@ -61,11 +75,19 @@ def proposal_params() -> L.IcpParams:
 
 
 def refine(ctx: Context, srcs, tgts, guesses: np.ndarray, first: L.IcpParams | None = None):
-    """A first point-to-plane ICP (coarse by default) then the fine one, both batched over all pairs."""
+    """A first point-to-plane ICP (coarse by default) then the fine one, both batched; a pair the first stage
+    stopped (or left without correspondences) keeps that result and skips the fine stage."""
     coarse = ctx.icp_batch(srcs, tgts, first or eval_params(), guesses)
-    start = np.stack([r.transform for r in coarse])
-    fine = ctx.icp_batch(srcs, tgts, fine_params(), start)
-    return [f if f.state != L.ICP_STATE_NO_CORRESPONDENCES else c for c, f in zip(coarse, fine)]
+    go = [i for i, r in enumerate(coarse)
+          if r.state not in (L.ICP_STATE_STOPPED, L.ICP_STATE_NO_CORRESPONDENCES)]
+    out = list(coarse)
+    if go:
+        start = np.stack([coarse[i].transform for i in go])
+        fine = ctx.icp_batch([srcs[i] for i in go], [tgts[i] for i in go], fine_params(), start)
+        for i, f in zip(go, fine):
+            if f.state != L.ICP_STATE_NO_CORRESPONDENCES:
+                out[i] = f
+    return out
 
 
 def icp_labels(ctx: Context, srcs, tgts, T_gt: np.ndarray, max_deg: float = 1.0,
@@ -107,6 +129,57 @@ def train(ctx: Context, steps: int, batch: int = 256, lr: float = 1e-3, seed: in
         if log_every and (step % log_every == 0 or step == steps - 1):
             print(f"step {step:5d}  loss {np.mean(losses[-log_every:]):.4f}  lr {a:.2e}", flush=True)
     return net, losses
+
+
+def depth_pairs(ctx: Context, seed: int, batch: int, rng: np.random.Generator, yaw_deg: float = 180.0,
+                max_points: float = 2e5):
+    """Training pairs as the depth pipeline sees them: lcr_synthetic_depth
+    renders `batch` pairs with one camera (Kinect v1 uint16 or Kinect v2
+    float32, upsampling 1 or 2), each object at the distance that gives it
+    5k-max_points pixels per view, and every view is back-projected in metres.
+    Returns (sources, targets, exact transforms)."""
+    import torch
+
+    from . import synthetic as S
+    v1 = bool(rng.random() < 0.5)
+    cam = S.upsampled(S.KINECT_V1 if v1 else S.KINECT_V2, int(rng.choice([1, 2])))
+    model = L.KINECT_V1 if v1 else L.KINECT_V2
+    want = np.exp(rng.uniform(np.log(5e3), np.log(max_points), batch)).astype(np.float32)
+    pix = cam["width"] * cam["height"]
+    buf = torch.empty(2 * batch * pix, dtype=torch.int16 if v1 else torch.float32,
+                      device=f"cuda:{torch.cuda.current_device()}")
+    torch.cuda.synchronize()
+    T = ctx.synthetic_depth(seed, batch, model, cam["width"], cam["height"], cam["fx"], cam["fy"], cam["cx"],
+                            cam["cy"], buf.data_ptr(), points=want, yaw_deg=yaw_deg)
+    params = ctx.depth_params(model, cam["width"], cam["height"], fx=cam["fx"], fy=cam["fy"], cx=cam["cx"],
+                              cy=cam["cy"], depth_min=300.0, depth_max=9000.0, scale=0.001 if v1 else 1.0,
+                              normals=False)
+    es = buf.element_size()
+    clouds = [ctx.backproject_device(buf.data_ptr() + v * pix * es, params) for v in range(2 * batch)]
+    del buf
+    return clouds[0::2], clouds[1::2], T
+
+
+def train_depth(ctx: Context, net: PoseNet, steps: int, batch: int = 256, lr: float = 3e-4, lr_final: float = 1e-5,
+                seed: int = 0, point_every: int = 2, log_every: int = 0) -> list[float]:
+    """Fine-tuning on depth-image pairs (depth_pairs, exact transforms as
+    labels), every point_every-th step on a batch of lcr_synthetic_pairs
+    point samples so the network keeps both input forms; AdamW with cosine
+    decay from lr to lr_final."""
+    rng = np.random.default_rng(seed)
+    losses = []
+    for step in range(steps):
+        if point_every and step % point_every == point_every - 1:
+            srcs, tgts, T = ctx.synthetic_pairs(20_000_000 + seed * 100_003 + step, batch, TRAIN_POINTS)
+        else:
+            srcs, tgts, T = depth_pairs(ctx, 10_000_000 + seed * 100_003 + step, batch, rng)
+        a = lr_final + 0.5 * (lr - lr_final) * (1 + np.cos(np.pi * step / max(steps - 1, 1)))
+        losses.append(net.train_step(srcs, tgts, T, seed=step, opt=adamw(lr=float(a))))
+        for c in srcs + tgts:
+            c.free()
+        if log_every and (step % log_every == 0 or step == steps - 1):
+            print(f"depth step {step:5d}  loss {np.mean(losses[-log_every:]):.4f}  lr {a:.2e}", flush=True)
+    return losses
 
 
 @dataclass
@@ -211,15 +284,24 @@ def main() -> None:
     ap.add_argument("--out", help="write the trained parameters here (.npy)")
     ap.add_argument("--eval-pairs", type=int, default=2000)
     ap.add_argument("--no-icp-labels", action="store_true", help="train on the exact transforms")
+    ap.add_argument("--depth-steps", type=int, default=0,
+                    help="then fine-tune this many steps on depth-image pairs (train_depth)")
+    ap.add_argument("--depth-lr", type=float, default=3e-4)
     args = ap.parse_args()
     ctx = Context(0)
     net = PoseNet(ctx, seed=args.seed)
     if args.init:
         net.load(args.init)
     t0 = time.perf_counter()
-    net, losses = train(ctx, args.steps, args.batch, args.lr, args.seed, net=net,
-                        label_with_icp=not args.no_icp_labels, log_every=500, warmup_frac=0.3)
-    print(f"trained {args.steps} steps x {args.batch} pairs in {time.perf_counter() - t0:.1f} s", flush=True)
+    if args.steps:
+        net, losses = train(ctx, args.steps, args.batch, args.lr, args.seed, net=net,
+                            label_with_icp=not args.no_icp_labels, log_every=500, warmup_frac=0.3)
+        print(f"trained {args.steps} steps x {args.batch} pairs in {time.perf_counter() - t0:.1f} s", flush=True)
+    if args.depth_steps:
+        t1 = time.perf_counter()
+        train_depth(ctx, net, args.depth_steps, args.batch, lr=args.depth_lr, seed=args.seed, log_every=250)
+        print(f"fine-tuned {args.depth_steps} steps x {args.batch} depth pairs in {time.perf_counter() - t1:.1f} s",
+              flush=True)
     if args.out:
         net.save(args.out)
     for yaw in (180.0, 90.0, 30.0) if args.eval_pairs else ():

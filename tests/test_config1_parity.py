@@ -4,8 +4,9 @@ VoxelGrid 1 mm, StatisticalOutlierRemoval k=50 mul 1.0, NormalEstimation k=30
 of the inliers from SOR's neighbour lists, point-to-plane ICP with the bench's
 parameters), stage by stage against the CPU oracle run on the same inputs.
 
-Bars (the benchmark spec's): back-projection and the VoxelGrid output (at this
-extent PCL's index-overflow rule returns the input) bit-exact; SOR distances,
+Bars (the benchmark spec's): back-projection and the VoxelGrid output (where a
+capture's extent overflows the voxel index, PCL's rule returns the input)
+bit-exact; SOR distances,
 statistics and masks bit-exact; normals within 1e-3 rad at the
 99.9th percentile and curvature within 1e-4 of the FP64 oracle; the final ICP
 transform within 1e-5 rad and 1e-6 x cloud extent, iteration counts within 1.
@@ -76,15 +77,20 @@ def c1(ctx):
 
 
 def test_config1_backprojection_and_voxels_bit_exact(c1):
-    """The capture spans metres (the background), so 1 mm voxel indices exceed
-    int32: PCL's VoxelGrid warns and returns its input, and so do the oracle
-    and the GPU.  Both sides must agree on that, point for point."""
+    """A capture spans metres (the background), so 1 mm voxel indices can
+    exceed int32: PCL's VoxelGrid then warns and returns its input, and so do
+    the oracle and the GPU (here the source capture; the moved target's box
+    fits, and at ~2 mm pixel spacing every point keeps a voxel of its own).
+    Both sides agree point for point either way."""
+    overflowed = []
     for g, o in zip(c1["gpu"], c1["orc"]):
         _bits_equal(g["bp"], o["bp"], ALL)
         assert len(g["bp"]) > 250_000
-        assert o["overflow"]
         _bits_equal(g["vg"], o["vg"], ALL)
-        _bits_equal(g["vg"], g["bp"], ALL)
+        if o["overflow"]:
+            _bits_equal(g["vg"], g["bp"], ALL)
+        overflowed.append(o["overflow"])
+    assert overflowed == [True, False]
 
 
 def test_config1_sor_bit_exact(c1):

@@ -84,3 +84,29 @@ def test_turntable_cycle_aligns_consecutive_views(ctx):
         xyz = xyz_of(cl[i + 1].download())
         assert r.converged
         assert S.rmse(r.transform64, T_gt, xyz) < 1e-3, (i, S.rmse(r.transform64, T_gt, xyz))
+
+
+@pytest.mark.gpu
+def test_stop_rule_ends_only_what_it_names(ctx, cfg0):
+    """stop_iteration / stop_rms (no counterpart in PCL): a pair still above
+    stop_rms after stop_iteration iterations ends there, not converged, with the
+    transform of that iteration; a rule it never meets changes nothing."""
+    s, t = ctx.upload(cfg0["vsrc"]), ctx.upload(cfg0["vtgt"])
+    base = dict(max_correspondence_distance=0.05, max_iterations=50, transformation_epsilon=1e-8)
+    free = ctx.icp(s, t, ctx.icp_params(**base))
+    three = ctx.icp(s, t, ctx.icp_params(**{**base, "max_iterations": 3}))
+    stopped = ctx.icp(s, t, ctx.icp_params(**base, stop_iteration=3, stop_rms=1e-9))
+    assert stopped.state == L.ICP_STATE_STOPPED and not stopped.converged and stopped.iterations == 3
+    np.testing.assert_array_equal(stopped.transform64, three.transform64)
+    loose = ctx.icp(s, t, ctx.icp_params(**base, stop_iteration=3, stop_rms=1.0))
+    np.testing.assert_array_equal(loose.transform64, free.transform64)
+    assert loose.state == free.state and loose.iterations == free.iterations
+    # in a batch each pair meets the rule on its own: a pair that stops leaves
+    # the other's result as it is alone
+    rule = ctx.icp_params(**base, stop_iteration=3, stop_rms=0.004)
+    turned = ctx.upload(O.transform(cfg0["vsrc"], S.turntable(60.0, S.OBJECT_AXIS).astype(np.float32)))
+    alone = [ctx.icp(a, t, rule) for a in (s, turned)]
+    res = ctx.icp_batch([s, turned], [t, t], rule)
+    for r, a in zip(res, alone):
+        _same(r, a)
+    assert any(r.state == L.ICP_STATE_STOPPED for r in res)

@@ -7,6 +7,24 @@
 
 namespace {
 
+// Lanes whose k-th neighbour lies above their histogram range (isolated
+// points: a fragment far from the rest) leave their tile and are queued with
+// the largest squared distance they met; k_normals_escaped searches each of
+// them alone with a range that holds its k-th (k_sor_dist_escaped for SOR).
+// One such lane used to make its whole warp traverse the cloud, with a bound
+// that did not prune.
+struct EscapeQueue {
+  uint32_t* slot;   // sorted slot of the query in the index
+  float* top;       // largest squared distance met before leaving (>= its k-th)
+  unsigned int* n;
+};
+
+__device__ __forceinline__ void escape_push(const EscapeQueue& q, uint32_t slot, float top) {
+  const unsigned i = atomicAdd(q.n, 1u);
+  q.slot[i] = slot;
+  q.top[i] = top;
+}
+
 // ------------------------------------------------------------------ SOR
 // outlier_removal.cpp:80-84.  kNN with k+1 results (the query itself first),
 // mean of sqrt(d) over results 1..k summed in double in ascending order
@@ -104,7 +122,7 @@ __device__ __forceinline__ void sor_store(const float4& q, double s, int mean_k,
 // at most k finite points); the host reports it after the pass.
 __global__ void k_sor_dist(IndexView ix, int mean_k, float* __restrict__ dist, uint8_t* __restrict__ valid,
                            unsigned int* __restrict__ nvalid, uint32_t* __restrict__ redo, unsigned int* nredo,
-                           int* too_few, unsigned long long* __restrict__ lists) {
+                           int* too_few, unsigned long long* __restrict__ lists, EscapeQueue eq) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int K = mean_k + 1;
@@ -117,15 +135,54 @@ __global__ void k_sor_dist(IndexView ix, int mean_k, float* __restrict__ dist, u
   if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
   SorAcc acc;
   acc.init(lists && qv ? lists + static_cast<size_t>(__float_as_uint(q.w)) * K : nullptr);
+  bool esc = false;
+  float top = 0.f;
   tile_kset(ix, q.x, q.y, q.z, qv, K, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), wbase + sizeof(KnnWarp), tile,
-            acc);
-  if (qv && acc.cnt < K) *too_few = 1;
+            acc, 0.f, &esc, &top);
+  const bool mine = qv && !esc;
+  if (mine && acc.cnt < K) *too_few = 1;
   double s = 0.0;
-  if (!__all_sync(LCR_FULL, !qv || acc.result(s))) {
+  if (!__all_sync(LCR_FULL, !mine || acc.result(s))) {
+    // the sorted form redoes the whole tile, escaped lanes included
     if (lane == 0) redo[atomicAdd(nredo, 1u)] = static_cast<uint32_t>(tile);
     return;
   }
-  if (qv) sor_store(q, s, mean_k, dist, valid, nvalid);
+  if (mine) sor_store(q, s, mean_k, dist, valid, nvalid);
+  if (esc) escape_push(eq, static_cast<uint32_t>(tile) * 32u + lane, top);
+}
+
+// The escaped SOR queries, one warp each (warps stride over the queue): the
+// sorted k-NN of the query alone (tile_knn, the ascending double sum of the
+// sorted form), its histogram topped at four times the largest squared
+// distance it met, seeded with its own leaf and two either side.
+__global__ void k_sor_dist_escaped(IndexView ix, int mean_k, float* __restrict__ dist, uint8_t* __restrict__ valid,
+                                   unsigned int* __restrict__ nvalid, unsigned long long* __restrict__ lists,
+                                   EscapeQueue eq) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int K = mean_k + 1;
+  unsigned char* wbase = smem + wib * knn_warp_bytes(K);
+  unsigned char* region = wbase + sizeof(KnnWarp);
+  const unsigned long long* list = reinterpret_cast<const unsigned long long*>(region);
+  const unsigned int count = *eq.n;
+  for (unsigned int w = blockIdx.x * nw + wib; w < count; w += gridDim.x * nw) {
+    const uint32_t slot = eq.slot[w];
+    const float4 p = ix.pts[slot];
+    const bool qv = lane == 0;
+    const float qx = qv ? p.x : 0.f, qy = qv ? p.y : 0.f, qz = qv ? p.z : 0.f;
+    float4 tlo, thi;
+    tile_box(qx, qy, qz, qv, tlo, thi);
+    tile_knn(ix, qx, qy, qz, qv, K, LCR_INF, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), region,
+             static_cast<int>(slot >> 5), 4.f * fmaxf(eq.top[w], 1e-30f));
+    if (qv) {
+      double s = 0.0;
+      for (int j = 1; j < K; ++j) s = __dadd_rn(s, static_cast<double>(__fsqrt_rn(key_dist(list[j * 32]))));
+      sor_store(p, s, mean_k, dist, valid, nvalid);
+      if (lists)
+        for (int j = 0; j < K; ++j) lists[static_cast<size_t>(__float_as_uint(p.w)) * K + j] = list[j * 32];
+    }
+    __syncwarp();
+  }
 }
 
 // Sorted form for the queued tiles: the ascending double sum over the sorted
@@ -370,7 +427,7 @@ __device__ __forceinline__ void normal_store(const NeAcc& a, float vx, float vy,
 }
 
 __global__ void k_normals(IndexView ix, int K, const float4* __restrict__ xyz, float vx, float vy, float vz,
-                          int flip_all, float4* __restrict__ onrm) {
+                          int flip_all, float4* __restrict__ onrm, EscapeQueue eq) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned char* wbase = smem + wib * kset_warp_bytes();
@@ -382,9 +439,38 @@ __global__ void k_normals(IndexView ix, int K, const float4* __restrict__ xyz, f
   if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
   NeAcc acc;
   acc.init(q.x, q.y, q.z, xyz);
+  bool esc = false;
+  float top = 0.f;
   tile_kset(ix, q.x, q.y, q.z, qv, K, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), wbase + sizeof(KnnWarp), tile,
-            acc);
-  if (qv) normal_store(acc, vx, vy, vz, flip_all, __float_as_uint(q.w), onrm);
+            acc, 0.f, &esc, &top);
+  if (esc) escape_push(eq, static_cast<uint32_t>(tile) * 32u + lane, top);
+  else if (qv) normal_store(acc, vx, vy, vz, flip_all, __float_as_uint(q.w), onrm);
+}
+
+// One warp per escaped query (warps stride over the queue): the query alone
+// as the tile, seeded with its own leaf and two either side, its histogram
+// topped at four times the largest squared distance it met (an octave of
+// distance above its k-th, so the k-th lies inside the range).
+__global__ void k_normals_escaped(IndexView ix, int K, const float4* __restrict__ xyz, float vx, float vy, float vz,
+                                  int flip_all, float4* __restrict__ onrm, EscapeQueue eq) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned char* wbase = smem + wib * kset_warp_bytes();
+  const unsigned count = *eq.n;
+  for (unsigned w = blockIdx.x * nw + wib; w < count; w += gridDim.x * nw) {
+    const uint32_t slot = eq.slot[w];
+    const float4 p = ix.pts[slot];
+    const bool qv = lane == 0;
+    const float qx = qv ? p.x : 0.f, qy = qv ? p.y : 0.f, qz = qv ? p.z : 0.f;
+    float4 tlo, thi;
+    tile_box(qx, qy, qz, qv, tlo, thi);
+    NeAcc acc;
+    acc.init(qx, qy, qz, xyz);
+    tile_kset(ix, qx, qy, qz, qv, K, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), wbase + sizeof(KnnWarp),
+              static_cast<int>(slot >> 5), acc, 4.f * fmaxf(eq.top[w], 1e-30f));
+    if (qv) normal_store(acc, vx, vy, vz, flip_all, __float_as_uint(p.w), onrm);
+    __syncwarp();
+  }
 }
 
 // Normals of SOR inliers from SOR's neighbour lists (no search).  A warp takes
@@ -654,6 +740,10 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
   CUDA_TRY(cudaMemsetAsync(valid, 0, n, ctx->stream));
   CUDA_TRY(cudaMemsetAsync(sums + 4 * nc0 + 4, 0, 2 * sizeof(double), ctx->stream));
   const RedoQueue rq = redo_queue(ctx, ix.nleaf);
+  char* eblk = static_cast<char*>(dev_alloc(ctx, 2 * align_up(sizeof(uint32_t) * n) + 256));
+  EscapeQueue eq{reinterpret_cast<uint32_t*>(eblk), reinterpret_cast<float*>(eblk + align_up(sizeof(uint32_t) * n)),
+                 reinterpret_cast<unsigned int*>(eblk + 2 * align_up(sizeof(uint32_t) * n))};
+  CUDA_TRY(cudaMemsetAsync(eq.n, 0, sizeof(unsigned int), ctx->stream));
   // neighbour lists for the inliers' normals (k <= 64 only: two keys per lane there)
   NbrHint* hint = nullptr;
   unsigned long long* lists = nullptr;
@@ -674,14 +764,18 @@ void sor_run(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double std_mul, lcr_
   CUDA_TRY(cudaFuncSetAttribute(k_sor_dist, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_set)));
   CUDA_TRY(cudaFuncSetAttribute(k_sor_dist_sorted, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 static_cast<int>(smem)));
+  CUDA_TRY(cudaFuncSetAttribute(k_sor_dist_escaped, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(smem)));
   {
     KernelTimer kt(ctx, LCR_KT_SOR_KNN);
     LCR_LAUNCH(ctx, k_sor_dist, (ix.nleaf + set_warps - 1) / set_warps, set_warps * 32, smem_set, ix, mean_k, dist,
-               valid, nvalid, rq.tiles(), rq.count(), too_few, lists);
+               valid, nvalid, rq.tiles(), rq.count(), too_few, lists, eq);
+    LCR_LAUNCH(ctx, k_sor_dist_escaped, ctx->sms, nw * 32, smem, ix, mean_k, dist, valid, nvalid, lists, eq);
   }
   LCR_LAUNCH(ctx, k_sor_dist_sorted, ctx->sms, nw * 32, smem, ix, mean_k, dist, valid, nvalid, rq.tiles(), rq.count(),
              lists);
   dev_free(ctx, rq.block);
+  dev_free(ctx, eblk);
   // blocked sums (ping-pong between two halves of `sums`)
   double *a = sums, *b = sums + nc0, *a2 = sums + 2 * nc0, *b2 = sums + 3 * nc0;
   int m = nc0;
@@ -795,11 +889,20 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
     return out;
   }
   CUDA_TRY(cudaFuncSetAttribute(k_normals, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_set)));
+  CUDA_TRY(cudaFuncSetAttribute(k_normals_escaped, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(smem_set)));
+  char* eblk = static_cast<char*>(dev_alloc(ctx, 2 * align_up(sizeof(uint32_t) * n) + 256));
+  EscapeQueue eq{reinterpret_cast<uint32_t*>(eblk), reinterpret_cast<float*>(eblk + align_up(sizeof(uint32_t) * n)),
+                 reinterpret_cast<unsigned int*>(eblk + 2 * align_up(sizeof(uint32_t) * n))};
+  CUDA_TRY(cudaMemsetAsync(eq.n, 0, sizeof(unsigned int), ctx->stream));
   {
     KernelTimer kt(ctx, LCR_KT_NORMALS_KNN);
     LCR_LAUNCH(ctx, k_normals, (ix.nleaf + set_warps - 1) / set_warps, set_warps * 32, smem_set, ix, k, in->xyz,
-               vp[0], vp[1], vp[2], flip, out->nrm);
+               vp[0], vp[1], vp[2], flip, out->nrm, eq);
+    LCR_LAUNCH(ctx, k_normals_escaped, ctx->sms, set_warps * 32, smem_set, ix, k, in->xyz, vp[0], vp[1], vp[2],
+               flip, out->nrm, eq);
   }
+  dev_free(ctx, eblk);
   out->index = share_index(in->index);  // same points in the same order
   return out;
 }

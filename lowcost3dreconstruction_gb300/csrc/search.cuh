@@ -378,6 +378,18 @@ struct KHist {
   WarpScratch* ws;
   float R;
   float top_max;  // largest candidate binned into the last (open) bin
+  // A lane whose k-th key falls in the open last bin has a bound that no longer
+  // prunes (it is the farthest candidate seen).  With can_escape set, such a
+  // lane leaves the tile (esc) once the seed leaves are scanned (seeded):
+  // the caller searches it again on its own with a range from top_max, and the
+  // tile keeps its compact radius.  Deciding only after the seeds keeps a lane
+  // from leaving while it has met just its own leaf and one far neighbour.
+  bool can_escape, esc, seeded;
+  __device__ __forceinline__ bool should_escape() const { return can_escape && seeded && cl >= K && bs == kBins; }
+  __device__ __forceinline__ void escape() {
+    esc = true;
+    qv = false;
+  }
 
   __device__ __forceinline__ int bin(float d) const {
     const int b = static_cast<int>(__float_as_uint(d) >> 21) - e0;
@@ -426,6 +438,10 @@ struct KHist {
           --bs;
         }
         tau = fminf(edge(bs - 1), cap);
+        if (should_escape()) {
+          escape();
+          tau = -1.f;
+        }
       }
       }
     }
@@ -504,7 +520,7 @@ struct KCollect {
 // seeding.  Afterwards kw.leaves holds the scanned leaves (h.nleaves of them).
 __device__ __forceinline__ void knn_pass1(const IndexView& ix, float qx, float qy, float qz, bool qv, int K, float cap,
                                           const float4& tlo, const float4& thi, KnnWarp& kw, unsigned char* region,
-                                          int self_leaf, KHist& h, float top_hint = 0.f) {
+                                          int self_leaf, KHist& h, float top_hint = 0.f, bool can_escape = false) {
   const int lane = threadIdx.x & 31;
   // Each lane's bins span 16 octaves of d^2 below min(16 x the tile diagonal,
   // 64 x the distance to the nearer of its two neighbours along the Hilbert
@@ -531,6 +547,9 @@ __device__ __forceinline__ void knn_pass1(const IndexView& ix, float qx, float q
   h.K = K; h.lane = lane;
   h.e0 = static_cast<int>(__float_as_uint(top2) >> 21) - (kBins - 1);
   h.bs = kBins; h.cl = 0; h.nleaves = 0; h.top_max = 0.f;
+  h.can_escape = can_escape;
+  h.esc = false;
+  h.seeded = self_leaf < 0;
   h.cap = cap;
   h.hist = reinterpret_cast<uint32_t*>(region);
   h.leaves = kw.leaves;
@@ -548,6 +567,9 @@ __device__ __forceinline__ void knn_pass1(const IndexView& ix, float qx, float q
       if (self_leaf - d >= 0) h.scan_leaf(ix, self_leaf - d, kw.ws);
       if (self_leaf + d < ix.nleaf) h.scan_leaf(ix, self_leaf + d, kw.ws);
     }
+    h.seeded = true;
+    if (h.should_escape()) h.escape();
+    h.refresh();
   }
   tile_traverse(ix, h, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), kw.ws);
   __syncwarp();
@@ -581,10 +603,10 @@ __device__ __forceinline__ void knn_pass2(const IndexView& ix, const KHist& h, V
 // first K rows (missing entries: key (inf, 0xffffffff)).
 __device__ __forceinline__ void tile_knn(const IndexView& ix, float qx, float qy, float qz, bool qv, int K, float cap,
                                          const float4& tlo, const float4& thi, KnnWarp& kw, unsigned char* region,
-                                         int self_leaf = -1) {
+                                         int self_leaf = -1, float top_hint = 0.f) {
   const int lane = threadIdx.x & 31;
   KHist h;
-  knn_pass1(ix, qx, qy, qz, qv, K, cap, tlo, thi, kw, region, self_leaf, h);
+  knn_pass1(ix, qx, qy, qz, qv, K, cap, tlo, thi, kw, region, self_leaf, h, top_hint);
   const float tau = h.bound();
   const int cnt = h.cl;
   KCollect c;
@@ -734,13 +756,23 @@ struct KSet {
 // acc.begin(tau, k) with the largest squared distance that can be fed, then
 // acc.add(point, d) for points met in the collect pass and acc.add_key(key)
 // for the selected boundary keys.  Queries are the points of leaf self_leaf of ix.
+// With escape non-null, a lane whose k-th key lies above its histogram range
+// leaves the tile (see KHist): *escape is set, its accumulator gets nothing,
+// and *escape_top holds the largest squared distance it met -- at least its
+// k-th -- for the caller's second search of that query.
 template <class Acc>
 __device__ __forceinline__ void tile_kset(const IndexView& ix, float qx, float qy, float qz, bool qv, int K,
                                           const float4& tlo, const float4& thi, KnnWarp& kw, unsigned char* region,
-                                          int self_leaf, Acc& acc, float top_hint = 0.f) {
+                                          int self_leaf, Acc& acc, float top_hint = 0.f, bool* escape = nullptr,
+                                          float* escape_top = nullptr) {
   const int lane = threadIdx.x & 31;
   KHist h;
-  knn_pass1(ix, qx, qy, qz, qv, K, LCR_INF, tlo, thi, kw, region, self_leaf, h, top_hint);
+  knn_pass1(ix, qx, qy, qz, qv, K, LCR_INF, tlo, thi, kw, region, self_leaf, h, top_hint, escape != nullptr);
+  if (escape) {
+    *escape = h.esc;
+    if (escape_top) *escape_top = h.top_max;
+    qv = qv && !h.esc;
+  }
   // boundary range: the bin holding the k-th key (everything if fewer than k)
   unsigned long long klo = make_key(LCR_INF, 0xffffffffu), khi = klo;  // fewer than k: every key is below klo
   int m = 0, cnt = 0;

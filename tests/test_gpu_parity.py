@@ -524,3 +524,44 @@ def test_launch_shapes_do_not_change_results(ctx, cfg0, tmp_path):
     assert [again[k] for k in ("sor_warps", "normals_warps", "icp_blocks_per_sm")] == \
         [first[k] for k in ("sor_warps", "normals_warps", "icp_blocks_per_sm")]
     ctx.tune_set(base["sor_warps"], base["normals_warps"], base["icp_blocks_per_sm"])
+
+
+# ------------------------------------------- isolated points (escaped lanes)
+def _with_fragments(pts, seed):
+    """Small fragments (3 points, 2 mm apart) far from the cloud: their k-th
+    neighbour lies beyond the histogram range their tile gives them, so their
+    lanes leave the tile and are searched again on their own."""
+    rng = np.random.default_rng(seed)
+    c = xyz_of(pts).astype(np.float64).mean(0)
+    frags = []
+    for j in range(6):
+        d = rng.normal(size=3)
+        base = c + 0.4 * d / np.linalg.norm(d)
+        frags.append(base + np.array([[0, 0, 0], [0.002, 0, 0], [0, 0.002, 0]]))
+    extra = random_cloud(18, seed)
+    f = np.concatenate(frags).astype(np.float32)
+    extra["x"], extra["y"], extra["z"] = f[:, 0], f[:, 1], f[:, 2]
+    return np.concatenate([pts, extra])
+
+
+def test_isolated_fragments_sor_bit_exact(ctx, cfg0):
+    pts = _with_fragments(cfg0["vsrc"], 41)
+    gd, _ = ctx.sor_distances(ctx.upload(pts), 50)
+    od, _, _ = O.sor(pts, 50, 1.0)
+    np.testing.assert_array_equal(gd.view(np.uint32), od.view(np.uint32))
+
+
+@pytest.mark.parametrize("k", [30, 50])
+def test_isolated_fragments_normals(ctx, cfg0, k):
+    pts = _with_fragments(cfg0["vsrc"], 42)
+    g = ctx.normals(ctx.upload(pts), k).download()
+    o = O.normals(pts, k)
+    ng, no = normals_of(g).astype(np.float64), normals_of(o).astype(np.float64)
+    ok = o["curvature"] < 0.2
+    ang = np.arccos(np.clip(np.abs(np.sum(ng * no, axis=1)[ok]), -1, 1))
+    assert np.percentile(ang, 99.9) < 1e-3
+    # the fragments' own neighbourhoods (two near points, the rest ~0.4 m off)
+    fr = slice(len(pts) - 18, len(pts))
+    ang_fr = np.arccos(np.clip(np.abs(np.sum(ng[fr] * no[fr], axis=1)), -1, 1))
+    assert np.all(ang_fr < 1e-2), ang_fr
+    np.testing.assert_allclose(g["curvature"][fr], o["curvature"][fr], atol=1e-3)

@@ -80,8 +80,11 @@ LCR_API uint64_t lcr_ctx_launch_count(const lcr_ctx* ctx);
  * timing enabled, the launches of the listed kernels are bracketed by CUDA
  * events on the context's stream; lcr_kernel_time synchronises the stream and
  * returns the summed device time and launch count since timing was enabled.
- * lcr_kernel_timing(ctx, 1) also resets the sums. */
-enum { LCR_KT_SOR_KNN = 0, LCR_KT_NORMALS_KNN = 1, LCR_KT_ENCODE = 2, LCR_KT_COUNT = 3 };
+ * lcr_kernel_timing(ctx, 1) also resets the sums.  LCR_KT_ICP_SEARCH (the
+ * correspondence search of an ICP round) is timed only when the rounds run
+ * from the host loop (environment LCR_ICP_GRAPH=0): inside the CUDA-graph loop
+ * no event can bracket a single kernel. */
+enum { LCR_KT_SOR_KNN = 0, LCR_KT_NORMALS_KNN = 1, LCR_KT_ENCODE = 2, LCR_KT_ICP_SEARCH = 3, LCR_KT_COUNT = 4 };
 LCR_API lcr_status lcr_kernel_timing(lcr_ctx* ctx, int enable);
 LCR_API lcr_status lcr_kernel_time(lcr_ctx* ctx, int which, double* ms, uint64_t* launches);
 
@@ -384,6 +387,18 @@ typedef struct lcr_render_params {
 LCR_API lcr_status lcr_synthetic_depth(lcr_ctx* ctx, uint64_t seed, size_t npairs, const lcr_synth_params* p,
                                        const lcr_render_params* camera, const float* distance,
                                        const float* points, void* d_depth, float* transforms);
+
+/* A turntable cycle of one object (the object of pair 0 of lcr_synthetic_pairs
+ * for this seed, its centre `distance` m in front of the camera): view v turns
+ * it by v * step_deg about its vertical axis through its centre.  Images go to
+ * d_depth [views][height][width] as for lcr_synthetic_depth; poses [views][16]
+ * receives each view's object -> camera transform (row-major), so the
+ * transform from view j into view i is poses[i] * inverse(poses[j]).  noise:
+ * sigma = 1.5 mm (z/1 m)^2 per pixel.  Synchronises before returning.
+ * views <= 65535. */
+LCR_API lcr_status lcr_synthetic_turntable(lcr_ctx* ctx, uint64_t seed, int views, float step_deg,
+                                           const lcr_render_params* camera, float distance, int noise,
+                                           void* d_depth, float* poses);
 
 /* Alignment error of n clouds: out[i] = RMS over the finite points p of
  * clouds[i] of |Ta_i p - Tb_i p| (FP64; Ta, Tb [n][16] row-major), the RMSE

@@ -60,7 +60,7 @@ class SorStats(C.Structure):
                 ("valid", C.c_size_t), ("kept", C.c_size_t), ("removed", C.c_size_t)]
 
 
-KT_SOR_KNN, KT_NORMALS_KNN, KT_ENCODE = 0, 1, 2
+KT_SOR_KNN, KT_NORMALS_KNN, KT_ENCODE, KT_ICP_SEARCH = 0, 1, 2, 3
 POSENET_PARAMS, POSENET_POINTS = 1323401, 1024
 
 
@@ -158,6 +158,8 @@ _SIGS = {
                                       _VP]),
     "lcr_synthetic_depth": (C.c_int, [_VP, C.c_uint64, C.c_size_t, C.POINTER(SynthParams), C.POINTER(RenderParams),
                                       _VP, _VP, _VP, _VP]),
+    "lcr_synthetic_turntable": (C.c_int, [_VP, C.c_uint64, C.c_int, C.c_float, C.POINTER(RenderParams), C.c_float,
+                                          C.c_int, _VP, _VP]),
     "lcr_rmse_batch": (C.c_int, [_VP, _VP, C.c_size_t, _VP, _VP, _VP]),
     "lcr_posenet_create": (C.c_int, [_VP, C.c_uint64, C.POINTER(_VP)]),
     "lcr_posenet_free": (C.c_int, [_VP, _VP]),

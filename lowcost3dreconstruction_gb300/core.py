@@ -331,6 +331,18 @@ class Context:
                                                  L.ptr(w) if w is not None else None, C.c_void_p(dev_ptr), L.ptr(T)))
         return T[:npairs].reshape(npairs, 4, 4)
 
+    def synthetic_turntable(self, seed: int, views: int, step_deg: float, model: int, width: int, height: int,
+                            fx: float, fy: float, cx: float, cy: float, dev_ptr: int, distance: float = 1.0,
+                            noise: bool = True, samples_per_pixel: float = 0.0) -> np.ndarray:
+        """lcr_synthetic_turntable: `views` depth images of one object turned by
+        step_deg per view about its vertical axis, into the device buffer at
+        dev_ptr; returns each view's object -> camera pose [views][4][4]."""
+        P = np.zeros((max(views, 1), 16), dtype=np.float32)
+        cam = L.RenderParams(model, width, height, fx, fy, cx, cy, samples_per_pixel)
+        self._check(self.lib.lcr_synthetic_turntable(self.h, seed, views, step_deg, C.byref(cam), distance,
+                                                     1 if noise else 0, C.c_void_p(dev_ptr), L.ptr(P)))
+        return P[:views].reshape(views, 4, 4)
+
     def rmse_batch(self, clouds: list[Cloud], Ta: np.ndarray, Tb: np.ndarray) -> np.ndarray:
         """lcr_rmse_batch: RMS over each cloud's points of |Ta p - Tb p|."""
         n = len(clouds)

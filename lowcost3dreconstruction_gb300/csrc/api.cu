@@ -744,6 +744,25 @@ lcr_status lcr_synthetic_depth(lcr_ctx* ctx, uint64_t seed, size_t npairs, const
   return LCR_OK;
 }
 
+lcr_status lcr_synthetic_turntable(lcr_ctx* ctx, uint64_t seed, int views, float step_deg,
+                                   const lcr_render_params* cam, float distance, int noise, void* d_depth,
+                                   float* poses) {
+  API_BEGIN(ctx)
+  REQUIRE(cam && (views == 0 || (d_depth && poses)), "null argument");
+  REQUIRE(views >= 0 && views <= 65535, "views out of [0, 65535]");
+  REQUIRE(cam->model == LCR_DEPTH_KINECT_V1 || cam->model == LCR_DEPTH_KINECT_V2 ||
+              cam->model == LCR_DEPTH_PINHOLE_F32,
+          "unknown depth model %d", cam->model);
+  REQUIRE(cam->width >= 1 && cam->height >= 1 && static_cast<long long>(cam->width) * cam->height <= (1ll << 26),
+          "image size %dx%d out of range", cam->width, cam->height);
+  REQUIRE(cam->fx > 0 && cam->fy > 0 && std::isfinite(cam->cx) && std::isfinite(cam->cy), "bad intrinsics");
+  REQUIRE(cam->samples_per_pixel >= 0 && cam->samples_per_pixel <= 64, "samples_per_pixel out of [0, 64]");
+  REQUIRE(distance >= 0.2f && distance <= 20.f && std::isfinite(step_deg), "distance out of [0.2, 20] m");
+  synth_turntable(ctx, seed, views, step_deg, cam, distance, noise, d_depth, poses);
+  API_END(ctx)
+  return LCR_OK;
+}
+
 lcr_status lcr_rmse_batch(lcr_ctx* ctx, const lcr_cloud* const* clouds, size_t n, const double* Ta, const double* Tb,
                           double* out) {
   API_BEGIN(ctx)

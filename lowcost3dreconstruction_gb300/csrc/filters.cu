@@ -295,17 +295,22 @@ __global__ void k_sor_flags(const float* __restrict__ dist, int n, const double*
 // Smallest eigenpair of a symmetric 3x3 (FP64): FP32 trigonometric estimate of
 // the smallest root of the characteristic cubic, Newton refinement in FP64, and
 // the eigenvector as the best-conditioned cross product of two rows of A - l*I.
-__device__ void smallest_eig(const double C[6], double& lam, double n[3]) {
-  // C = {a00, a01, a02, a11, a12, a22}
-  double s = 0.0;
-  for (int i = 0; i < 6; ++i) s = fmax(s, fabs(C[i]));
+// Everything stays in registers: scalars and selects, no arrays indexed at run
+// time (those went to the stack, ~200 bytes of local-memory traffic per point).
+struct Eig3 {
+  double lam, n0, n1, n2;
+};
+
+__device__ __forceinline__ Eig3 smallest_eig(double c00, double c01, double c02, double c11, double c12, double c22) {
+  Eig3 r;
+  const double s = fmax(fmax(fmax(fabs(c00), fabs(c01)), fmax(fabs(c02), fabs(c11))), fmax(fabs(c12), fabs(c22)));
   if (!(s > 0.0)) {
     // all neighbours coincide: no plane (PCL's eigen33 divides 0 by 0 here)
-    lam = 0.0;
-    n[0] = n[1] = n[2] = __longlong_as_double(0x7ff8000000000000ll);
-    return;
+    r.lam = 0.0;
+    r.n0 = r.n1 = r.n2 = __longlong_as_double(0x7ff8000000000000ll);
+    return r;
   }
-  const double a00 = C[0] / s, a01 = C[1] / s, a02 = C[2] / s, a11 = C[3] / s, a12 = C[4] / s, a22 = C[5] / s;
+  const double a00 = c00 / s, a01 = c01 / s, a02 = c02 / s, a11 = c11 / s, a12 = c12 / s, a22 = c22 / s;
   const double c2 = a00 + a11 + a22;
   const double c1 = a00 * a11 + a00 * a22 + a11 * a22 - a01 * a01 - a02 * a02 - a12 * a12;
   const double c0 = a00 * (a11 * a22 - a12 * a12) - a01 * (a01 * a22 - a12 * a02) + a02 * (a01 * a12 - a11 * a02);
@@ -321,9 +326,9 @@ __device__ void smallest_eig(const double C[6], double& lam, double n[3]) {
     if (p > 0.f) {
       const float ip = 1.f / p;
       const float B00 = b00 * ip, B11 = b11 * ip, B22 = b22 * ip, B01 = f01 * ip, B02 = f02 * ip, B12 = f12 * ip;
-      float r = 0.5f * (B00 * (B11 * B22 - B12 * B12) - B01 * (B01 * B22 - B12 * B02) + B02 * (B01 * B12 - B11 * B02));
-      r = fminf(1.f, fmaxf(-1.f, r));
-      const float phi = acosf(r) / 3.f;
+      float rr = 0.5f * (B00 * (B11 * B22 - B12 * B12) - B01 * (B01 * B22 - B12 * B02) + B02 * (B01 * B12 - B11 * B02));
+      rr = fminf(1.f, fmaxf(-1.f, rr));
+      const float phi = acosf(rr) / 3.f;
       l0 = q + 2.f * p * cosf(phi + 2.0943951f);
     } else {
       l0 = q;
@@ -338,42 +343,43 @@ __device__ void smallest_eig(const double C[6], double& lam, double n[3]) {
     l -= step;
     if (fabs(step) <= 1e-17 * fmax(1.0, fabs(l))) break;
   }
-  const double r0[3] = {a00 - l, a01, a02}, r1[3] = {a01, a11 - l, a12}, r2[3] = {a02, a12, a22 - l};
-  double x[3][3];
-  x[0][0] = r0[1] * r1[2] - r0[2] * r1[1]; x[0][1] = r0[2] * r1[0] - r0[0] * r1[2]; x[0][2] = r0[0] * r1[1] - r0[1] * r1[0];
-  x[1][0] = r0[1] * r2[2] - r0[2] * r2[1]; x[1][1] = r0[2] * r2[0] - r0[0] * r2[2]; x[1][2] = r0[0] * r2[1] - r0[1] * r2[0];
-  x[2][0] = r1[1] * r2[2] - r1[2] * r2[1]; x[2][1] = r1[2] * r2[0] - r1[0] * r2[2]; x[2][2] = r1[0] * r2[1] - r1[1] * r2[0];
-  int best = 0;
-  double bn = -1.0;
-  for (int k = 0; k < 3; ++k) {
-    const double m = x[k][0] * x[k][0] + x[k][1] * x[k][1] + x[k][2] * x[k][2];
-    if (m > bn) { bn = m; best = k; }
-  }
+  // rows of A - l I
+  const double r00 = a00 - l, r01 = a01, r02 = a02;
+  const double r10 = a01, r11 = a11 - l, r12 = a12;
+  const double r20 = a02, r21 = a12, r22 = a22 - l;
+  // cross products of row pairs (0,1), (0,2), (1,2); the largest is the best conditioned
+  const double x00 = r01 * r12 - r02 * r11, x01 = r02 * r10 - r00 * r12, x02 = r00 * r11 - r01 * r10;
+  const double x10 = r01 * r22 - r02 * r21, x11 = r02 * r20 - r00 * r22, x12 = r00 * r21 - r01 * r20;
+  const double x20 = r11 * r22 - r12 * r21, x21 = r12 * r20 - r10 * r22, x22 = r10 * r21 - r11 * r20;
+  const double m0 = x00 * x00 + x01 * x01 + x02 * x02, m1 = x10 * x10 + x11 * x11 + x12 * x12,
+               m2 = x20 * x20 + x21 * x21 + x22 * x22;
+  double bn = m0, b0 = x00, b1 = x01, b2 = x02;
+  if (m1 > bn) { bn = m1; b0 = x10; b1 = x11; b2 = x12; }
+  if (m2 > bn) { bn = m2; b0 = x20; b1 = x21; b2 = x22; }
   if (bn > 1e-28) {
     const double inv = 1.0 / sqrt(bn);
-    n[0] = x[best][0] * inv; n[1] = x[best][1] * inv; n[2] = x[best][2] * inv;
+    r.n0 = b0 * inv; r.n1 = b1 * inv; r.n2 = b2 * inv;
   } else {
     // A - l I has rank <= 1: any unit vector orthogonal to its largest row.
-    const double* rr[3] = {r0, r1, r2};
-    int br = 0;
-    double brn = -1.0;
-    for (int k = 0; k < 3; ++k) {
-      const double m = rr[k][0] * rr[k][0] + rr[k][1] * rr[k][1] + rr[k][2] * rr[k][2];
-      if (m > brn) { brn = m; br = k; }
-    }
-    const double* a = rr[br];
-    double e[3] = {0, 0, 0};
-    const int ax = (fabs(a[0]) <= fabs(a[1]) && fabs(a[0]) <= fabs(a[2])) ? 0 : (fabs(a[1]) <= fabs(a[2]) ? 1 : 2);
-    e[ax] = 1.0;
-    double c[3] = {a[1] * e[2] - a[2] * e[1], a[2] * e[0] - a[0] * e[2], a[0] * e[1] - a[1] * e[0]};
-    double cn = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    const double q0 = r00 * r00 + r01 * r01 + r02 * r02, q1 = r10 * r10 + r11 * r11 + r12 * r12,
+                 q2 = r20 * r20 + r21 * r21 + r22 * r22;
+    double qn = q0, g0 = r00, g1 = r01, g2 = r02;
+    if (q1 > qn) { qn = q1; g0 = r10; g1 = r11; g2 = r12; }
+    if (q2 > qn) { qn = q2; g0 = r20; g1 = r21; g2 = r22; }
+    // the axis of the row's smallest component
+    const bool ax0 = fabs(g0) <= fabs(g1) && fabs(g0) <= fabs(g2);
+    const bool ax1 = !ax0 && fabs(g1) <= fabs(g2);
+    const double e0 = ax0 ? 1.0 : 0.0, e1 = ax1 ? 1.0 : 0.0, e2 = (!ax0 && !ax1) ? 1.0 : 0.0;
+    double v0 = g1 * e2 - g2 * e1, v1 = g2 * e0 - g0 * e2, v2 = g0 * e1 - g1 * e0;
+    double cn = sqrt(v0 * v0 + v1 * v1 + v2 * v2);
     if (!(cn > 0.0)) {
-      c[0] = 0.0; c[1] = 0.0; c[2] = 1.0;
+      v0 = 0.0; v1 = 0.0; v2 = 1.0;
       cn = 1.0;
     }
-    n[0] = c[0] / cn; n[1] = c[1] / cn; n[2] = c[2] / cn;
+    r.n0 = v0 / cn; r.n1 = v1 / cn; r.n2 = v2 / cn;
   }
-  lam = l * s;
+  r.lam = l * s;
+  return r;
 }
 
 // normal_estimation.cpp:84-118: kNN(k) including the point itself, covariance,
@@ -412,18 +418,17 @@ __device__ __forceinline__ void normal_store(const NeAcc& a, float vx, float vy,
   }
   const double im = 1.0 / a.m;
   const double mx = a.sx * im, my = a.sy * im, mz = a.sz * im;
-  const double C[6] = {a.sxx * im - mx * mx, a.sxy * im - mx * my, a.sxz * im - mx * mz,
-                       a.syy * im - my * my, a.syz * im - my * mz, a.szz * im - mz * mz};
-  double lam, nn[3];
-  smallest_eig(C, lam, nn);
-  const double tr = C[0] + C[3] + C[5];
-  const double curv = tr != 0.0 ? fabs(lam / tr) : 0.0;
-  const double cs = static_cast<double>(__fsub_rn(vx, a.qx)) * nn[0] + static_cast<double>(__fsub_rn(vy, a.qy)) * nn[1] +
-                    static_cast<double>(__fsub_rn(vz, a.qz)) * nn[2];
+  const double C0 = a.sxx * im - mx * mx, C1 = a.sxy * im - mx * my, C2 = a.sxz * im - mx * mz,
+               C3 = a.syy * im - my * my, C4 = a.syz * im - my * mz, C5 = a.szz * im - mz * mz;
+  const Eig3 e = smallest_eig(C0, C1, C2, C3, C4, C5);
+  const double tr = C0 + C3 + C5;
+  const double curv = tr != 0.0 ? fabs(e.lam / tr) : 0.0;
+  const double cs = static_cast<double>(__fsub_rn(vx, a.qx)) * e.n0 + static_cast<double>(__fsub_rn(vy, a.qy)) * e.n1 +
+                    static_cast<double>(__fsub_rn(vz, a.qz)) * e.n2;
   double sgn = cs < 0 ? -1.0 : 1.0;
   if (flip_all) sgn = -sgn;
-  onrm[o] = make_float4(static_cast<float>(sgn * nn[0]), static_cast<float>(sgn * nn[1]),
-                        static_cast<float>(sgn * nn[2]), static_cast<float>(curv));
+  onrm[o] = make_float4(static_cast<float>(sgn * e.n0), static_cast<float>(sgn * e.n1),
+                        static_cast<float>(sgn * e.n2), static_cast<float>(curv));
 }
 
 __global__ void k_normals(IndexView ix, int K, const float4* __restrict__ xyz, float vx, float vy, float vz,

@@ -1109,8 +1109,11 @@ void icp_batch_run(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* c
     const int grid = icp_grid(ctx);
     unsigned* hlive = reinterpret_cast<unsigned*>(stage + hdr + 1024);
     for (int it = 0; it < p->max_iterations + 1; ++it) {
-      if (p2pl) LCR_LAUNCH(ctx, k_icp_search<1>, grid, kIcpThreads, 0, B.desc, B.cnt);
-      else LCR_LAUNCH(ctx, k_icp_search<0>, grid, kIcpThreads, 0, B.desc, B.cnt);
+      {
+        KernelTimer kt(ctx, LCR_KT_ICP_SEARCH);
+        if (p2pl) LCR_LAUNCH(ctx, k_icp_search<1>, grid, kIcpThreads, 0, B.desc, B.cnt);
+        else LCR_LAUNCH(ctx, k_icp_search<0>, grid, kIcpThreads, 0, B.desc, B.cnt);
+      }
       LCR_LAUNCH(ctx, k_icp_hard, grid, kIcpThreads, 0, B.desc, B.cnt);
       if (p2pl) LCR_LAUNCH(ctx, k_icp_wide<1>, grid, kIcpThreads, 0, B.desc, B.cnt);
       else LCR_LAUNCH(ctx, k_icp_wide<0>, grid, kIcpThreads, 0, B.desc, B.cnt);

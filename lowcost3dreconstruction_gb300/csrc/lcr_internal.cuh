@@ -236,6 +236,8 @@ void rmse_batch(lcr_ctx* ctx, const lcr_cloud* const* clouds, int n, const doubl
 // Seeded synthetic capture pairs (synth.cu); allocates src[i], tgt[i].
 void synth_depth(lcr_ctx* ctx, uint64_t seed, int npairs, const lcr_synth_params* prm, const lcr_render_params* cam,
                  const float* distance, const float* points, void* d_out, float* transforms);
+void synth_turntable(lcr_ctx* ctx, uint64_t seed, int views, float step_deg, const lcr_render_params* cam,
+                     float distance, int noise, void* d_out, float* poses);
 void synth_pairs(lcr_ctx* ctx, uint64_t seed, int npairs, int npts, const lcr_synth_params* prm, lcr_cloud** src,
                  lcr_cloud** tgt, float* transforms);
 // Device-side bounding box of the finite points of an xyz array: out[0] = lo, out[1] = hi.

@@ -321,11 +321,13 @@ struct RenderCam {
   float spp;
 };
 
+// Image v is view v&1 of pair v>>1 (views == null) or, on a turntable, pose
+// views[v] (3x4 row-major object -> camera) of object 0.
 __global__ void k_render_splat(uint64_t seed, const SynthObject* __restrict__ objs, RenderCam cam,
-                               uint32_t* __restrict__ zbuf) {
-  const int v = blockIdx.y, b = v >> 1;
+                               uint32_t* __restrict__ zbuf, const float* __restrict__ views = nullptr) {
+  const int v = blockIdx.y, b = views ? 0 : v >> 1;
   const SynthObject& o = objs[b];
-  const float* P = (v & 1) ? o.Pt : o.Ps;
+  const float* P = views ? views + 12 * v : ((v & 1) ? o.Pt : o.Ps);
   const float zc = fmaxf(-P[11], 0.05f);
   float area = 0.f;
   for (int k = 0; k < 4; ++k) area += o.part[k].area;
@@ -426,6 +428,67 @@ void synth_depth(lcr_ctx* ctx, uint64_t seed, int npairs, const lcr_synth_params
   LCR_LAUNCH(ctx, k_render_finish, dim3(static_cast<unsigned>((plane + 255) / 256), 2 * npairs), 256, 0, seed, zb,
              static_cast<int>(plane), f32, prm->noise, d_out);
   CUDA_TRY(cudaMemcpyAsync(transforms, T, npairs * 64ull, cudaMemcpyDeviceToHost, ctx->stream));
+  sync(ctx);
+  dev_free(ctx, d);
+}
+
+// The turntable poses: view v turns the object by v * step about its vertical
+// axis through its centre, from the object's own source pose (pair 0 of the
+// seed); poses[v] = object -> camera, 4x4 row-major.
+__global__ void k_turntable_poses(const SynthObject* __restrict__ objs, int views, float step_rad,
+                                  float* __restrict__ P12, float* __restrict__ poses) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= views) return;
+  const float* Ps = objs[0].Ps;
+  float Rv[9];
+  rot_y(step_rad * static_cast<float>(v), Rv);
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) {
+      const float r = Rv[3 * i] * Ps[j] + Rv[3 * i + 1] * Ps[4 + j] + Rv[3 * i + 2] * Ps[8 + j];
+      P12[12 * v + 4 * i + j] = r;
+      poses[16 * v + 4 * i + j] = r;
+    }
+    P12[12 * v + 4 * i + 3] = Ps[4 * i + 3];
+    poses[16 * v + 4 * i + 3] = Ps[4 * i + 3];
+  }
+  poses[16 * v + 12] = poses[16 * v + 13] = poses[16 * v + 14] = 0.f;
+  poses[16 * v + 15] = 1.f;
+}
+
+void synth_turntable(lcr_ctx* ctx, uint64_t seed, int views, float step_deg, const lcr_render_params* cam,
+                     float distance, int noise, void* d_out, float* poses) {
+  if (views == 0) return;
+  const size_t plane = static_cast<size_t>(cam->width) * cam->height;
+  const size_t zbytes = plane * 4 * static_cast<size_t>(views);
+  const size_t head = (sizeof(SynthObject) + 64 + 4 + views * (48 + 64) + 255) & ~static_cast<size_t>(255);
+  char* d = static_cast<char*>(dev_alloc(ctx, head + zbytes));
+  auto* objs = reinterpret_cast<SynthObject*>(d);
+  auto* T = reinterpret_cast<float*>(d + sizeof(SynthObject));
+  auto* dd = reinterpret_cast<float*>(d + sizeof(SynthObject) + 64);
+  auto* P12 = reinterpret_cast<float*>(d + sizeof(SynthObject) + 68);
+  auto* P16 = P12 + 12 * views;
+  auto* zb = reinterpret_cast<uint32_t*>(d + head);
+  CUDA_TRY(cudaMemcpyAsync(dd, &distance, 4, cudaMemcpyHostToDevice, ctx->stream));
+  CUDA_TRY(cudaMemsetAsync(zb, 0x7f, zbytes, ctx->stream));
+  lcr_synth_params prm{0.f, 0.f, 0.f, noise};
+  LCR_LAUNCH(ctx, k_synth_objects, 1, 32, 0, seed, 1, prm, objs, T, static_cast<const float*>(dd),
+             static_cast<const float*>(nullptr), 0.f);
+  LCR_LAUNCH(ctx, k_turntable_poses, (views + 63) / 64, 64, 0, objs, views,
+             step_deg * 3.14159265358979f / 180.0f, P12, P16);
+  RenderCam rc;
+  rc.w = cam->width;
+  rc.h = cam->height;
+  rc.fx = static_cast<float>(cam->fx);
+  rc.fy = static_cast<float>(cam->fy);
+  rc.cx = static_cast<float>(cam->cx);
+  rc.cy = static_cast<float>(cam->cy);
+  rc.off = cam->model == LCR_DEPTH_KINECT_V2 ? 0.5f : 0.f;
+  rc.spp = cam->samples_per_pixel > 0 ? cam->samples_per_pixel : 6.f;
+  LCR_LAUNCH(ctx, k_render_splat, dim3(64, views), 256, 0, seed, objs, rc, zb, static_cast<const float*>(P12));
+  const int f32 = cam->model == LCR_DEPTH_KINECT_V1 ? 0 : 1;
+  LCR_LAUNCH(ctx, k_render_finish, dim3(static_cast<unsigned>((plane + 255) / 256), views), 256, 0, seed, zb,
+             static_cast<int>(plane), f32, noise, d_out);
+  CUDA_TRY(cudaMemcpyAsync(poses, P16, views * 64ull, cudaMemcpyDeviceToHost, ctx->stream));
   sync(ctx);
   dev_free(ctx, d);
 }

@@ -84,3 +84,33 @@ def test_render_rejects_bad_arguments(ctx):
     with pytest.raises(L.LcrError):
         ctx.synthetic_depth(1, 1, L.KINECT_V1, 4, 2, 1.0, 1.0, 0.0, 0.0, buf.data_ptr(),
                             distance=np.array([0.01], np.float32))
+
+
+def test_turntable_views_turn_about_the_vertical_axis(ctx):
+    """lcr_synthetic_turntable: view 0 is the source view of the seed's pair 0,
+    image for image, and view j is the object turned by j * step about its
+    vertical axis through its centre."""
+    import math
+    seed, views, step = 61, 5, 10.0
+    pix = V1["width"] * V1["height"]
+    buf = torch.zeros(views * pix, dtype=torch.int16, device="cuda")
+    torch.cuda.synchronize()
+    P = ctx.synthetic_turntable(seed, views, step, L.KINECT_V1, V1["width"], V1["height"], V1["fx"], V1["fy"],
+                                V1["cx"], V1["cy"], buf.data_ptr(), distance=1.0).astype(np.float64)
+    pair, _ = _render(ctx, seed, 1, V1, distance=np.array([1.0], np.float32), noise=True)
+    np.testing.assert_array_equal(buf[:pix].cpu().numpy(), pair[:pix].cpu().numpy())
+    for j in range(1, views):
+        Tj = P[j] @ np.linalg.inv(P[0])
+        c = np.clip((np.trace(Tj[:3, :3]) - 1) / 2, -1, 1)
+        assert abs(math.degrees(math.acos(c)) - step * j) < 1e-3
+        # the axis is the camera's y axis, and the object's centre stays put
+        assert abs(abs(Tj[1, 1]) - 1.0) < 1e-6
+        np.testing.assert_allclose(P[j][:3, 3], P[0][:3, 3], atol=1e-6)
+    # consecutive views back-project into clouds that overlap after the known motion
+    prm = ctx.depth_params(L.KINECT_V1, V1["width"], V1["height"], scale=0.001, depth_max=9000.0, normals=False)
+    a = xyz_of(ctx.backproject_device(buf.data_ptr(), prm).download()).astype(np.float64)
+    b = xyz_of(ctx.backproject_device(buf.data_ptr() + 2 * pix, prm).download()).astype(np.float64)
+    T10 = P[0] @ np.linalg.inv(P[1])
+    bb = b @ T10[:3, :3].T + T10[:3, 3]
+    d, _ = cKDTree(a).query(bb)
+    assert np.median(d) < 2e-3

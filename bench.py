@@ -1275,6 +1275,8 @@ def cpu_pipeline(pr, threads: int):
 
 
 def cpu_baseline(pr, sample_pairs: int = 1) -> dict:
+    """The CPU restatement on all host threads (the value), and on one thread
+    as the pcl_tools run (they have no threading)."""
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     aligned = 0
@@ -1282,9 +1284,14 @@ def cpu_baseline(pr, sample_pairs: int = 1) -> dict:
         ok, _ = cpu_pipeline(pr, threads)
         aligned += int(ok)
     dt = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ok1, _ = cpu_pipeline(pr, 1)
+    dt1 = time.perf_counter() - t0
     return {"value": round(aligned / dt, 5), "unit": "pairs/s", "cores": threads, "kind": "port",
             "sample": f"{sample_pairs} full pair(s) of the same workload through the CPU restatement "
-                      f"(own kd-tree, OpenMP over {threads} threads), {dt:.2f} s"}
+                      f"(own kd-tree, OpenMP over {threads} threads), {dt:.2f} s",
+            "single_thread": {"value": round(int(ok1) / dt1, 5), "unit": "pairs/s", "cores": 1,
+                              "sample": f"1 full pair on one thread, {dt1:.2f} s"}}
 
 
 def reference_arm(args, rank: int) -> dict | None:

@@ -430,17 +430,25 @@ struct KHist {
       if (b == kBins - 1) top_max = fmaxf(top_max, d);
       hist[b * 32 + lane] += 1u;
       if (++cl >= K) {
-        // drop the top bins while the ones below still hold k candidates
+        // drop the top bins while the ones below still hold k candidates;
+        // the bound moves only when a bin is dropped, or when the k-th
+        // candidate first arrives (cl never falls below K after that, and with
+        // the last bin as the boundary, its edge top_max cannot grow: every
+        // accepted candidate lies at or below it)
+        const bool first = cl == K;
+        const int bs0 = bs;
         while (bs > 1) {
           const int top = static_cast<int>(hist[(bs - 1) * 32 + lane]);
           if (cl - top < K) break;
           cl -= top;
           --bs;
         }
-        tau = fminf(edge(bs - 1), cap);
-        if (should_escape()) {
-          escape();
-          tau = -1.f;
+        if (first || bs != bs0) {
+          tau = fminf(edge(bs - 1), cap);
+          if (should_escape()) {
+            escape();
+            tau = -1.f;
+          }
         }
       }
       }

@@ -514,11 +514,13 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_search(const BatchDesc* __r
     unsigned long long sk;
     float4 sp;
     prev_candidate(d, prm, gslot, pv, q, sk, sp);
-    v.seed(sk, sp);
+    v.seed(sk);
     tile_traverse(pcs[wib].tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), wss[wib]);
     d->prev_ti[gslot] = key_idx(v.best);
+    const bool found = pv && v.found();
+    const float4 tp = found ? prm->tgt_xyz[key_idx(v.best)] : make_float4(0.f, 0.f, 0.f, 0.f);
     float t[32];
-    corr_terms<P2PL>(t, pv && v.found(), q, v.bp, key_dist(v.best), key_idx(v.best), prm);
+    corr_terms<P2PL>(t, found, q, tp, key_dist(v.best), key_idx(v.best), prm);
     d->tile_part[gslot] = reduce_scatter32(t, lane);
   }
 }
@@ -713,7 +715,7 @@ __global__ void __launch_bounds__(kIcpThreads) k_fitness(const BatchDesc* __rest
       unsigned long long sk;
       float4 sp;
       prev_candidate(d, prm, gslot, pv, q, sk, sp);
-      v.seed(sk, sp);
+      v.seed(sk);
       tile_traverse(pcs[wib].tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z),
                     wss[wib]);
       found = v.found();

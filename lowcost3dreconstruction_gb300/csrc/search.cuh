@@ -170,18 +170,19 @@ __device__ __forceinline__ bool tile_box(float x, float y, float z, bool v, floa
 
 // ------------------------------------------------------------ 1-NN visitor
 // best starts at (cap, 0xffffffff): a point is accepted iff its distance <= cap.
+// Only the (distance, index) key is carried through the scan; a caller that
+// needs the point reads it by index afterwards (one load instead of four
+// selects per candidate).
 struct NN1 {
   float qx, qy, qz;
   bool qv;
   unsigned long long best;
-  float4 bp;
   WarpScratch* ws;
   float R;
 
   __device__ __forceinline__ void init(float x, float y, float z, bool v, float cap, WarpScratch& w) {
     qx = x; qy = y; qz = z; qv = v;
     best = make_key(cap, 0xffffffffu);
-    bp = make_float4(0.f, 0.f, 0.f, 0.f);
     ws = &w;
     subtile_setup(x, y, z, v, w);
     refresh();
@@ -189,11 +190,8 @@ struct NN1 {
   // Starts from a known candidate (warp-collective): the result is still the
   // exact nearest -- the candidate is one of the points -- but the search
   // prunes with its distance from the first node on.
-  __device__ __forceinline__ void seed(unsigned long long k, const float4& p) {
-    if (k < best) {
-      best = k;
-      bp = p;
-    }
+  __device__ __forceinline__ void seed(unsigned long long k) {
+    if (k < best) best = k;
     refresh();
   }
   __device__ __forceinline__ float bound() const { return key_dist(best); }
@@ -204,17 +202,27 @@ struct NN1 {
   __device__ __forceinline__ bool need(const float4& lo, const float4& hi) const {
     return qv && box_dist2(lo, hi, qx, qy, qz) <= bound();
   }
+  // Four independent minimum chains over the 32 staged points, merged at the
+  // end: keys are unique (the index is part of them), so the minimum is the
+  // same whatever the grouping, and the loop no longer waits on one serial
+  // compare-and-select chain.
   __device__ __forceinline__ void scan(const float4* st) {
-#pragma unroll 8
-    for (int j = 0; j < 32; ++j) {
-      const float4 p = st[j];
-      const float d = exact_dist2(qx, qy, qz, p.x, p.y, p.z);
-      const unsigned long long k = make_key(d, __float_as_uint(p.w));
-      if (k < best) {
-        best = k;
-        bp = p;
-      }
+    unsigned long long b0 = best, b1 = best, b2 = best, b3 = best;
+#pragma unroll 2
+    for (int j = 0; j < 32; j += 4) {
+      const float4 p0 = st[j], p1 = st[j + 1], p2 = st[j + 2], p3 = st[j + 3];
+      const unsigned long long k0 = make_key(exact_dist2(qx, qy, qz, p0.x, p0.y, p0.z), __float_as_uint(p0.w));
+      const unsigned long long k1 = make_key(exact_dist2(qx, qy, qz, p1.x, p1.y, p1.z), __float_as_uint(p1.w));
+      const unsigned long long k2 = make_key(exact_dist2(qx, qy, qz, p2.x, p2.y, p2.z), __float_as_uint(p2.w));
+      const unsigned long long k3 = make_key(exact_dist2(qx, qy, qz, p3.x, p3.y, p3.z), __float_as_uint(p3.w));
+      b0 = k0 < b0 ? k0 : b0;
+      b1 = k1 < b1 ? k1 : b1;
+      b2 = k2 < b2 ? k2 : b2;
+      b3 = k3 < b3 ? k3 : b3;
     }
+    b0 = b1 < b0 ? b1 : b0;
+    b2 = b3 < b2 ? b3 : b2;
+    best = b2 < b0 ? b2 : b0;
   }
   __device__ __forceinline__ bool skip(int) const { return false; }
   __device__ __forceinline__ void visited(int) {}
@@ -303,7 +311,6 @@ __device__ __forceinline__ void tile_nn1(const IndexView& ix, float qx, float qy
   }
   const int lane = threadIdx.x & 31, grp = lane >> 3;
   unsigned long long best = make_key(cap, 0xffffffffu);
-  float4 bp = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int g = 0; g < 4; ++g) {
     const bool mine = qv && grp == g;
     float4 slo, shi;
@@ -313,10 +320,7 @@ __device__ __forceinline__ void tile_nn1(const IndexView& ix, float qx, float qy
       NN1 s;
       s.init(qx, qy, qz, mine, cap, ws);
       tile_traverse(ix, s, 0.5f * (slo.x + shi.x), 0.5f * (slo.y + shi.y), 0.5f * (slo.z + shi.z), ws);
-      if (mine) {
-        best = s.best;
-        bp = s.bp;
-      }
+      if (mine) best = s.best;
     } else {
       const unsigned valid = __ballot_sync(LCR_FULL, mine);
       for (unsigned t = valid; t; t &= t - 1u) {
@@ -325,16 +329,12 @@ __device__ __forceinline__ void tile_nn1(const IndexView& ix, float qx, float qy
         unsigned long long b;
         float4 p;
         warp_query_nn(ix, x, y, z, cap, ws, b, p);
-        if (lane == l) {
-          best = b;
-          bp = p;
-        }
+        if (lane == l) best = b;
       }
     }
   }
   v.qx = qx; v.qy = qy; v.qz = qz; v.qv = qv;
   v.best = best;
-  v.bp = bp;
 }
 
 // ---------------------------------------------------------------- k-NN

@@ -352,7 +352,7 @@ def turntable_arm(args) -> dict:
         for c in cl:
             c.free()
     P, vox = render(7000 + best[1])
-    cl = [ctx.normals(c, 30) for c in vox]
+    cl = [ctx.normals(c, 30, keep_neighbours=True) for c in vox]  # every view is a target
     for c in vox:
         c.free()
     src = [cl[(i + 1) % views] for i in range(views)]
@@ -521,7 +521,7 @@ def proposal_arm(args) -> dict:
     clouds = []
     for v in range(2 * npairs):
         c = ctx.backproject_device(buf.data_ptr() + 2 * pix * v, bp)
-        clouds.append(ctx.normals(c, 30))
+        clouds.append(ctx.normals(c, 30, keep_neighbours=v % 2 == 1))
         c.free()
     del buf
     srcs, tgts = clouds[0::2], clouds[1::2]
@@ -916,7 +916,8 @@ def config4_clouds(ctxs, c4: Config4, from_host: bool = False, k: int = 30):
         for v in range(t, 2 * n, len(ctxs)):
             ptr, host, params = c4.view(v // 2, v % 2)
             bp = c.backproject(host, params) if from_host else c.backproject_device(ptr, params)
-            out[v] = c.normals(bp, k)
+            # targets keep their neighbour rows: ICP proves most correspondences from them
+            out[v] = c.normals(bp, k, keep_neighbours=v % 2 == 1)
             bp.free()
         c.synchronize()
 

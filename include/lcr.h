@@ -100,6 +100,14 @@ LCR_API size_t lcr_cloud_size(const lcr_cloud* c);
 /* Copies min(n, capacity) points out; returns LCR_ERR_INVALID_ARG if capacity < n. */
 LCR_API lcr_status lcr_cloud_download(lcr_ctx* ctx, const lcr_cloud* c, lcr_point* out, size_t capacity);
 LCR_API void lcr_cloud_free(lcr_ctx* ctx, lcr_cloud* c);
+/* The neighbour rows an lcr_normals call with LCR_NORMALS_KEEP_NEIGHBOURS kept
+ * with its output cloud c: *k = the k it was called with; with host_rows
+ * (32 * n words) non-NULL, row i holds in words [0, k) the indices of point
+ * i's k nearest, itself included, in no particular order, and in word 31 the
+ * largest squared distance among them as float bits (+inf when the cloud has
+ * fewer than k finite points).  Rows of non-finite points are unspecified.
+ * LCR_ERR_INVALID_ARG if c holds no rows (*k = 0). */
+LCR_API lcr_status lcr_cloud_neighbours(lcr_ctx* ctx, const lcr_cloud* c, int* k, uint32_t* host_rows);
 /* a followed by b (PointCloud operator+, e.g. accumulate_clouds.cpp:121-123). */
 LCR_API lcr_status lcr_cloud_concat(lcr_ctx* ctx, const lcr_cloud* a, const lcr_cloud* b, lcr_cloud** out);
 
@@ -180,10 +188,15 @@ LCR_API lcr_status lcr_sor(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, double
 LCR_API lcr_status lcr_sor_distances(lcr_ctx* ctx, const lcr_cloud* in, int mean_k, float* distances,
                                      lcr_sor_stats* stats);
 
-enum { LCR_NORMALS_FLIP_ALL = 1 };
+enum { LCR_NORMALS_FLIP_ALL = 1, LCR_NORMALS_KEEP_NEIGHBOURS = 2 };
 /* pcl::NormalEstimation with k neighbours and a viewpoint
  * (pcl_tools/normal_estimation.cpp:84-118).  flags LCR_NORMALS_FLIP_ALL negates
  * every normal afterwards (the tool's centroid XOR reverse rule :112-118).
+ * LCR_NORMALS_KEEP_NEIGHBOURS (k <= 31; ignored above) keeps every point's k
+ * nearest neighbours with the output cloud (128 B per point, freed with it):
+ * lcr_icp / lcr_icp_batch with that cloud as the target then settle most
+ * correspondences from the previous iteration's one and its neighbour list
+ * instead of a tree search, with the same result.
  * Output: the input cloud with normal_x/y/z and curvature replaced. */
 LCR_API lcr_status lcr_normals(lcr_ctx* ctx, const lcr_cloud* in, int k, const float viewpoint[3], int flags,
                                lcr_cloud** out);

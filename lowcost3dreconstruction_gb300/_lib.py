@@ -36,7 +36,7 @@ KINECT_V1, KINECT_V2, PINHOLE_F32 = 0, 1, 2
 ICP_POINT_TO_POINT, ICP_POINT_TO_PLANE = 0, 1
 (ICP_STATE_NOT_CONVERGED, ICP_STATE_ITERATIONS, ICP_STATE_TRANSFORM, ICP_STATE_ABS_MSE, ICP_STATE_REL_MSE,
  ICP_STATE_NO_CORRESPONDENCES, ICP_STATE_STOPPED) = range(7)
-NORMALS_FLIP_ALL = 1
+NORMALS_FLIP_ALL, NORMALS_KEEP_NEIGHBOURS = 1, 2
 ACCUM_ALL = 1
 
 
@@ -121,6 +121,7 @@ _SIGS = {
     "lcr_cloud_from_device": (C.c_int, [_VP, _VP, C.c_size_t, C.POINTER(_VP)]),
     "lcr_cloud_size": (C.c_size_t, [_VP]),
     "lcr_cloud_download": (C.c_int, [_VP, _VP, _VP, C.c_size_t]),
+    "lcr_cloud_neighbours": (C.c_int, [_VP, _VP, C.POINTER(C.c_int), _VP]),
     "lcr_cloud_free": (None, [_VP, _VP]),
     "lcr_cloud_concat": (C.c_int, [_VP, _VP, _VP, C.POINTER(_VP)]),
     "lcr_backproject": (C.c_int, [_VP, _VP, C.POINTER(DepthParams), C.POINTER(_VP)]),

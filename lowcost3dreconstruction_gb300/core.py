@@ -65,6 +65,14 @@ class Cloud:
         self._ctx._check(self._ctx.lib.lcr_cloud_download(self._ctx.h, self.handle, L.ptr(out), n))
         return out
 
+    def neighbours(self) -> tuple[int, np.ndarray]:
+        """The neighbour rows kept by normals(..., keep_neighbours=True):
+        (k, rows) with rows an (n, 32) uint32 array (lcr_cloud_neighbours)."""
+        k = C.c_int(0)
+        rows = np.zeros((len(self), 32), dtype=np.uint32)
+        self._ctx._check(self._ctx.lib.lcr_cloud_neighbours(self._ctx.h, self.handle, C.byref(k), L.ptr(rows)))
+        return k.value, rows
+
     def free(self) -> None:
         if self.handle and self._ctx.h:
             self._ctx.lib.lcr_cloud_free(self._ctx.h, self.handle)
@@ -203,9 +211,14 @@ class Context:
         self._check(self.lib.lcr_sor_distances(self.h, cloud.handle, mean_k, L.ptr(out), C.byref(stats)))
         return out, stats
 
-    def normals(self, cloud: Cloud, k: int, viewpoint=(0.0, 0.0, 0.0), flip_all: bool = False) -> Cloud:
+    def normals(self, cloud: Cloud, k: int, viewpoint=(0.0, 0.0, 0.0), flip_all: bool = False,
+                keep_neighbours: bool = False) -> Cloud:
+        """NormalEstimation (lcr_normals).  keep_neighbours (k <= 31) keeps each
+        point's k nearest with the output, so that ICP with it as the target
+        settles most correspondences without a search (same result)."""
         vp = np.asarray(viewpoint, dtype=np.float32)
-        return self._cloud(self.lib.lcr_normals, cloud.handle, k, L.ptr(vp), L.NORMALS_FLIP_ALL if flip_all else 0)
+        flags = (L.NORMALS_FLIP_ALL if flip_all else 0) | (L.NORMALS_KEEP_NEIGHBOURS if keep_neighbours else 0)
+        return self._cloud(self.lib.lcr_normals, cloud.handle, k, L.ptr(vp), flags)
 
     # ------------------------------------------------------------------ ICP
     @staticmethod

@@ -223,6 +223,20 @@ lcr_status lcr_cloud_download(lcr_ctx* ctx, const lcr_cloud* c, lcr_point* out, 
   return LCR_OK;
 }
 
+lcr_status lcr_cloud_neighbours(lcr_ctx* ctx, const lcr_cloud* c, int* k, uint32_t* host_rows) {
+  API_BEGIN(ctx)
+  REQUIRE(c && k, "null argument");
+  *k = c->graph ? c->graph->k : 0;
+  REQUIRE(c->graph, "the cloud holds no neighbour rows (lcr_normals with LCR_NORMALS_KEEP_NEIGHBOURS makes them)");
+  if (host_rows && c->n) {
+    CUDA_TRY(cudaMemcpyAsync(host_rows, c->graph->rows, sizeof(uint32_t) * 32 * c->n, cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    sync(ctx);
+  }
+  API_END(ctx)
+  return LCR_OK;
+}
+
 void lcr_cloud_free(lcr_ctx* ctx, lcr_cloud* c) {
   if (!ctx || !c) return;
   try {

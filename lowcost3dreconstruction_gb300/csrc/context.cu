@@ -69,6 +69,10 @@ void cloud_release(lcr_ctx* ctx, lcr_cloud* c) {
     dev_free(ctx, c->nbr->block);
     delete c->nbr;
   }
+  if (c->graph) {
+    dev_free(ctx, c->graph->rows);
+    delete c->graph;
+  }
   dev_free(ctx, c->xyz);
   delete c;
 }

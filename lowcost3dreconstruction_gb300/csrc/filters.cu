@@ -387,27 +387,55 @@ __device__ __forceinline__ Eig3 smallest_eig(double c00, double c01, double c02,
 // that (vp - p).n >= 0, optionally negated afterwards.  The covariance sums run
 // in FP32 over offsets from the query point, in the order the unordered k-NN
 // set reduction meets the neighbours; the eigen-solve is FP64.
+// With a neighbour row (LCR_NORMALS_KEEP_NEIGHBOURS) it also records each
+// neighbour's original index and the largest squared distance (NbrGraph).
 struct NeAcc {
   float qx, qy, qz;
   const float4* __restrict__ xyz;
   float sx, sy, sz, sxx, sxy, sxz, syy, syz, szz;
   int m;
-  __device__ __forceinline__ void init(float x, float y, float z, const float4* p) {
+  uint32_t* row;
+  float rmax;
+  __device__ __forceinline__ void init(float x, float y, float z, const float4* p, uint32_t* r = nullptr) {
     qx = x; qy = y; qz = z;
     xyz = p;
     sx = sy = sz = sxx = sxy = sxz = syy = syz = szz = 0.f;
     m = 0;
+    row = r;
+    rmax = 0.f;
   }
-  __device__ __forceinline__ void add(const float4& p, float) {
+  __device__ __forceinline__ void take(const float4& p) {
     const float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
     sx += dx; sy += dy; sz += dz;
     sxx += dx * dx; sxy += dx * dy; sxz += dx * dz;
     syy += dy * dy; syz += dy * dz; szz += dz * dz;
     ++m;
   }
+  // p: a staged index point (w = original index), d its squared distance
+  __device__ __forceinline__ void add(const float4& p, float d) {
+    if (row) {
+      row[m] = __float_as_uint(p.w);
+      rmax = fmaxf(rmax, d);
+    }
+    take(p);
+  }
   __device__ __forceinline__ void begin(float, int) {}
-  __device__ __forceinline__ void add_key(unsigned long long k) { add(xyz[key_idx(k)], 0.f); }
+  __device__ __forceinline__ void add_key(unsigned long long k) {
+    if (row) {
+      row[m] = key_idx(k);
+      rmax = fmaxf(rmax, key_dist(k));
+    }
+    take(xyz[key_idx(k)]);
+  }
+  // The row's radius word, once every neighbour is in (K asked for).
+  __device__ __forceinline__ void finish_row(int K) {
+    if (row) row[kGraphR] = __float_as_uint(m < K ? LCR_INF : rmax);
+  }
 };
+
+__device__ __forceinline__ uint32_t* graph_row(uint32_t* rows, bool qv, float w) {
+  return rows && qv ? rows + static_cast<size_t>(__float_as_uint(w)) * 32 : nullptr;
+}
 
 __device__ __forceinline__ void normal_store(const NeAcc& a, float vx, float vy, float vz, int flip_all, uint32_t o,
                                              float4* __restrict__ onrm) {
@@ -432,7 +460,7 @@ __device__ __forceinline__ void normal_store(const NeAcc& a, float vx, float vy,
 }
 
 __global__ void k_normals(IndexView ix, int K, const float4* __restrict__ xyz, float vx, float vy, float vz,
-                          int flip_all, float4* __restrict__ onrm, EscapeQueue eq) {
+                          int flip_all, float4* __restrict__ onrm, EscapeQueue eq, uint32_t* __restrict__ rows) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned char* wbase = smem + wib * kset_warp_bytes();
@@ -443,13 +471,17 @@ __global__ void k_normals(IndexView ix, int K, const float4* __restrict__ xyz, f
   float4 tlo, thi;
   if (!tile_box(q.x, q.y, q.z, qv, tlo, thi)) return;
   NeAcc acc;
-  acc.init(q.x, q.y, q.z, xyz);
+  acc.init(q.x, q.y, q.z, xyz, graph_row(rows, qv, q.w));
   bool esc = false;
   float top = 0.f;
   tile_kset(ix, q.x, q.y, q.z, qv, K, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), wbase + sizeof(KnnWarp), tile,
             acc, 0.f, &esc, &top);
-  if (esc) escape_push(eq, static_cast<uint32_t>(tile) * 32u + lane, top);
-  else if (qv) normal_store(acc, vx, vy, vz, flip_all, __float_as_uint(q.w), onrm);
+  if (esc) {
+    escape_push(eq, static_cast<uint32_t>(tile) * 32u + lane, top);
+  } else if (qv) {
+    normal_store(acc, vx, vy, vz, flip_all, __float_as_uint(q.w), onrm);
+    acc.finish_row(K);
+  }
 }
 
 // One warp per escaped query (warps stride over the queue): the query alone
@@ -457,7 +489,8 @@ __global__ void k_normals(IndexView ix, int K, const float4* __restrict__ xyz, f
 // topped at four times the largest squared distance it met (an octave of
 // distance above its k-th, so the k-th lies inside the range).
 __global__ void k_normals_escaped(IndexView ix, int K, const float4* __restrict__ xyz, float vx, float vy, float vz,
-                                  int flip_all, float4* __restrict__ onrm, EscapeQueue eq) {
+                                  int flip_all, float4* __restrict__ onrm, EscapeQueue eq,
+                                  uint32_t* __restrict__ rows) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int nw = blockDim.x >> 5, wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned char* wbase = smem + wib * kset_warp_bytes();
@@ -470,10 +503,13 @@ __global__ void k_normals_escaped(IndexView ix, int K, const float4* __restrict_
     float4 tlo, thi;
     tile_box(qx, qy, qz, qv, tlo, thi);
     NeAcc acc;
-    acc.init(qx, qy, qz, xyz);
+    acc.init(qx, qy, qz, xyz, graph_row(rows, qv, p.w));
     tile_kset(ix, qx, qy, qz, qv, K, tlo, thi, *reinterpret_cast<KnnWarp*>(wbase), wbase + sizeof(KnnWarp),
               static_cast<int>(slot >> 5), acc, 4.f * fmaxf(eq.top[w], 1e-30f));
-    if (qv) normal_store(acc, vx, vy, vz, flip_all, __float_as_uint(p.w), onrm);
+    if (qv) {
+      normal_store(acc, vx, vy, vz, flip_all, __float_as_uint(p.w), onrm);
+      acc.finish_row(K);
+    }
     __syncwarp();
   }
 }
@@ -865,8 +901,11 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
   const int set_warps = ctx->tune.ne_warps;
   const size_t smem_set = set_warps * kset_warp_bytes();
   const int flip = (flags & LCR_NORMALS_FLIP_ALL) ? 1 : 0;
+  // the neighbour rows come from the search below (the SOR-list path selects
+  // from lists of another cloud's numbering and does not produce them)
+  const bool keep = (flags & LCR_NORMALS_KEEP_NEIGHBOURS) != 0 && k <= kGraphMaxK;
   const NbrHint* h = in->nbr;
-  if (h && k <= h->K && h->K <= kListMaxK) {
+  if (!keep && h && k <= h->K && h->K <= kListMaxK) {
     // SOR inliers: select from SOR's neighbour lists; points whose list holds
     // fewer than k inliers are searched one per warp
     char* tmp = static_cast<char*>(dev_alloc(ctx, 2 * align_up(sizeof(uint32_t) * n) + 256));
@@ -900,12 +939,19 @@ lcr_cloud* normals_run(lcr_ctx* ctx, const lcr_cloud* in, int k, const float vp[
   EscapeQueue eq{reinterpret_cast<uint32_t*>(eblk), reinterpret_cast<float*>(eblk + align_up(sizeof(uint32_t) * n)),
                  reinterpret_cast<unsigned int*>(eblk + 2 * align_up(sizeof(uint32_t) * n))};
   CUDA_TRY(cudaMemsetAsync(eq.n, 0, sizeof(unsigned int), ctx->stream));
+  uint32_t* rows = nullptr;
+  if (keep) {
+    rows = static_cast<uint32_t*>(dev_alloc(ctx, sizeof(uint32_t) * 32 * static_cast<size_t>(n)));
+    out->graph = new NbrGraph;
+    out->graph->rows = rows;
+    out->graph->k = k;
+  }
   {
     KernelTimer kt(ctx, LCR_KT_NORMALS_KNN);
     LCR_LAUNCH(ctx, k_normals, (ix.nleaf + set_warps - 1) / set_warps, set_warps * 32, smem_set, ix, k, in->xyz,
-               vp[0], vp[1], vp[2], flip, out->nrm, eq);
+               vp[0], vp[1], vp[2], flip, out->nrm, eq, rows);
     LCR_LAUNCH(ctx, k_normals_escaped, ctx->sms, set_warps * 32, smem_set, ix, k, in->xyz, vp[0], vp[1], vp[2],
-               flip, out->nrm, eq);
+               flip, out->nrm, eq, rows);
   }
   dev_free(ctx, eblk);
   out->index = share_index(in->index);  // same points in the same order

@@ -52,6 +52,8 @@ struct IcpParams {
   double teps, feps;
   int stop_iter;          // 0: off
   double stop_mse;        // stop_rms^2
+  const uint32_t* tgt_rows;  // the target's neighbour rows (NbrGraph), or null
+  int tgt_k;
 };
 
 // Per pair, device-resident across rounds.
@@ -454,17 +456,97 @@ __device__ __forceinline__ unsigned vload(const unsigned* p) { return *reinterpr
 // Last round's correspondence of a slot as a starting candidate for this
 // round's search: key (distance under the current transform, index) if it is
 // still within the cap, else "none".
+// Also returns that correspondence's index (prev, 0xffffffff: none) and its
+// squared distance under the current transform whatever the cap (dd).
 __device__ __forceinline__ void prev_candidate(const BatchDesc* __restrict__ d, const IcpParams* __restrict__ prm,
                                                int gslot, bool pv, const float3& q, unsigned long long& key,
-                                               float4& p) {
+                                               float4& p, uint32_t& prev, float& dd) {
   key = ~0ull;
   p = make_float4(0.f, 0.f, 0.f, 0.f);
-  const uint32_t prev = pv ? d->prev_ti[gslot] : 0xffffffffu;
+  dd = LCR_INF;
+  prev = pv ? d->prev_ti[gslot] : 0xffffffffu;
   if (prev == 0xffffffffu) return;
   p = prm->tgt_xyz[prev];
-  const float dd = exact_dist2(q.x, q.y, q.z, p.x, p.y, p.z);
+  dd = exact_dist2(q.x, q.y, q.z, p.x, p.y, p.z);
   if (dd <= prm->cap) key = make_key(dd, prev);
   p.w = __uint_as_float(prev);
+}
+
+// The nearest of row `row`'s k points to q: min of the (distance, index) keys,
+// uncapped.  Four indices, then their four points, are loaded before any is
+// used (two memory latencies per four points rather than one per point);
+// words past k hold no index and are replaced by the row's own point c (a
+// valid index) and masked out.
+__device__ __forceinline__ unsigned long long row_min(const uint32_t* __restrict__ row, int k, uint32_t c,
+                                                      const float4* __restrict__ xyz, const float3& q) {
+  unsigned long long b = ~0ull;
+#pragma unroll 2
+  for (int j0 = 0; j0 < 32; j0 += 4) {
+    if (j0 < k) {
+      const uint4 ta = __ldg(reinterpret_cast<const uint4*>(row + j0));
+      uint32_t t[4] = {ta.x, ta.y, ta.z, ta.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) t[u] = j0 + u < k ? t[u] : c;
+      float4 p[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) p[u] = __ldg(xyz + t[u]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const unsigned long long key = make_key(exact_dist2(q.x, q.y, q.z, p[u].x, p[u].y, p[u].z), t[u]);
+        b = key < b ? key : b;
+      }
+    }
+  }
+  return b;
+}
+
+// The capped nearest target of q proven from the target's neighbour rows,
+// without a search.  c is a target point at squared distance dc from q, and
+// R, its row's radius word, is the largest squared distance from c to the k
+// points of its row, so every target point t outside the row has
+// D(c, t) >= R.  In true distances |qt| >= |ct| - |qc|, so R > 4 dc puts every
+// such t strictly farther from q than c whenever the three rounded squared
+// distances are within a factor (1 +- 1e-5) of the true ones: each is five
+// roundings of positive terms (within 5 ulps, 3e-7), and the 1e-30 floor keeps
+// subnormal squares out of it (dc == 0: q and c agree to 1e-22 while every t
+// outside lies at least 1e-15 from c).  The 4.0001 factor holds the margin.
+// Then the nearest under the (distance, index) order lies in the row, c
+// included, and the row's minimum, capped, is the exact answer.
+// Starting from c = s (last round's correspondence): when the test fails but
+// R >= dc (within a factor 4 of passing), the row's nearest point b, strictly
+// closer in key order, is tried once more with its own row.  A lane further
+// off goes to the search at once: a few rows would not settle it, and their
+// scattered loads cost more than its share of the tile's traversal.  Returns
+// true with best = the capped answer, or false with seed = the best key met,
+// a valid first bound for the search.
+__device__ __forceinline__ bool row_proves(float R, float dc) {
+  return R > 4.0001f * dc && R >= 1e-30f && (dc == 0.f || dc >= 1e-30f);
+}
+__device__ __forceinline__ bool graph_nn(const IcpParams* __restrict__ prm, const float3& q, uint32_t s, float ds,
+                                         unsigned long long& best, unsigned long long& seed) {
+  const int k = prm->tgt_k;
+  const unsigned long long none = make_key(prm->cap, 0xffffffffu);
+  uint32_t c = s;
+  float dc = ds;
+  seed = make_key(dc, c);
+  const uint32_t* __restrict__ row = prm->tgt_rows + static_cast<size_t>(c) * 32;
+  float R = __uint_as_float(__ldg(row + kGraphR));
+  if (!(row_proves(R, dc) || R >= dc)) return false;
+  unsigned long long b = row_min(row, k, c, prm->tgt_xyz, q);
+  if (row_proves(R, dc)) {
+    best = b < none ? b : none;
+    return true;
+  }
+  if (!(b < seed)) return false;  // no closer point in the row
+  seed = b;
+  c = key_idx(b);
+  dc = key_dist(b);
+  row = prm->tgt_rows + static_cast<size_t>(c) * 32;
+  R = __uint_as_float(__ldg(row + kGraphR));
+  if (!row_proves(R, dc)) return false;
+  b = row_min(row, k, c, prm->tgt_xyz, q);
+  best = b < none ? b : none;
+  return true;
 }
 
 // 1. Tiles of the live pairs: compact ones searched and reduced to a row,
@@ -491,36 +573,56 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_search(const BatchDesc* __r
     const bool pv = finite3(pt.x, pt.y, pt.z);
     float3 q = make_float3(0.f, 0.f, 0.f);
     if (pv) q = xf_apply(pcs[wib].T, pt.x, pt.y, pt.z);
-    float4 tlo, thi;
-    if (!tile_box(q.x, q.y, q.z, pv, tlo, thi)) {
-      d->tile_part[gslot] = 0.f;
-      continue;
-    }
     const float cap = prm->cap;
-    const float dx = thi.x - tlo.x, dy = thi.y - tlo.y, dz = thi.z - tlo.z;
-    if (dx * dx + dy * dy + dz * dz > 16.f * cap) {
-      const unsigned valid = __ballot_sync(LCR_FULL, pv);
-      unsigned base = 0;
-      if (lane == 0) {
-        base = atomicAdd(&cnt->nhard, static_cast<unsigned>(__popc(valid)));
-        d->wide_tiles[atomicAdd(&cnt->nwide, 1u)] = static_cast<uint32_t>(g);
-      }
-      base = __shfl_sync(LCR_FULL, base, 0);
-      if (pv) d->hard_q[base + __popc(valid & ((1u << lane) - 1u))] = static_cast<uint32_t>(gslot);
-      continue;
-    }
-    NN1 v;
-    v.init(q.x, q.y, q.z, pv, cap, wss[wib]);
     unsigned long long sk;
     float4 sp;
-    prev_candidate(d, prm, gslot, pv, q, sk, sp);
-    v.seed(sk);
-    tile_traverse(pcs[wib].tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), wss[wib]);
-    d->prev_ti[gslot] = key_idx(v.best);
-    const bool found = pv && v.found();
-    const float4 tp = found ? prm->tgt_xyz[key_idx(v.best)] : make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t prev;
+    float ds;
+    prev_candidate(d, prm, gslot, pv, q, sk, sp, prev, ds);
+    // lanes whose correspondence follows from the target's neighbour rows
+    unsigned long long best = make_key(cap, 0xffffffffu);
+    bool settled = false;
+    if (prm->tgt_rows != nullptr && prev != 0xffffffffu) {
+      unsigned long long g;
+      settled = graph_nn(prm, q, prev, ds, best, g);
+      if (!settled && g < sk) sk = g;  // a closer first bound for the search
+    }
+    const bool sv = pv && !settled;  // still to search
+    float4 tlo, thi;
+    if (tile_box(q.x, q.y, q.z, sv, tlo, thi)) {
+      const float dx = thi.x - tlo.x, dy = thi.y - tlo.y, dz = thi.z - tlo.z;
+      if (dx * dx + dy * dy + dz * dz > 16.f * cap) {
+        // the lanes still to search go one per warp; the settled ones leave
+        // their results in the per-slot arrays for the tile's row
+        const unsigned valid = __ballot_sync(LCR_FULL, sv);
+        unsigned base = 0;
+        if (lane == 0) {
+          base = atomicAdd(&cnt->nhard, static_cast<unsigned>(__popc(valid)));
+          d->wide_tiles[atomicAdd(&cnt->nwide, 1u)] = static_cast<uint32_t>(g);
+        }
+        base = __shfl_sync(LCR_FULL, base, 0);
+        if (sv) d->hard_q[base + __popc(valid & ((1u << lane) - 1u))] = static_cast<uint32_t>(gslot);
+        if (settled) {
+          const uint32_t ti = key_idx(best);
+          const float4 tp = ti != 0xffffffffu ? prm->tgt_xyz[ti] : make_float4(0.f, 0.f, 0.f, 0.f);
+          d->hard_tp[gslot] = make_float4(tp.x, tp.y, tp.z, key_dist(best));
+          d->hard_ti[gslot] = ti;
+          d->prev_ti[gslot] = ti;
+        }
+        continue;
+      }
+      NN1 v;
+      v.init(q.x, q.y, q.z, sv, cap, wss[wib]);
+      v.seed(sk);
+      tile_traverse(pcs[wib].tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z),
+                    wss[wib]);
+      if (sv) best = v.best;
+    }
+    d->prev_ti[gslot] = key_idx(best);
+    const bool found = pv && key_idx(best) != 0xffffffffu;
+    const float4 tp = found ? prm->tgt_xyz[key_idx(best)] : make_float4(0.f, 0.f, 0.f, 0.f);
     float t[32];
-    corr_terms<P2PL>(t, found, q, tp, key_dist(v.best), key_idx(v.best), prm);
+    corr_terms<P2PL>(t, found, q, tp, key_dist(best), key_idx(best), prm);
     d->tile_part[gslot] = reduce_scatter32(t, lane);
   }
 }
@@ -548,7 +650,9 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_hard(const BatchDesc* __res
     const float3 q = xf_apply(pcs[wib].T, pt.x, pt.y, pt.z);
     unsigned long long sk;
     float4 sp;
-    prev_candidate(d, prm, static_cast<int>(gslot), true, q, sk, sp);
+    uint32_t prev;
+    float ds;
+    prev_candidate(d, prm, static_cast<int>(gslot), true, q, sk, sp, prev, ds);
     unsigned long long best;
     float4 bp;
     warp_query_nn(pcs[wib].tgt, q.x, q.y, q.z, prm->cap, wss[wib], best, bp, sk, sp);
@@ -714,7 +818,9 @@ __global__ void __launch_bounds__(kIcpThreads) k_fitness(const BatchDesc* __rest
       v.init(q.x, q.y, q.z, pv, prm->cap, wss[wib]);
       unsigned long long sk;
       float4 sp;
-      prev_candidate(d, prm, gslot, pv, q, sk, sp);
+      uint32_t prev;
+      float ds;
+      prev_candidate(d, prm, gslot, pv, q, sk, sp, prev, ds);
       v.seed(sk);
       tile_traverse(pcs[wib].tgt, v, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z),
                     wss[wib]);
@@ -1023,6 +1129,10 @@ void icp_batch_run(lcr_ctx* ctx, const lcr_cloud* const* src, const lcr_cloud* c
     q.feps = p->euclidean_fitness_epsilon;
     q.stop_iter = p->stop_iteration;
     q.stop_mse = p->stop_rms * p->stop_rms;
+    if (tgt[i]->graph) {
+      q.tgt_rows = tgt[i]->graph->rows;
+      q.tgt_k = tgt[i]->graph->k;
+    }
     tile0[i] = tiles;
     chunk0[i] = chunks;
     tiles += si.v.nleaf;

@@ -86,6 +86,22 @@ struct NbrHint {
   int n_src = 0;
 };
 
+// The exact k nearest neighbours NormalEstimation found for every point of its
+// output cloud (LCR_NORMALS_KEEP_NEIGHBOURS, k <= kGraphMaxK).  Row i (32
+// words, 128 B) holds in words [0, k) the original indices of point i's k
+// nearest, itself included, in no particular order, and in word kGraphR the
+// largest squared distance among them as float bits (+inf when the cloud has
+// fewer than k finite points, so that the row lists all of them).  Rows of
+// non-finite points are not written: such a point is never a neighbour or a
+// correspondence.  ICP against the cloud proves most correspondences from
+// these rows instead of searching (icp.cu, k_icp_search).
+constexpr int kGraphMaxK = 31;
+constexpr int kGraphR = 31;
+struct NbrGraph {
+  uint32_t* rows = nullptr;     // [n][32]
+  int k = 0;
+};
+
 struct lcr_cloud {
   size_t n = 0;
   float4* xyz = nullptr;        // x y z 0
@@ -93,6 +109,7 @@ struct lcr_cloud {
   uint32_t* rgb = nullptr;      // packed b g r a (little-endian PCL rgba)
   Index* index = nullptr;       // built on first search, freed with the cloud
   NbrHint* nbr = nullptr;       // SOR inliers only: their source's neighbour lists
+  NbrGraph* graph = nullptr;    // normals output with LCR_NORMALS_KEEP_NEIGHBOURS only
 };
 
 struct lcr_ctx {
@@ -152,6 +169,41 @@ void sync(lcr_ctx* ctx);
 __device__ __forceinline__ float exact_dist2(float qx, float qy, float qz, float px, float py, float pz) {
   const float d0 = __fsub_rn(qx, px), d1 = __fsub_rn(qy, py), d2 = __fsub_rn(qz, pz);
   return __fadd_rn(__fadd_rn(__fmul_rn(d0, d0), __fmul_rn(d1, d1)), __fmul_rn(d2, d2));
+}
+
+// Paired FP32 (sm_100 family): two IEEE single-precision operations in one
+// instruction on a 64-bit register holding {low half, high half}, each half
+// rounded to nearest like the scalar __fsub_rn / __fmul_rn.  A paired product
+// feeding a paired add may still be fused into a paired FMA by the assembler
+// (an exact_dist2 one ulp off was observed), so sums of products stay scalar
+// __fadd_rn, which is never fused.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f32x2_dup(float a) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(a));
+  return r;
+}
+__device__ __forceinline__ float f32x2_lo(f32x2 v) { return __uint_as_float(static_cast<uint32_t>(v)); }
+__device__ __forceinline__ float f32x2_hi(f32x2 v) { return __uint_as_float(static_cast<uint32_t>(v >> 32)); }
+__device__ __forceinline__ f32x2 f32x2_sub(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f32x2_mul(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+// exact_dist2 of one query (each coordinate duplicated into both halves) to
+// two points (x, y, z pairs): differences and squares paired, the two sums
+// scalar; d0 and d1 are bit-identical to exact_dist2 of the low and high point.
+__device__ __forceinline__ void exact_dist2_x2(f32x2 qx, f32x2 qy, f32x2 qz, f32x2 px, f32x2 py, f32x2 pz, float& d0,
+                                               float& d1) {
+  const f32x2 e0 = f32x2_sub(qx, px), e1 = f32x2_sub(qy, py), e2 = f32x2_sub(qz, pz);
+  const f32x2 s0 = f32x2_mul(e0, e0), s1 = f32x2_mul(e1, e1), s2 = f32x2_mul(e2, e2);
+  d0 = __fadd_rn(__fadd_rn(f32x2_lo(s0), f32x2_lo(s1)), f32x2_lo(s2));
+  d1 = __fadd_rn(__fadd_rn(f32x2_hi(s0), f32x2_hi(s1)), f32x2_hi(s2));
 }
 
 // Lower bound of exact_dist2 over every point inside [lo, hi]: each per-axis gap

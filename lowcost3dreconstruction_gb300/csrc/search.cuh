@@ -21,10 +21,21 @@
 // node pushes at most 32 children): 1 + 31 * top <= 156 for top <= 5.
 constexpr int kStack = 32 * (kMaxLevels - 1) + 8;
 
+// A leaf's 32 points by coordinate: one 16-byte shared load gives the same
+// coordinate of four consecutive points, i.e. two ready pairs for the paired
+// FP32 distance.
+struct SoaStage {
+  float x[32], y[32], z[32];
+  uint32_t i[32];
+};
+
 struct WarpScratch {
   uint32_t node[kStack];
   float d[kStack];
-  float4 stage[32];
+  union {  // one layout per visitor (stages_soa)
+    float4 stage[32];
+    SoaStage soa;
+  };
   // Four sub-tiles of 8 consecutive lanes (nearby along the Hilbert order):
   // their boxes and largest per-lane radii.  A node must come within the
   // radius of some sub-tile, so a tile whose 32 queries straddle two distant
@@ -80,11 +91,64 @@ __device__ __forceinline__ float subtile_metric(const float4& lo, const float4& 
   return m;
 }
 
+// A visitor that declares `static constexpr bool kSoa = true` receives the
+// staged leaf as a SoaStage, every other one as float4[32].
+template <class V, class = void>
+struct stages_soa {
+  static constexpr bool value = false;
+};
+template <class V>
+struct stages_soa<V, decltype(void(V::kSoa))> {
+  static constexpr bool value = V::kSoa;
+};
+
+// Stages leaf `id` of ix for the warp (each lane one point, coalesced).
+template <bool Soa>
+__device__ __forceinline__ void stage_leaf(const IndexView& ix, int id, WarpScratch& ws) {
+  const int lane = threadIdx.x & 31;
+  const float4 p = ix.pts[static_cast<size_t>(id) * 32 + lane];
+  if constexpr (Soa) {
+    ws.soa.x[lane] = p.x;
+    ws.soa.y[lane] = p.y;
+    ws.soa.z[lane] = p.z;
+    ws.soa.i[lane] = __float_as_uint(p.w);
+  } else {
+    ws.stage[lane] = p;
+  }
+}
+
+// Stages leaf `id` in the visitor's layout and lets the lanes that need it
+// scan it (warp-uniform call).
+template <class V>
+__device__ __forceinline__ void scan_staged(const IndexView& ix, int id, bool need, V& vis, WarpScratch& ws) {
+  constexpr bool soa = stages_soa<V>::value;
+  stage_leaf<soa>(ix, id, ws);
+  __syncwarp();
+  if (need) {
+    if constexpr (soa) vis.scan(ws.soa);
+    else vis.scan(ws.stage);
+  }
+  __syncwarp();
+}
+
+// The exact_dist2 of one query to staged points j .. j+3 (j a multiple of 4).
+__device__ __forceinline__ void soa_dist4(const SoaStage& st, int j, f32x2 qx, f32x2 qy, f32x2 qz, float (&d)[4]) {
+  const ulonglong2 x = *reinterpret_cast<const ulonglong2*>(st.x + j);
+  const ulonglong2 y = *reinterpret_cast<const ulonglong2*>(st.y + j);
+  const ulonglong2 z = *reinterpret_cast<const ulonglong2*>(st.z + j);
+  exact_dist2_x2(qx, qy, qz, x.x, y.x, z.x, d[0], d[1]);
+  exact_dist2_x2(qx, qy, qz, x.y, y.y, z.y, d[2], d[3]);
+}
+__device__ __forceinline__ float4 soa_point(const SoaStage& st, int j) {
+  return make_float4(st.x[j], st.y[j], st.z[j], __uint_as_float(st.i[j]));
+}
+
 // Visitor contract (per-lane state, warp-synchronous calls):
 //   float metric(lo, hi)  warp-level pruning metric of a node (tile vs box)
 //   bool  still(m)        node with metric m may still hold useful points
 //   bool  need(lo, hi)    this lane needs the leaf
-//   void  scan(stage)     this lane scans the 32 staged points
+//   void  scan(stage)     this lane scans the 32 staged points (float4[32],
+//                         or the SoaStage of a kSoa visitor)
 //   void  visited(leaf)   warp-uniform notification after a leaf was scanned
 //   void  refresh()       recompute the warp-level radius after a scan
 template <class V>
@@ -110,10 +174,7 @@ __device__ __forceinline__ void tile_traverse(const IndexView& ix, V& vis, float
       const float4 lo = ix.lo[0][id], hi = ix.hi[0][id];
       const bool need = vis.need(lo, hi);
       if (!__any_sync(LCR_FULL, need)) continue;
-      ws.stage[lane] = ix.pts[static_cast<size_t>(id) * 32 + lane];
-      __syncwarp();
-      if (need) vis.scan(ws.stage);
-      __syncwarp();
+      scan_staged(ix, id, need, vis, ws);
       vis.visited(id);
       vis.refresh();
     } else {
@@ -205,16 +266,25 @@ struct NN1 {
   // Four independent minimum chains over the 32 staged points, merged at the
   // end: keys are unique (the index is part of them), so the minimum is the
   // same whatever the grouping, and the loop no longer waits on one serial
-  // compare-and-select chain.
-  __device__ __forceinline__ void scan(const float4* st) {
+  // compare-and-select chain.  The distances are computed two at a time in
+  // paired FP32 (bit-identical to exact_dist2) from the coordinate-major stage.
+  static constexpr bool kSoa = true;
+  __device__ __forceinline__ void scan(const SoaStage& st) {
+    const f32x2 qx2 = f32x2_dup(qx), qy2 = f32x2_dup(qy), qz2 = f32x2_dup(qz);
     unsigned long long b0 = best, b1 = best, b2 = best, b3 = best;
-#pragma unroll 2
+#pragma unroll
     for (int j = 0; j < 32; j += 4) {
-      const float4 p0 = st[j], p1 = st[j + 1], p2 = st[j + 2], p3 = st[j + 3];
-      const unsigned long long k0 = make_key(exact_dist2(qx, qy, qz, p0.x, p0.y, p0.z), __float_as_uint(p0.w));
-      const unsigned long long k1 = make_key(exact_dist2(qx, qy, qz, p1.x, p1.y, p1.z), __float_as_uint(p1.w));
-      const unsigned long long k2 = make_key(exact_dist2(qx, qy, qz, p2.x, p2.y, p2.z), __float_as_uint(p2.w));
-      const unsigned long long k3 = make_key(exact_dist2(qx, qy, qz, p3.x, p3.y, p3.z), __float_as_uint(p3.w));
+      const ulonglong2 x = *reinterpret_cast<const ulonglong2*>(st.x + j);
+      const ulonglong2 y = *reinterpret_cast<const ulonglong2*>(st.y + j);
+      const ulonglong2 z = *reinterpret_cast<const ulonglong2*>(st.z + j);
+      const uint4 id = *reinterpret_cast<const uint4*>(st.i + j);
+      float e0, e1, e2, e3;
+      exact_dist2_x2(qx2, qy2, qz2, x.x, y.x, z.x, e0, e1);
+      exact_dist2_x2(qx2, qy2, qz2, x.y, y.y, z.y, e2, e3);
+      const unsigned long long k0 = make_key(e0, id.x);
+      const unsigned long long k1 = make_key(e1, id.y);
+      const unsigned long long k2 = make_key(e2, id.z);
+      const unsigned long long k3 = make_key(e3, id.w);
       b0 = k0 < b0 ? k0 : b0;
       b1 = k1 < b1 ? k1 : b1;
       b2 = k2 < b2 ? k2 : b2;
@@ -411,17 +481,15 @@ struct KHist {
   __device__ __forceinline__ bool need(const float4& lo, const float4& hi) const {
     return qv && box_dist2(lo, hi, qx, qy, qz) <= bound();
   }
-  __device__ __forceinline__ void scan(const float4* st) {
+  static constexpr bool kSoa = true;
+  __device__ __forceinline__ void scan(const SoaStage& st) {
     float tau = bound();
+    const f32x2 qx2 = f32x2_dup(qx), qy2 = f32x2_dup(qy), qz2 = f32x2_dup(qz);
     for (int j0 = 0; j0 < 32; j0 += 4) {
-      // four independent distances first (the staged loads and the FP32
-      // chains overlap), then the order-dependent histogram updates
+      // four independent distances first (paired FP32 from the staged
+      // coordinates), then the order-dependent histogram updates
       float dd[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const float4 p = st[j0 + u];
-        dd[u] = exact_dist2(qx, qy, qz, p.x, p.y, p.z);
-      }
+      soa_dist4(st, j0, qx2, qy2, qz2, dd);
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
       const float d = dd[u];
@@ -466,10 +534,7 @@ struct KHist {
     const float4 lo = ix.lo[0][id], hi = ix.hi[0][id];
     const bool nd = need(lo, hi);
     if (!__any_sync(LCR_FULL, nd)) return;
-    ws.stage[lane] = ix.pts[static_cast<size_t>(id) * 32 + lane];
-    __syncwarp();
-    if (nd) scan(ws.stage);
-    __syncwarp();
+    scan_staged(ix, id, nd, *this, ws);
     visited(id);
     refresh();
   }
@@ -494,24 +559,29 @@ struct KCollect {
   __device__ __forceinline__ bool need(const float4& lo, const float4& hi) const {
     return qv && box_dist2(lo, hi, qx, qy, qz) <= tau;
   }
-  __device__ __forceinline__ void scan(const float4* st) {
-    for (int j = 0; j < 32; ++j) {
-      const float4 p = st[j];
-      const float d = exact_dist2(qx, qy, qz, p.x, p.y, p.z);
-      if (!(d <= tau)) continue;
-      const unsigned long long k = make_key(d, __float_as_uint(p.w));
-      if (!insert) {
-        buf[cnt * 32 + lane] = k;
-        ++cnt;
-      } else if (k < buf[(K - 1) * 32 + lane]) {
-        int pos = K - 1;
-        while (pos > 0) {
-          const unsigned long long prev = buf[(pos - 1) * 32 + lane];
-          if (prev <= k) break;
-          buf[pos * 32 + lane] = prev;
-          --pos;
+  static constexpr bool kSoa = true;
+  __device__ __forceinline__ void scan(const SoaStage& st) {
+    const f32x2 qx2 = f32x2_dup(qx), qy2 = f32x2_dup(qy), qz2 = f32x2_dup(qz);
+    for (int j0 = 0; j0 < 32; j0 += 4) {
+      float dd[4];
+      soa_dist4(st, j0, qx2, qy2, qz2, dd);
+      for (int u = 0; u < 4; ++u) {
+        const float d = dd[u];
+        if (!(d <= tau)) continue;
+        const unsigned long long k = make_key(d, st.i[j0 + u]);
+        if (!insert) {
+          buf[cnt * 32 + lane] = k;
+          ++cnt;
+        } else if (k < buf[(K - 1) * 32 + lane]) {
+          int pos = K - 1;
+          while (pos > 0) {
+            const unsigned long long prev = buf[(pos - 1) * 32 + lane];
+            if (prev <= k) break;
+            buf[pos * 32 + lane] = prev;
+            --pos;
+          }
+          buf[pos * 32 + lane] = k;
         }
-        buf[pos * 32 + lane] = k;
       }
     }
   }
@@ -588,17 +658,13 @@ __device__ __forceinline__ void knn_pass1(const IndexView& ix, float qx, float q
 template <class V>
 __device__ __forceinline__ void knn_pass2(const IndexView& ix, const KHist& h, V& vis, const float4& tlo,
                                           const float4& thi, KnnWarp& kw) {
-  const int lane = threadIdx.x & 31;
   if (h.nleaves <= kLeafList) {
     for (int l = 0; l < h.nleaves; ++l) {
       const int id = static_cast<int>(kw.leaves[l]);
       const float4 lo = ix.lo[0][id], hi = ix.hi[0][id];
       const bool nd = vis.need(lo, hi);
       if (!__any_sync(LCR_FULL, nd)) continue;
-      kw.ws.stage[lane] = ix.pts[static_cast<size_t>(id) * 32 + lane];
-      __syncwarp();
-      if (nd) vis.scan(kw.ws.stage);
-      __syncwarp();
+      scan_staged(ix, id, nd, vis, kw.ws);
     }
   } else {
     tile_traverse(ix, vis, 0.5f * (tlo.x + thi.x), 0.5f * (tlo.y + thi.y), 0.5f * (tlo.z + thi.z), kw.ws);
@@ -692,15 +758,20 @@ struct KRefine {
   __device__ __forceinline__ bool need(const float4& lo, const float4& hi) const {
     return active && box_dist2(lo, hi, qx, qy, qz) <= tau;
   }
-  __device__ __forceinline__ void scan(const float4* st) {
-#pragma unroll 4
-    for (int j = 0; j < 32; ++j) {
-      const float4 p = st[j];
-      const float d = exact_dist2(qx, qy, qz, p.x, p.y, p.z);
-      if (!(d <= tau)) continue;
-      const unsigned long long k = make_key(d, __float_as_uint(p.w));
-      if (k < klo || k > khi) continue;
-      hist[static_cast<int>((k - klo) >> sh) * 32 + lane] += 1u;
+  static constexpr bool kSoa = true;
+  __device__ __forceinline__ void scan(const SoaStage& st) {
+    const f32x2 qx2 = f32x2_dup(qx), qy2 = f32x2_dup(qy), qz2 = f32x2_dup(qz);
+    for (int j0 = 0; j0 < 32; j0 += 4) {
+      float dd[4];
+      soa_dist4(st, j0, qx2, qy2, qz2, dd);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float d = dd[u];
+        if (!(d <= tau)) continue;
+        const unsigned long long k = make_key(d, st.i[j0 + u]);
+        if (k < klo || k > khi) continue;
+        hist[static_cast<int>((k - klo) >> sh) * 32 + lane] += 1u;
+      }
     }
   }
   __device__ __forceinline__ bool skip(int) const { return false; }
@@ -729,23 +800,19 @@ struct KSet {
   __device__ __forceinline__ bool need(const float4& lo, const float4& hi) const {
     return qv && box_dist2(lo, hi, qx, qy, qz) <= tau;
   }
-  __device__ __forceinline__ void scan(const float4* st) {
+  static constexpr bool kSoa = true;
+  __device__ __forceinline__ void scan(const SoaStage& st) {
+    const f32x2 qx2 = f32x2_dup(qx), qy2 = f32x2_dup(qy), qz2 = f32x2_dup(qz);
     for (int j0 = 0; j0 < 32; j0 += 4) {
-      float4 pp[4];
       float dd[4];
+      soa_dist4(st, j0, qx2, qy2, qz2, dd);
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        pp[u] = st[j0 + u];
-        dd[u] = exact_dist2(qx, qy, qz, pp[u].x, pp[u].y, pp[u].z);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-      const float4 p = pp[u];
       const float d = dd[u];
       if (!(d <= tau)) continue;
-      const unsigned long long k = make_key(d, __float_as_uint(p.w));
+      const unsigned long long k = make_key(d, st.i[j0 + u]);
       if (k < klo) {
-        acc->add(p, d);
+        acc->add(soa_point(st, j0 + u), d);
       } else if (k <= khi) {
         if (nb < kBoundCap) bbuf[nb * 32 + lane] = k;
         ++nb;

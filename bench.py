@@ -902,11 +902,15 @@ class Config4:
         return dict(views=views, T=self.T[i].astype(np.float64))
 
 
+PRE_STREAMS = 12  # contexts (streams) the config-4 preprocessing deals its views to (throughput levels off near 12)
+
+
 def config4_clouds(ctxs, c4: Config4, from_host: bool = False, k: int = 30):
     """Back-projection and NormalEstimation (k = 30) of every view, the views
-    split between the contexts (one host thread each, so the two halves
-    overlap on the device).  Returns (sources, targets) in pair order; every
-    context's work is complete on return."""
+    dealt round-robin to the contexts (one host thread and one stream each, so
+    that several views' launches run on the device at once).  Returns
+    (sources, targets) in pair order; every context's work is complete on
+    return."""
     from concurrent.futures import ThreadPoolExecutor
     n = c4.npairs
     out = [None] * (2 * n)
@@ -945,7 +949,9 @@ def config4_arm(args, rank: int, world: int, dist) -> dict | None:
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    ctxs = [Context(dev), Context(dev)]
+    # preprocessing contexts: one host thread and one stream each, so that the
+    # per-view launches of several views overlap on the device
+    ctxs = [Context(dev) for _ in range(PRE_STREAMS)]
     ctx = ctxs[0]
     streams = [torch.cuda.ExternalStream(c.stream, device=dev) for c in ctxs]
     c4 = Config4(ctx, dev, npairs=args.pairs or 512, seed=4 + rank)
@@ -957,11 +963,13 @@ def config4_arm(args, rank: int, world: int, dist) -> dict | None:
     def preprocess(from_host: bool):
         ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ea.record(streams[0])
-        streams[1].wait_event(ea)
+        for st in streams[1:]:
+            st.wait_event(ea)
         srcs, tgts = config4_clouds(ctxs, c4, from_host=from_host)
-        done = torch.cuda.Event()
-        done.record(streams[1])
-        streams[0].wait_event(done)
+        for st in streams[1:]:
+            done = torch.cuda.Event()
+            done.record(st)
+            streams[0].wait_event(done)
         eb.record(streams[0])
         eb.synchronize()
         return srcs, tgts, ea.elapsed_time(eb)
@@ -1125,7 +1133,8 @@ def config4_arm(args, rank: int, world: int, dist) -> dict | None:
             "rmse_limit_m": RMSE_LIMIT,
             "l2": "inputs (%.1f GB of depth images) larger than L2; 256 MB flush before every stage" % (
                 c4.image_bytes() / 1e9),
-            "launch_shapes": ctx.tune_get()},
+            "launch_shapes": ctx.tune_get(),
+            "preprocess_streams": len(ctxs)},
         "roofline": {"kernel": "k_icp_search<1> (one ICP round's correspondence search over every live pair)",
                      "bound": "hbm", "achieved": round(achieved, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / pk["hbm_gbs"], 5), "peak_src": pk["src"],

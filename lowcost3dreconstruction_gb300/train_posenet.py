@@ -240,6 +240,59 @@ def settled(r, max_rms: float = 0.004) -> bool:
     return bool(r.converged) and r.state != L.ICP_STATE_NO_CORRESPONDENCES and r.mse <= max_rms * max_rms
 
 
+def propose_refine(ctx: Context, net: PoseNet, srcs, tgts, ctx2: Context | None = None):
+    """The proposal pipeline: the learned proposal, point-to-plane ICP at 2 cm
+    then 1 cm (refine with proposal_params), and plain ICP from the centroid
+    guess (refine with eval_params) as the fallback for every pair that did
+    not settle; a fallback result replaces the pair's only if it settled.
+    Returns (results, number of fallback pairs).
+
+    A pair the 2 cm stage ended (stopped, or left without correspondences)
+    skips the 1 cm stage, so its result is known once that stage returns.
+    With a second context, the fallback of those pairs runs on it while the
+    1 cm stage runs on ctx (two host threads).  Every pair's result is the one
+    the sequential order gives: a batched ICP call gives each pair its
+    single-pair result, and a centroid guess depends on its own pair only."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    P = net.propose(srcs, tgts)
+    coarse = ctx.icp_batch(srcs, tgts, proposal_params(), P)
+    go = [i for i, r in enumerate(coarse) if r.state not in (L.ICP_STATE_STOPPED, L.ICP_STATE_NO_CORRESPONDENCES)]
+    res = list(coarse)
+    gos = set(go)
+    early = [i for i in range(len(srcs)) if i not in gos and not settled(coarse[i])]
+    late: list[int] = []
+
+    def fallback(c: Context, idx: list[int], G: np.ndarray):
+        return refine(c, [srcs[i] for i in idx], [tgts[i] for i in idx], G) if idx else []
+
+    def fine_then_late():
+        if go:
+            start = np.stack([coarse[i].transform for i in go])
+            fine = ctx.icp_batch([srcs[i] for i in go], [tgts[i] for i in go], fine_params(), start)
+            for i, f in zip(go, fine):
+                if f.state != L.ICP_STATE_NO_CORRESPONDENCES:
+                    res[i] = f
+        late.extend(i for i in go if not settled(res[i]))
+        G = centroid_guesses(net, [srcs[i] for i in late], [tgts[i] for i in late]) if late else None
+        return fallback(ctx, late, G)
+
+    G_early = centroid_guesses(net, [srcs[i] for i in early], [tgts[i] for i in early]) if early else None
+    if ctx2 is None:
+        fb_early = fallback(ctx, early, G_early)
+        fb_late = fine_then_late()
+    else:
+        with ThreadPoolExecutor(max_workers=2) as ex:
+            f_early = ex.submit(fallback, ctx2, early, G_early)
+            fb_late = fine_then_late()
+            fb_early = f_early.result()
+    for idx, fb in ((early, fb_early), (late, fb_late)):
+        for j, i in enumerate(idx):
+            if settled(fb[j]):
+                res[i] = fb[j]
+    return res, len(early) + len(late)
+
+
 def evaluate(ctx: Context, net: PoseNet, npairs: int = 2000, seed: int = 987_654_321, points: int = EVAL_POINTS,
              chunk: int = 500, yaw_deg: float = 180.0) -> EvalResult:
     """Plain ICP from centroid alignment vs proposal + ICP on held-out pairs; plain ICP from the centroid

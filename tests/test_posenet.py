@@ -273,3 +273,35 @@ def test_oracle_reproduces_the_committed_fixture():
     np.testing.assert_array_equal(argmax, g["argmax"])
     np.testing.assert_allclose(feat, g["feat"], rtol=1e-5, atol=1e-6)
     np.testing.assert_allclose(y, g["y"], rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.gpu
+def test_overlapped_fallback_equals_the_sequential_pipeline(ctx):
+    """propose_refine with a second context (the fallback of the pairs the
+    2 cm stage ended runs beside the 1 cm stage) gives every pair the result
+    of the sequential order, field for field."""
+    from lowcost3dreconstruction_gb300 import train_posenet as TP
+    from lowcost3dreconstruction_gb300.core import Context
+    from lowcost3dreconstruction_gb300.posenet import WEIGHTS, PoseNet
+    net = PoseNet(ctx)
+    net.load(WEIGHTS)
+    srcs, tgts, _ = ctx.synthetic_pairs(424_242, 96, 8000, yaw_deg=180.0)
+    # the sequential pipeline, written out
+    seq = TP.refine(ctx, srcs, tgts, net.propose(srcs, tgts), TP.proposal_params())
+    weak = [i for i, r in enumerate(seq) if not TP.settled(r)]
+    fb = TP.refine(ctx, [srcs[i] for i in weak], [tgts[i] for i in weak],
+                   TP.centroid_guesses(net, [srcs[i] for i in weak], [tgts[i] for i in weak]))
+    for j, i in enumerate(weak):
+        if TP.settled(fb[j]):
+            seq[i] = fb[j]
+    ctx2 = Context(0)
+    try:
+        for other in (None, ctx2):
+            res, nfb = TP.propose_refine(ctx, net, srcs, tgts, other)
+            assert nfb == len(weak) and nfb > 10
+            for a, b in zip(res, seq):
+                np.testing.assert_array_equal(a.transform64, b.transform64)
+                assert (a.converged, a.iterations, a.state, a.n_correspondences, a.mse, a.fitness) == \
+                    (b.converged, b.iterations, b.state, b.n_correspondences, b.mse, b.fitness)
+    finally:
+        ctx2.close()

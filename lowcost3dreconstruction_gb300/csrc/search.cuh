@@ -42,6 +42,7 @@ struct WarpScratch {
   // surfaces does not admit everything between them.
   float4 sub_lo[4], sub_hi[4];
   float sub_r[4];
+  uint8_t qown[32];  // compacted leaf scans: lane of the r-th lane that needs the leaf
 };
 
 __device__ __forceinline__ void subtile_setup(float x, float y, float z, bool v, WarpScratch& ws) {
@@ -117,6 +118,17 @@ __device__ __forceinline__ void stage_leaf(const IndexView& ix, int id, WarpScra
   }
 }
 
+// A visitor with `static constexpr bool kWarpScan = true` scans a leaf with
+// the whole warp (scan_warp(stage, need), called by every lane).
+template <class V, class = void>
+struct scans_warp {
+  static constexpr bool value = false;
+};
+template <class V>
+struct scans_warp<V, decltype(void(V::kWarpScan))> {
+  static constexpr bool value = V::kWarpScan;
+};
+
 // Stages leaf `id` in the visitor's layout and lets the lanes that need it
 // scan it (warp-uniform call).
 template <class V>
@@ -124,7 +136,9 @@ __device__ __forceinline__ void scan_staged(const IndexView& ix, int id, bool ne
   constexpr bool soa = stages_soa<V>::value;
   stage_leaf<soa>(ix, id, ws);
   __syncwarp();
-  if (need) {
+  if constexpr (scans_warp<V>::value) {
+    vis.scan_warp(ws.soa, need);
+  } else if (need) {
     if constexpr (soa) vis.scan(ws.soa);
     else vis.scan(ws.stage);
   }
@@ -293,6 +307,52 @@ struct NN1 {
     b0 = b1 < b0 ? b1 : b0;
     b2 = b3 < b2 ? b3 : b2;
     best = b2 < b0 ? b2 : b0;
+  }
+  // Warp-collective form (every lane calls it).  When more than 16 lanes need
+  // the leaf, each of them scans all 32 points (scan).  Otherwise the needing
+  // lanes are spread over the warp: each is served by g = 2, 4 or 8 lanes
+  // (the most that fit), which scan 32/g points apiece, and a shuffle tree
+  // hands the owner its group's minimum key.  The minimum does not depend on
+  // how the points are grouped, so the result is the same.
+  static constexpr bool kWarpScan = true;
+  __device__ __forceinline__ void scan_warp(const SoaStage& st, bool need) {
+    const unsigned mask = __ballot_sync(LCR_FULL, need);
+    const int nq = __popc(mask);
+    if (nq > 16) {
+      if (need) scan(st);
+      return;
+    }
+    const int lane = threadIdx.x & 31;
+    const int lg = nq <= 4 ? 3 : (nq <= 8 ? 2 : 1);    // log2 of the lanes per needing lane
+    const int r = __popc(mask & ((1u << lane) - 1u));  // rank among the needing lanes
+    if (need) ws->qown[r] = static_cast<uint8_t>(lane);
+    __syncwarp();
+    const int qi = lane >> lg;
+    const int owner = qi < nq ? static_cast<int>(ws->qown[qi]) : lane;
+    const f32x2 x2 = f32x2_dup(__shfl_sync(LCR_FULL, qx, owner));
+    const f32x2 y2 = f32x2_dup(__shfl_sync(LCR_FULL, qy, owner));
+    const f32x2 z2 = f32x2_dup(__shfl_sync(LCR_FULL, qz, owner));
+    const int per = 32 >> lg;  // 16, 8 or 4 points
+    const int j0 = (lane & ((1 << lg) - 1)) * per;
+    unsigned long long b = ~0ull;
+#pragma unroll 4
+    for (int j = j0; j < j0 + per; j += 4) {
+      float d[4];
+      soa_dist4(st, j, x2, y2, z2, d);
+      const uint4 id = *reinterpret_cast<const uint4*>(st.i + j);
+      const unsigned long long k0 = make_key(d[0], id.x), k1 = make_key(d[1], id.y);
+      const unsigned long long k2 = make_key(d[2], id.z), k3 = make_key(d[3], id.w);
+      const unsigned long long m01 = k1 < k0 ? k1 : k0, m23 = k3 < k2 ? k3 : k2;
+      const unsigned long long m = m23 < m01 ? m23 : m01;
+      b = m < b ? m : b;
+    }
+    for (int o = 1; o < (1 << lg); o <<= 1) {
+      const unsigned long long t = __shfl_xor_sync(LCR_FULL, b, o);
+      b = t < b ? t : b;
+    }
+    const unsigned long long gb = __shfl_sync(LCR_FULL, b, (r << lg) & 31);
+    if (need && gb < best) best = gb;
+    __syncwarp();  // qown is rewritten at the next leaf
   }
   __device__ __forceinline__ bool skip(int) const { return false; }
   __device__ __forceinline__ void visited(int) {}

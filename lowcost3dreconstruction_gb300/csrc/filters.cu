@@ -60,6 +60,7 @@ struct SorAcc {
   // E = exponent of sqrt(tau) - 150; a term shifted onto the grid stays below
   // 2^56 and k of them below 2^63 for k < 128 (the shift shrinks beyond).
   __device__ __forceinline__ void begin(float tau, int K) {
+    kcap = K;
     const int e = static_cast<int>(__float_as_uint(__fsqrt_rn(tau)) >> 23);
     int lg = 0;
     while ((1 << lg) < K) ++lg;
@@ -85,14 +86,17 @@ struct SorAcc {
       emin = min(emin, max(1, static_cast<int>(__float_as_uint(v) >> 23)));
     }
   }
-  // the neighbour list of the query (may be null): the keys as they come
+  // the neighbour list of the query (may be null): the keys as they come.  The
+  // k-set hands over exactly K keys; the write is bounded all the same, so that
+  // no error upstream can write past the list.
   unsigned long long* out;
+  int kcap = 0;
   __device__ __forceinline__ void add(const float4& p, float d) {
-    if (out) out[cnt] = make_key(d, __float_as_uint(p.w));
+    if (out && cnt < kcap) out[cnt] = make_key(d, __float_as_uint(p.w));
     add_d(d);
   }
   __device__ __forceinline__ void add_key(unsigned long long k) {
-    if (out) out[cnt] = k;
+    if (out && cnt < kcap) out[cnt] = k;
     add_d(key_dist(k));
   }
   // true if the ascending double sum is the exact one; s = that sum of all
@@ -411,9 +415,11 @@ struct NeAcc {
     syy += dy * dy; syz += dy * dz; szz += dz * dz;
     ++m;
   }
-  // p: a staged index point (w = original index), d its squared distance
+  // p: a staged index point (w = original index), d its squared distance.
+  // The k-set hands over exactly K <= kGraphMaxK points; the row write is
+  // bounded all the same, so that no error upstream can write past a row.
   __device__ __forceinline__ void add(const float4& p, float d) {
-    if (row) {
+    if (row && m < kGraphR) {
       row[m] = __float_as_uint(p.w);
       rmax = fmaxf(rmax, d);
     }
@@ -421,7 +427,7 @@ struct NeAcc {
   }
   __device__ __forceinline__ void begin(float, int) {}
   __device__ __forceinline__ void add_key(unsigned long long k) {
-    if (row) {
+    if (row && m < kGraphR) {
       row[m] = key_idx(k);
       rmax = fmaxf(rmax, key_dist(k));
     }

@@ -482,6 +482,7 @@ __device__ __forceinline__ void tile_nn1(const IndexView& ix, float qx, float qy
 // The result is the exact first k keys in (distance, index) order, in
 // list[j*32 + lane], j < k.
 constexpr int kLeafList = 192;
+constexpr int kSeedLeaves = 2;  // pass 1 first scans the query leaf and this many either side
 constexpr int kBins = 64;  // 16 octaves of d^2, 8 of distance
 
 __host__ __device__ constexpr int knn_buffer(int K) { return K + 32; }
@@ -630,7 +631,7 @@ struct KCollect {
         if (!(d <= tau)) continue;
         const unsigned long long k = make_key(d, st.i[j0 + u]);
         if (!insert) {
-          buf[cnt * 32 + lane] = k;
+          if (cnt < knn_buffer(K)) buf[cnt * 32 + lane] = k;  // fits by pass 1's count; bounded all the same
           ++cnt;
         } else if (k < buf[(K - 1) * 32 + lane]) {
           int pos = K - 1;
@@ -698,10 +699,11 @@ __device__ __forceinline__ void knn_pass1(const IndexView& ix, float qx, float q
   subtile_setup(qx, qy, qz, qv, kw.ws);
   h.refresh();
   if (self_leaf >= 0) {
-    h.seed_lo = max(0, self_leaf - 2);
-    h.seed_hi = min(ix.nleaf - 1, self_leaf + 2);
+    // the traversal skips exactly the leaves scanned here: one constant for both
+    h.seed_lo = max(0, self_leaf - kSeedLeaves);
+    h.seed_hi = min(ix.nleaf - 1, self_leaf + kSeedLeaves);
     h.scan_leaf(ix, self_leaf, kw.ws);
-    for (int d = 1; d <= 2; ++d) {
+    for (int d = 1; d <= kSeedLeaves; ++d) {
       if (self_leaf - d >= 0) h.scan_leaf(ix, self_leaf - d, kw.ws);
       if (self_leaf + d < ix.nleaf) h.scan_leaf(ix, self_leaf + d, kw.ws);
     }

@@ -5,10 +5,12 @@ Default workload (config 4): 512 pairs of synthetic depth images of the
 turntable object family (Kinect v1 640x480 uint16 mm and Kinect v2 512x424
 float32 mm, at the super-resolution tools' upsampling factors 1, 2 and 4;
 5k-500k points per view), resident in HBM.  One step = back-projection and
-NormalEstimation (k = 30) of all 1024 views, then the proposal arm (learned
-pose proposal, point-to-plane ICP 2 cm then 1 cm, plain ICP as the fallback)
-and, beside it, the plain arm (centroid alignment, point-to-plane ICP 5 cm
-then 1 cm), each over all pairs in batched ICP calls.  A pair counts as
+NormalEstimation (k = 30) of all 1024 views, dealt to 12 streams (the targets
+keep their neighbour rows for ICP), then the proposal arm (learned pose
+proposal, point-to-plane ICP 2 cm then 1 cm, plain ICP as the fallback, whose
+pairs known after the 2 cm stage run on a second context beside the 1 cm
+stage) and, beside it, the plain arm (centroid alignment, point-to-plane ICP
+5 cm then 1 cm), each over all pairs in batched ICP calls.  A pair counts as
 aligned when ICP converged and RMS |T_est p - T_gt p| over the source points
 is <= 1 mm.  value = aligned pairs/s of preprocessing + the proposal arm;
 e2e = the same from pinned host images (H2D inside the timed region).  L2 is

@@ -542,44 +542,44 @@ struct KHist {
   __device__ __forceinline__ bool need(const float4& lo, const float4& hi) const {
     return qv && box_dist2(lo, hi, qx, qy, qz) <= bound();
   }
+  // Every staged point updates the lane's histogram without a branch (adding
+  // 0 or 1 to its bin): a per-candidate branch ran for nearly every point,
+  // since some lane of the warp usually takes it.  The bound is the one at
+  // the start of the leaf and the top bins are dropped once after it.  The bin
+  // that holds the k-th key comes out the same as with per-candidate drops: a
+  // candidate above a bound that would have shrunk within the leaf lands in a
+  // bin that is dropped.  Only the open last bin's edge can come out larger,
+  // and it is still an upper bound on the k-th key, so the k-set is unchanged.
   static constexpr bool kSoa = true;
   __device__ __forceinline__ void scan(const SoaStage& st) {
-    float tau = bound();
+    const float tau = bound();
     const f32x2 qx2 = f32x2_dup(qx), qy2 = f32x2_dup(qy), qz2 = f32x2_dup(qz);
+    int add = 0;
+    float tm = top_max;
     for (int j0 = 0; j0 < 32; j0 += 4) {
-      // four independent distances first (paired FP32 from the staged
-      // coordinates), then the order-dependent histogram updates
       float dd[4];
       soa_dist4(st, j0, qx2, qy2, qz2, dd);
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-      const float d = dd[u];
-      if (!(d <= tau)) continue;
-      const int b = bin(d);
-      if (b == kBins - 1) top_max = fmaxf(top_max, d);
-      hist[b * 32 + lane] += 1u;
-      if (++cl >= K) {
-        // drop the top bins while the ones below still hold k candidates;
-        // the bound moves only when a bin is dropped, or when the k-th
-        // candidate first arrives (cl never falls below K after that, and with
-        // the last bin as the boundary, its edge top_max cannot grow: every
-        // accepted candidate lies at or below it)
-        const bool first = cl == K;
-        const int bs0 = bs;
+        const float d = dd[u];
+        const bool c = d <= tau;
+        const int b = bin(d);
+        hist[b * 32 + lane] += static_cast<uint32_t>(c);
+        tm = (c && b == kBins - 1) ? fmaxf(tm, d) : tm;
+        add += c;
+      }
+    }
+    top_max = tm;
+    if (add) {
+      cl += add;
+      if (cl >= K) {
         while (bs > 1) {
           const int top = static_cast<int>(hist[(bs - 1) * 32 + lane]);
           if (cl - top < K) break;
           cl -= top;
           --bs;
         }
-        if (first || bs != bs0) {
-          tau = fminf(edge(bs - 1), cap);
-          if (should_escape()) {
-            escape();
-            tau = -1.f;
-          }
-        }
-      }
+        if (should_escape()) escape();
       }
     }
   }

@@ -546,10 +546,12 @@ struct KHist {
   // 0 or 1 to its bin): a per-candidate branch ran for nearly every point,
   // since some lane of the warp usually takes it.  The bound is the one at
   // the start of the leaf and the top bins are dropped once after it.  The bin
-  // that holds the k-th key comes out the same as with per-candidate drops: a
-  // candidate above a bound that would have shrunk within the leaf lands in a
-  // bin that is dropped.  Only the open last bin's edge can come out larger,
-  // and it is still an upper bound on the k-th key, so the k-set is unchanged.
+  // that holds the k-th key, and every count below it, come out the same as
+  // with per-candidate drops: a candidate above a bound that would have shrunk
+  // within the leaf lands in a bin that is dropped.  When that bin is the open
+  // last one, its count and edge (its largest candidate) can come out larger;
+  // its range still holds the keys pass 2 selects from, so the k-set is
+  // unchanged (tests/test_kset_pass1_model.py models both forms).
   static constexpr bool kSoa = true;
   __device__ __forceinline__ void scan(const SoaStage& st) {
     const float tau = bound();

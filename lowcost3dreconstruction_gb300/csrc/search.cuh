@@ -585,6 +585,47 @@ struct KHist {
       }
     }
   }
+  // Warp-collective form (every lane calls it).  When exactly one lane needs
+  // the leaf (an escaped query searched alone, or a sparse corner of a tile),
+  // the warp scans it for that lane, one point per lane: the same distances,
+  // the same bound and the same 0-or-1 additions as scan(), so the same
+  // histogram state, in one step instead of 32.
+  static constexpr bool kWarpScan = true;
+  __device__ __forceinline__ void scan_warp(const SoaStage& st, bool need) {
+    const unsigned mask = __ballot_sync(LCR_FULL, need);
+    if (__popc(mask) != 1) {
+      if (need) scan(st);
+      return;
+    }
+    const int owner = __ffs(mask) - 1;
+    const float tau = __shfl_sync(LCR_FULL, bound(), owner);
+    const int eo = __shfl_sync(LCR_FULL, e0, owner);
+    const float x = __shfl_sync(LCR_FULL, qx, owner), y = __shfl_sync(LCR_FULL, qy, owner),
+                z = __shfl_sync(LCR_FULL, qz, owner);
+    const float d = exact_dist2(x, y, z, st.x[lane], st.y[lane], st.z[lane]);
+    const bool c = d <= tau;
+    const int b = min(max(static_cast<int>(__float_as_uint(d) >> 21) - eo, 0), kBins - 1);
+    if (c) atomicAdd(&hist[b * 32 + owner], 1u);
+    const int cnt = __popc(__ballot_sync(LCR_FULL, c));
+    // largest candidate in the last bin: non-negative floats order as their bits
+    const float tm = __uint_as_float(
+        __reduce_max_sync(LCR_FULL, (c && b == kBins - 1) ? __float_as_uint(d) : 0u));
+    __syncwarp();  // the additions before the owner reads its column
+    if (lane == owner && cnt > 0) {
+      top_max = fmaxf(top_max, tm);
+      cl += cnt;
+      if (cl >= K) {
+        while (bs > 1) {
+          const int top = static_cast<int>(hist[(bs - 1) * 32 + lane]);
+          if (cl - top < K) break;
+          cl -= top;
+          --bs;
+        }
+        if (should_escape()) escape();
+      }
+    }
+    __syncwarp();
+  }
   // Leaves [seed_lo, seed_hi] were scanned before the traversal.
   int seed_lo, seed_hi;
   __device__ __forceinline__ bool skip(int id) const { return id >= seed_lo && id <= seed_hi; }
